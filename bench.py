@@ -1,0 +1,328 @@
+"""Benchmark of the HII-bubble filter bank (one JSON line on rank 0).
+
+Workload (default): the batched form at 512^3 -- L = 300 Mpc/h, one
+redshift z = 7, 64 efficiency / Rmax parameter sets (zeta log-uniform on
+[10, 100], Rmax uniform on [10, 60] Mpc/h, radius factor 1.05, so radius
+counts are uneven), seeded synthetic density and SFRD boxes.  A step is one
+full stage pass: prologue, shared forward transform, every set's radius loop,
+dilation, fill and cap, giving 64 xHII boxes.
+
+metric: voxel*radii/s = N^3 * (radii summed over the sets) / step time.
+value : device-resident inputs, CUDA events on the launch stream.
+e2e   : the same through the host-buffer C-ABI call sf21_hii_run_z (pinned
+        host inputs copied in, 64 xHII boxes copied out, neutral fractions
+        summed on the host) -- the reference-facing path.
+--impl reference: the CPU restatement of get_HIIbubbles.c (oracle/, FFTW-API
+        shim, OpenMP on all host cores) timed on a bounded sample of the
+        workload (first parameter set, first radii).
+Multi-GPU (torchrun): independent replicas (each rank runs the full
+workload on its GPU; scaling "weak"), barrier + max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from simfast21_gb300 import params as P  # noqa: E402
+from simfast21_gb300 import synth  # noqa: E402
+
+
+# ---------------------------------------------------------------------------
+def workload(name: str):
+    """(N, L, z, sets, seed, label) of a named workload."""
+    h = 0.71
+    if name == "batched512":
+        N, L, z, seed = 512, 300.0, 7.0, 1236
+        rng = np.random.default_rng(seed)
+        zetas = np.exp(rng.uniform(np.log(10.0), np.log(100.0), 64))
+        rmaxs = rng.uniform(10.0, 60.0, 64)
+    elif name == "batched256":
+        N, L, z, seed = 256, 150.0, 7.0, 1236
+        rng = np.random.default_rng(seed)
+        zetas = np.exp(rng.uniform(np.log(10.0), np.log(100.0), 16))
+        rmaxs = rng.uniform(5.0, 30.0, 16)
+    elif name == "plain128":
+        N, L, z, seed = 128, 100.0, 8.0, 1234
+        zetas, rmaxs = np.array([30.0]), np.array([50.0])
+    else:
+        raise SystemExit(f"unknown workload {name}")
+    dx = L / N
+    sets = []
+    for zt, rm in zip(zetas, rmaxs):
+        # ini values are in Mpc (bubble_Rmax = Rmax/h); the stage multiplies by h
+        rmax = min((rm / h) * h, L / 2.0)
+        factor = 1.1 if name == "plain128" else 1.05
+        nb = max(1, int(round(math.log(rmax / dx) / math.log(factor))))
+        sets.append((float(zt), float(rmax), nb))
+    return dict(N=N, L=L, z=z, hubble=h, sets=sets, seed=seed, name=name)
+
+
+def describe(w):
+    return {"batched512": "HII filter bank, batched: 512^3, L=300 Mpc/h, z=7, 64 sets "
+                          "(zeta log-U[10,100], Rmax U[10,60] Mpc/h, factor 1.05)",
+            "batched256": "HII filter bank, batched: 256^3, L=150 Mpc/h, z=7, 16 sets",
+            "plain128": "HII filter bank: 128^3, L=100 Mpc/h, z=8, zeta=30, Rmax=50, factor 1.1"}[w["name"]]
+
+
+def total_radii(w):
+    return sum(len(P.radii(s[1], w["L"] / w["N"], s[2])[0]) for s in w["sets"])
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for i, n in enumerate(names):
+                if len(r) > 5 + i and r[5 + i].lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(self.rows), "reasons": sorted(reasons)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+def cpu_sample(w, n_radii: int, nthreads: int):
+    """CPU restatement on the first parameter set, first n_radii radii."""
+    from oracle import oracle as O
+    O.build()
+    N = w["N"]
+    zt, rmax, nb = w["sets"][0]
+    delta, sfrd = synth.make_boxes(synth.Workload(N=N, L=w["L"], zs=[w["z"]], seed=w["seed"]), w["z"])
+    p = O.params(N, w["L"], w["hubble"], rmax, nb, zt, nthreads=nthreads, max_radii=n_radii)
+    t0 = time.perf_counter()
+    O.run_z_sfr(p, w["z"], delta, sfrd)
+    dt = time.perf_counter() - t0
+    return float(N) ** 3 * n_radii / dt, dt
+
+
+def run_reference(args, w, rank):
+    if rank != 0:
+        return
+    ncpu = os.cpu_count() or 1
+    n_radii = 2 if w["N"] >= 512 else 4
+    for _ in range(args.warmup):
+        cpu_sample(w, n_radii, ncpu)
+    vals, times = [], []
+    for _ in range(args.steps):
+        v, dt = cpu_sample(w, n_radii, ncpu)
+        vals.append(v)
+        times.append(dt)
+    v = float(np.mean(vals))
+    sample = (f"first parameter set, first {n_radii} radii (FFT branch) of the {w['N']}^3 box, "
+              f"prologue and forward transforms included")
+    print(json.dumps({
+        "impl": "reference", "metric": "HII filter-bank voxel*radii/s", "value": v,
+        "unit": "voxel*radii/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * float(np.mean(times)), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": describe(w), "flush": "inputs larger than L2"},
+        "cpu_baseline": {"value": v, "unit": "voxel*radii/s", "cores": ncpu, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": v, "unit": "voxel*radii/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+# ---------------------------------------------------------------------------
+def run_ours(args, w, rank, world):
+    import torch
+    from simfast21_gb300 import build as B
+    from simfast21_gb300 import hii
+
+    B.build()
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    N = w["N"]
+    n3 = N ** 3
+    nsets = len(w["sets"])
+    delta, sfrd = synth.make_boxes(synth.Workload(N=N, L=w["L"], zs=[w["z"]], seed=w["seed"]), w["z"])
+    fb = hii.FilterBank(N, w["L"], w["hubble"], w["sets"], device=dev)
+    R_total = sum(len(fb.radii(s)[0]) for s in range(nsets))
+    units = float(n3) * R_total
+    d_delta = torch.from_numpy(delta).cuda()
+    d_src = torch.from_numpy(sfrd).cuda()
+    d_x = torch.empty((nsets, N, N, N), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+
+    def step():
+        fb.run_z_device(w["z"], d_delta.data_ptr(), d_src.data_ptr(), d_x.data_ptr(), stream=sptr)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    fb.profile(True)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    prof = fb.profile_read()
+    fb.profile(False)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = units * world / (ms / 1e3)
+
+    # e2e through the host-buffer C-ABI call
+    h_delta = torch.from_numpy(delta).pin_memory().numpy()
+    h_src = torch.from_numpy(sfrd).pin_memory().numpy()
+    e2e_steps = max(1, min(args.steps, 2))
+    fb.run_z(w["z"], h_delta, h_src)  # warm (allocates nothing new)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        x, neutral = fb.run_z(w["z"], h_delta, h_src)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    barrier()
+    e2e_val = units * world / e2e_s
+
+    # roofline of the dominant kernel kind (largest device-time share)
+    hbm, peak_kind = peaks()
+    steps = args.steps
+    kinds = {k: v for k, v in prof.items() if v[1] > 0}
+    dom = max(kinds, key=lambda k: kinds[k][0])
+    dom_ms, dom_n = kinds[dom]
+    per_launch_ms = dom_ms / dom_n
+    # algorithmic bytes per launch (complex64 boxes: 8 B per voxel)
+    K_avg = R_total / (kinds.get("inv_rows_filter", (0, 1))[1] / steps)
+    alg = {
+        "inv_rows_filter": n3 * 8.0 * (1 + K_avg),      # spectrum read once, K boxes written
+        "inv_cols_b": n3 * 16.0 * K_avg,                 # K boxes read + written
+        "inv_cols_a_test": n3 * (8.0 * K_avg + 2.0),     # K boxes read, first-hit byte r/w
+    }.get(dom, None)
+    achieved = alg / (per_launch_ms / 1e3) / 1e9 if alg else None
+    # whole radius pipeline against the 16 B per voxel*radius algorithmic traffic
+    pipe_ms = sum(kinds.get(k, (0, 0))[0] for k in ("inv_rows_filter", "inv_cols_b", "inv_cols_a_test"))
+    pipe_gbs = 16.0 * units * steps / (pipe_ms / 1e3) / 1e9 if pipe_ms else None
+
+    # plain-form and CPU baseline (rank 0 only)
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        ncpu = os.cpu_count() or 1
+        n_radii = 2 if N >= 512 else 4
+        v, dt = cpu_sample(w, n_radii, ncpu)
+        cpu = {"value": v, "unit": "voxel*radii/s", "cores": ncpu, "kind": "port",
+               "sample": f"CPU restatement of get_HIIbubbles.c (FFTW-API shim, OpenMP), first parameter "
+                         f"set, first {n_radii} radii of the {N}^3 box incl. prologue+forward FFTs, "
+                         f"{dt:.1f} s"}
+
+    launches = int(sum(v[1] for v in kinds.values()) // steps)
+    if rank == 0:
+        out = {
+            "metric": "HII filter-bank voxel*radii/s (batched)",
+            "value": value, "unit": "voxel*radii/s", "n_gpus": world, "steps": steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded lognormal density + SFRD boxes)",
+            "config": {"workload": describe(w), "N": N, "sets": nsets, "radii_total": R_total,
+                       "flush": "inputs larger than L2 (every box >= 537 MB)"},
+            "e2e": {"value": e2e_val, "unit": "voxel*radii/s",
+                    "h2d_bytes_per_step": 2 * 4 * n3, "d2h_bytes_per_step": nsets * 4 * n3},
+            "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
+                         "unit": "GB/s", "frac": (achieved / hbm) if achieved else None,
+                         "peak_source": peak_kind, "traffic": None,
+                         "pipeline_16B_per_voxel_radius_gbs": pipe_gbs,
+                         "pipeline_frac": (pipe_gbs / hbm) if pipe_gbs else None},
+            "kernels_ms_per_step": {k: round(v[0] / steps, 3) for k, v in kinds.items()},
+            "clocks": clk.summary(),
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="batched512")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    w = workload(args.workload)
+    if args.impl == "reference":
+        run_reference(args, w, rank)
+        return
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl")
+    run_ours(args, w, rank, world)
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

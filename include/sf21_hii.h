@@ -1,0 +1,129 @@
+/*
+ * sf21_hii.h -- C-ABI of the GB300 HII-bubble filter bank (libsf21hii.so).
+ *
+ * Drop-in for the compute of SimFast21's get_HIIbubbles stage.  The stage's
+ * executable keeps its I/O (simfast21.ini, delta/SFR/Halos boxes in,
+ * Ionization/xHII boxes and text files out: get_HIIbubbles.c:63-96, 209-213,
+ * 236-246, 263-267, 473-528); what it did in-process with FFTW plans and
+ * OpenMP loops (get_HIIbubbles.c:98-194 and :215-471) is done behind these
+ * entry points on one GPU.  Plain C types only; host buffers belong to the
+ * caller, device buffers to the library (except in the *_device calls).
+ *
+ * Errors are returned as status codes (the reference printf()s and exit(1)s,
+ * e.g. get_HIIbubbles.c:102-191); sf21_hii_last_error() gives the message.
+ * A context is not thread-safe: one thread at a time per context.
+ */
+#ifndef SF21_HII_H
+#define SF21_HII_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SF21_HII_ABI_VERSION 1
+
+enum sf21_status {
+  SF21_OK = 0,
+  SF21_E_ARG = 1,         /* invalid argument (size, pointer, parameter)    */
+  SF21_E_ALLOC = 2,       /* device or host allocation failed              */
+  SF21_E_CUDA = 3,        /* CUDA runtime error                            */
+  SF21_E_TIMEOUT = 4,     /* a bounded device wait expired                 */
+  SF21_E_UNSUPPORTED = 5  /* configuration not supported (e.g. N not 2^k)  */
+};
+
+/* Source box kinds: what the caller passes as `src`.
+ *  SF21_SRC_SFRD: SFRD box [Msun/(Mpc/h)^3/yr] (use_SFR = T), converted as
+ *                 src*dx*dx*dx*Qion(z)*fesc   (get_HIIbubbles.c:272-274)
+ *  SF21_SRC_RION: Rion box after CIC and smooth_box (use_SFR = F), converted
+ *                 as src*pow(dx_s/dx_h,3)*fesc (get_HIIbubbles.c:257-259) */
+enum sf21_src_kind { SF21_SRC_SFRD = 0, SF21_SRC_RION = 1 };
+
+/* One efficiency / maximum-radius parameter set (the reference's fesc,
+ * bubble_Rmax and bubble_Nbins after Input_variables.c:123-124). */
+typedef struct {
+  double fesc;   /* zeta (global_fesc)                                   */
+  double Rmax;   /* global_bubble_Rmax in Mpc/h, already clamped to L/2  */
+  int Nbins;     /* global_bubble_Nbins                                  */
+} sf21_hii_set;
+
+typedef struct {
+  long N;            /* global_N_smooth: power of two, 16..1024            */
+  long N_halo;       /* global_N_halo (only for SF21_SRC_RION)             */
+  double L;          /* global_L in Mpc/h (after the *h of Input_variables.c:121) */
+  double hubble;     /* global_hubble                                       */
+  int device;        /* CUDA device ordinal                                 */
+  int nsets;         /* parameter sets sharing each forward transform (>=1) */
+  const sf21_hii_set *sets;
+  int kmax;          /* radii per spectrum read (0 = automatic, <= 8)       */
+} sf21_hii_config;
+
+typedef struct sf21_hii_ctx sf21_hii_ctx;
+
+/* Allocation, twiddle tables and per-set radius lists.
+ * Replaces get_HIIbubbles.c:98-194 (fftwf_malloc of the boxes, the seven
+ * FFTW_MEASURE plans, bfactor and the radius schedule of :298-461). */
+int sf21_hii_create(const sf21_hii_config *cfg, sf21_hii_ctx **out);
+
+/* Releases everything (get_HIIbubbles.c:530-541). */
+int sf21_hii_destroy(sf21_hii_ctx *ctx);
+
+/* Message of the last failing call on ctx (or of the last failed create
+ * when ctx is NULL).  Replaces the printf() before exit(1). */
+const char *sf21_hii_last_error(const sf21_hii_ctx *ctx);
+
+/* One redshift, host buffers: the body of the redshift loop,
+ * get_HIIbubbles.c:215-477 (prologue, source conversion, single-cell fill,
+ * forward transforms, both radius loops, cap, neutral fraction).
+ * delta, src: N^3 float (C order) as read from the deltanl and SFR/Rion files.
+ * xhii: nsets * N^3 floats, set-major, each box in the byte layout the
+ * reference writes to Ionization/xHII_*.dat (:485).
+ * neutral: nsets doubles (may be NULL): the serial double mean of 1 - xHII
+ * in the reference's order (:473-477). */
+int sf21_hii_run_z(sf21_hii_ctx *ctx, double z, int src_kind, const float *delta,
+                   const float *src, float *xhii, double *neutral);
+
+/* Same with device-resident buffers (no host copies); stream is a
+ * cudaStream_t (NULL = the context's stream).  The call returns after
+ * enqueueing; synchronise the stream before reading xhii. */
+int sf21_hii_run_z_device(sf21_hii_ctx *ctx, double z, int src_kind, const float *delta_dev,
+                          const float *src_dev, float *xhii_dev, void *stream);
+
+/* Radius list of a set exactly as the reference iterates it (:192, 298-461):
+ * writes up to cap radii (Mpc/h, descending), returns the count (or <0 on
+ * error); *n_fft receives how many take the FFT branch (R >= 2 dx). */
+int sf21_hii_radii(const sf21_hii_ctx *ctx, int set, double *R, int cap, int *n_fft);
+
+/* Check hooks.  Prologue outputs of one redshift for set `set`: the
+ * recombination-rate box (:222), the residual neutral fraction (:220-221)
+ * and the single-cell fill (:281-288); any pointer may be NULL. */
+int sf21_hii_prologue(sf21_hii_ctx *ctx, double z, int src_kind, const float *delta,
+                      const float *src, int set, float *rec0, float *fresid, float *fill0);
+
+/* Filtered fields at radius index ridx of set `set`: rec_R and ion_R as the
+ * reference's unnormalised c2r outputs hold them (:324-325). */
+int sf21_hii_filtered(sf21_hii_ctx *ctx, double z, int src_kind, const float *delta,
+                      const float *src, int set, int ridx, float *rec_R, float *ion_R);
+
+/* First-hit radius index per voxel of set `set` after the radius loops
+ * (0xFF = never a bubble centre): the largest R at which the voxel passes
+ * the centre test of :339-348 / :437-438. */
+int sf21_hii_first_hit(sf21_hii_ctx *ctx, double z, int src_kind, const float *delta,
+                       const float *src, int set, uint8_t *rc);
+
+/* Measurement hooks.  sf21_hii_profile(ctx, 1) starts recording CUDA events
+ * around every kernel the context launches (on its launch stream) and clears
+ * the totals; sf21_hii_profile_read() synchronises and returns the number of
+ * kernel kinds K, filling ms[k] (summed device time) and launches[k] for
+ * k < min(K, cap); sf21_hii_profile_name(k) names kind k.  No reference
+ * counterpart (the reference has no timers, get_HIIbubbles.c:193-195). */
+int sf21_hii_profile(sf21_hii_ctx *ctx, int enable);
+int sf21_hii_profile_read(sf21_hii_ctx *ctx, double *ms, long *launches, int cap);
+const char *sf21_hii_profile_name(int kind);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

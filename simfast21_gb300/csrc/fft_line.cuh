@@ -1,0 +1,154 @@
+// Batched 1D complex FFT of a power-of-two length N (16 <= N <= 1024) held
+// by N/8 threads of a CTA, 8 elements per thread.
+//
+// Stockham autosort with radix-8 stages and one radix-2 or radix-4 tail:
+//   stage with Ns = product of earlier radices:
+//     v[r] = x[j + r N/R] * w^((j mod Ns) r N/(Ns R)),   V = DFT_R(v),
+//     x'[(j/Ns) Ns R + (j mod Ns) + r Ns] = V[r]
+// The first stage takes its inputs from registers and the last stage leaves
+// its outputs in registers, in the same ownership: on entry and on exit
+// thread j holds elements j + r N/8 (r = 0..7) of its line, so global loads
+// and stores of a line are coalesced across the threads of a warp.  Only the
+// exchanges between stages go through shared memory (one float2 per element,
+// padded index n + n/16 to keep the strided stage stores at most 2-way
+// bank-conflicted).
+//
+// Twiddles come from a table tw[t] = exp(-2 pi i t / N) computed in double on
+// the host; the inverse transform uses the conjugates.  Transforms are
+// unnormalised (forward sign -1, inverse +1), the FFTW convention the
+// reference relies on (get_HIIbubbles.c:110-183).
+#pragma once
+#include <cuda_runtime.h>
+
+namespace sf21 {
+
+__host__ __device__ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n / 2); }
+
+__device__ __forceinline__ int padx(int n) { return n + (n >> 4); }
+
+template <int N>
+struct LineGeom {
+  static constexpr int LOG = ilog2c(N);
+  static constexpr int T = N / 8;                    // threads per line
+  static constexpr int LS = N + N / 16 + 1;          // float2 per line (odd)
+  static_assert((N & (N - 1)) == 0 && N >= 16 && N <= 1024, "N must be a power of two in [16, 1024]");
+};
+
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// multiply by -i (forward) or +i (inverse)
+template <bool INV>
+__device__ __forceinline__ float2 mul_mi(float2 a) {
+  return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
+}
+
+template <bool INV>
+__device__ __forceinline__ void dft4(float2& a0, float2& a1, float2& a2, float2& a3) {
+  float2 t0 = cadd(a0, a2), t1 = csub(a0, a2);
+  float2 t2 = cadd(a1, a3), t3 = mul_mi<INV>(csub(a1, a3));
+  a0 = cadd(t0, t2);
+  a2 = csub(t0, t2);
+  a1 = cadd(t1, t3);
+  a3 = csub(t1, t3);
+}
+
+template <bool INV>
+__device__ __forceinline__ void dft8(float2 (&v)[8]) {
+  const float h = 0.70710678118654752440f;
+  // DIT: E = DFT4(v0,v2,v4,v6), O = DFT4(v1,v3,v5,v7)
+  float2 e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
+  float2 o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
+  dft4<INV>(e0, e1, e2, e3);
+  dft4<INV>(o0, o1, o2, o3);
+  // twiddles w8^k, w8 = exp(-/+ i pi/4)
+  float2 w1o, w2o, w3o;
+  if (!INV) {
+    w1o = make_float2(h * (o1.x + o1.y), h * (o1.y - o1.x));
+    w2o = make_float2(o2.y, -o2.x);
+    w3o = make_float2(h * (o3.y - o3.x), -h * (o3.x + o3.y));
+  } else {
+    w1o = make_float2(h * (o1.x - o1.y), h * (o1.x + o1.y));
+    w2o = make_float2(-o2.y, o2.x);
+    w3o = make_float2(-h * (o3.x + o3.y), h * (o3.x - o3.y));
+  }
+  v[0] = cadd(e0, o0);
+  v[4] = csub(e0, o0);
+  v[1] = cadd(e1, w1o);
+  v[5] = csub(e1, w1o);
+  v[2] = cadd(e2, w2o);
+  v[6] = csub(e2, w2o);
+  v[3] = cadd(e3, w3o);
+  v[7] = csub(e3, w3o);
+}
+
+template <bool INV>
+__device__ __forceinline__ float2 twid(const float2* tw, int t) {
+  float2 w = tw[t];
+  if (INV) w.y = -w.y;
+  return w;
+}
+
+// One line: s = this line's shared-memory slice (LineGeom<N>::LS float2),
+// tw = shared or global twiddle table of N entries, j = thread index in line.
+// All threads of the CTA must call it together (it synchronises the CTA).
+template <int N, bool INV>
+__device__ __forceinline__ void fft_line(float2 (&v)[8], float2* s, const float2* tw, int j) {
+  constexpr int LOG = LineGeom<N>::LOG;
+  constexpr int Q = LOG / 3;
+  constexpr int RB = LOG % 3;
+  constexpr int N8 = N / 8;
+  int Ns = 1;
+#pragma unroll
+  for (int st = 0; st < Q; ++st) {
+    if (st > 0) {
+#pragma unroll
+      for (int r = 0; r < 8; ++r) v[r] = s[padx(j + r * N8)];
+      const int jm = j & (Ns - 1);
+      const int step = N / (8 * Ns);
+#pragma unroll
+      for (int r = 1; r < 8; ++r) v[r] = cmul(v[r], twid<INV>(tw, jm * r * step));
+    }
+    dft8<INV>(v);
+    const bool keep = (st == Q - 1) && (RB == 0);
+    if (!keep) {
+      __syncthreads();
+      const int base = (j / Ns) * Ns * 8 + (j & (Ns - 1));
+#pragma unroll
+      for (int r = 0; r < 8; ++r) s[padx(base + r * Ns)] = v[r];
+      __syncthreads();
+    }
+    Ns *= 8;
+  }
+  if (RB == 1) {
+    // radix-2 tail, Ns = N/2: butterflies j2 = j + m N/8, m = 0..3
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      const int j2 = j + m * N8;
+      float2 a = s[padx(j2)];
+      float2 b = cmul(s[padx(j2 + N / 2)], twid<INV>(tw, j2));
+      v[m] = cadd(a, b);
+      v[m + 4] = csub(a, b);
+    }
+  } else if (RB == 2) {
+    // radix-4 tail, Ns = N/4: butterflies j4 in {j, j + N/8}
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int j4 = j + h * N8;
+      float2 a0 = s[padx(j4)];
+      float2 a1 = cmul(s[padx(j4 + N / 4)], twid<INV>(tw, j4));
+      float2 a2 = cmul(s[padx(j4 + N / 2)], twid<INV>(tw, 2 * j4));
+      float2 a3 = cmul(s[padx(j4 + 3 * N / 4)], twid<INV>(tw, 3 * j4));
+      dft4<INV>(a0, a1, a2, a3);
+      // outputs j4 + r N/4 -> register j + (2r + h) N/8
+      v[0 + h] = a0;
+      v[2 + h] = a1;
+      v[4 + h] = a2;
+      v[6 + h] = a3;
+    }
+  }
+}
+
+}  // namespace sf21

@@ -1,0 +1,548 @@
+// C-ABI of the HII filter bank (include/sf21_hii.h): context, device
+// buffers, per-redshift scalars and the launch schedule.
+//
+// Schedule of one redshift (get_HIIbubbles.c:215-471), all on one stream:
+//   prologue            rec0, fresid, packed (rec0, ion)   (:216-225, :272-274)
+//   alpha               norm balance of the packed transform
+//   forward 3D FFT      spectrum of the packed box          (:290-291)
+//   for each set:
+//     rc := none
+//     for each batch of up to K radii (descending R):     (:298-461)
+//       c-axis inverse with the top-hat filter of K radii -> K work boxes
+//       b-axis inverse of the K boxes
+//       a-axis inverse + centre test + first-hit update of rc
+//     dilation of the first-hit field + single-cell fill + cap -> xHII (:281-288, :358-393, :427-458, :466-471)
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/sf21_hii.h"
+#include "sf21_kernels.h"
+
+using namespace sf21;
+
+namespace {
+
+const double kPI = 3.1415926535897932385E0;  // Input_variables.h:10
+const double kCM_PER_MPC = 3.0857e24;         // user_functions.c:26
+
+uint64_t dbits(double d) {
+  uint64_t u;
+  memcpy(&u, &d, 8);
+  return u;
+}
+
+// ---- per-redshift scalars, evaluated on the host with the C library's pow
+// and in the reference's operation order (user_functions.c:59-97) ---------
+double host_G_H(double z) {
+  double lo = -4.37152818e-05 * pow(z, 5.) + 1.64394635e-03 * pow(z, 4.) -
+              2.03044756e-02 * pow(z, 3.);
+  double hi = 7.18335221e-02 * pow(z, 2.) - 8.85791388e-02 * z - 1.20887500e+01;
+  return 4.19232273531e-13 / pow(10.0, lo + hi);
+}
+double host_Qion(double z) { return pow(10.0, 2.05707274e-02 * z + 5.29944413e+01) / 1.e+45; }
+
+struct SetInfo {
+  double fesc, Rmax;
+  int Nbins;
+  std::vector<double> R;     // radii, loop order
+  int n_fft;                 // radii with R >= 2 dx
+  std::vector<int> nmax;     // largest n with sqrt(n)*dx <= R
+  int vmax;
+  int* d_nmax = nullptr;
+};
+
+}  // namespace
+
+struct sf21_hii_ctx {
+  int device = 0;
+  long N = 0, N_halo = 0, n3 = 0;
+  double L = 0, hubble = 0, dx = 0, dk = 0;
+  int K = 8;
+  std::vector<SetInfo> sets;
+  cudaStream_t stream = nullptr;
+  float *d_delta = nullptr, *d_src = nullptr, *d_rec0 = nullptr, *d_fres = nullptr;
+  float *d_partials = nullptr, *d_alpha = nullptr, *d_xhii = nullptr;
+  float2 *d_spec = nullptr, *d_tw = nullptr;
+  std::vector<float2*> d_work;
+  uint8_t* d_rc = nullptr;
+  PrologueArgs* d_pa = nullptr;
+  int pro_blocks = 0;
+  std::string err;
+  // optional per-kernel timing (CUDA events on the launch stream)
+  bool prof = false;
+  std::vector<cudaEvent_t> ev;
+  size_t ev_used = 0;
+  struct Span { int kind, a, b; };
+  std::vector<Span> spans;
+  double prof_ms[16] = {0};
+  long prof_n[16] = {0};
+};
+
+// Kernel kinds reported by sf21_hii_profile_read, in this order.
+static const char* kKindNames[] = {"prologue", "alpha", "fwd_rows", "fwd_cols_b", "fwd_cols_a",
+                                   "inv_rows_filter", "inv_cols_b", "inv_cols_a_test", "dt_rows",
+                                   "dt_b", "dt_a_finish"};
+enum { KD_PRO, KD_ALPHA, KD_FROWS, KD_FCB, KD_FCA, KD_IROWS, KD_ICB, KD_ICA, KD_DTR, KD_DTB, KD_DTA, KD_COUNT };
+
+// Records an event on st when timing is on; returns its index (or -1).
+static int mark(sf21_hii_ctx* c, cudaStream_t st) {
+  if (!c->prof) return -1;
+  if (c->ev_used == c->ev.size()) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) return -1;
+    c->ev.push_back(e);
+  }
+  cudaEventRecord(c->ev[c->ev_used], st);
+  return (int)c->ev_used++;
+}
+static void span(sf21_hii_ctx* c, int kind, int a, int b) {
+  if (c->prof && a >= 0 && b >= 0) c->spans.push_back({kind, a, b});
+}
+
+static std::string g_create_err;
+
+#define CTX_FAIL(ctx, code, ...)                                  \
+  do {                                                            \
+    char _b[512];                                                 \
+    snprintf(_b, sizeof(_b), __VA_ARGS__);                        \
+    (ctx)->err = _b;                                              \
+    return (code);                                                \
+  } while (0)
+
+#define CTX_CUDA(ctx, call)                                                                  \
+  do {                                                                                       \
+    cudaError_t _e = (call);                                                                 \
+    if (_e != cudaSuccess)                                                                   \
+      CTX_FAIL(ctx, SF21_E_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(_e), \
+               __FILE__, __LINE__);                                                          \
+  } while (0)
+
+static int nmax_of(double R, double dx) {
+  long n = (long)floor((R / dx) * (R / dx));
+  if (n < 0) n = 0;
+  while (n > 0 && !(sqrt((double)n) * dx <= R)) --n;
+  while (sqrt((double)(n + 1)) * dx <= R) ++n;
+  return (int)n;
+}
+
+static void build_set(SetInfo& s, double dx) {
+  // bfactor (:192) and the two loops (:299, :397, :402, :461)
+  const double b = pow(10.0, log10(s.Rmax / dx) / s.Nbins);
+  double R = s.Rmax;
+  s.R.clear();
+  while (R >= 2 * dx) {
+    s.R.push_back(R);
+    R /= b;
+  }
+  s.n_fft = (int)s.R.size();
+  while (R >= dx) {
+    s.R.push_back(R);
+    R /= b;
+  }
+  s.nmax.resize(s.R.size());
+  s.vmax = 0;
+  for (size_t i = 0; i < s.R.size(); ++i) {
+    s.nmax[i] = nmax_of(s.R[i], dx);
+    if (s.nmax[i] > s.vmax) s.vmax = s.nmax[i];
+  }
+}
+
+static void free_ctx(sf21_hii_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  void* ptrs[] = {c->d_delta, c->d_src, c->d_rec0, c->d_fres, c->d_partials, c->d_alpha,
+                  c->d_xhii, c->d_spec, c->d_tw, c->d_rc, c->d_pa};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  for (float2* w : c->d_work)
+    if (w) cudaFree(w);
+  for (SetInfo& s : c->sets)
+    if (s.d_nmax) cudaFree(s.d_nmax);
+  for (cudaEvent_t e : c->ev) cudaEventDestroy(e);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+static int prologue_args(sf21_hii_ctx* c, double z, int kind, PrologueArgs* pa) {
+  memset(pa, 0, sizeof(*pa));
+  pa->one_plus_z_cubed = dbits(pow(1. + z, 3.0));
+  pa->g_h = dbits(host_G_H(z));
+  pa->rec1 = dbits(1.e-24 * 9.84815696 * pow((1.0 + z), 5.06773134));
+  pa->dvv = dbits(pow(c->L * kCM_PER_MPC / c->N / c->hubble / (1. + z), 3.0));
+  pa->c_resid = dbits(1.881e-7);
+  pa->r2 = dbits(1.76105133);
+  pa->r3 = dbits(0.81722878);
+  pa->v_norm = dbits(1.e+45);
+  if (kind == SF21_SRC_SFRD) {
+    // halo_map*dx*dx*dx*Qion(z) [*fesc]  (:273)
+    pa->src_mul[0] = pa->src_mul[1] = pa->src_mul[2] = dbits(c->dx);
+    pa->src_mul[3] = dbits(host_Qion(z));
+    pa->n_src_mul = 4;
+  } else if (kind == SF21_SRC_RION) {
+    // halo_map*pow(dx_s/dx_h,3) [*fesc]  (:258)
+    const double dxh = c->L / c->N_halo;
+    pa->src_mul[0] = dbits(pow(c->dx / dxh, 3));
+    pa->n_src_mul = 1;
+  } else {
+    CTX_FAIL(c, SF21_E_ARG, "unknown src_kind %d", kind);
+  }
+  return SF21_OK;
+}
+
+extern "C" int sf21_hii_create(const sf21_hii_config* cfg, sf21_hii_ctx** out) {
+  if (!out) return SF21_E_ARG;
+  *out = nullptr;
+  g_create_err.clear();
+  if (!cfg || cfg->nsets < 1 || !cfg->sets) {
+    g_create_err = "config must have nsets >= 1 and a sets array";
+    return SF21_E_ARG;
+  }
+  const long N = cfg->N;
+  if (N < 16 || N > 1024 || (N & (N - 1))) {
+    g_create_err = "N_smoothed must be a power of two between 16 and 1024";
+    return SF21_E_UNSUPPORTED;
+  }
+  if (!(cfg->L > 0) || !(cfg->hubble > 0)) {
+    g_create_err = "L and hubble must be positive";
+    return SF21_E_ARG;
+  }
+  sf21_hii_ctx* c = new sf21_hii_ctx();
+  c->device = cfg->device;
+  c->N = N;
+  c->N_halo = cfg->N_halo > 0 ? cfg->N_halo : N;
+  c->n3 = N * N * N;
+  c->L = cfg->L;
+  c->hubble = cfg->hubble;
+  c->dx = cfg->L / N;                 // Input_variables.c:129
+  c->dk = 2 * kPI / cfg->L;           // Input_variables.c:127
+  for (int s = 0; s < cfg->nsets; ++s) {
+    SetInfo si;
+    si.fesc = cfg->sets[s].fesc;
+    si.Rmax = cfg->sets[s].Rmax;
+    si.Nbins = cfg->sets[s].Nbins;
+    if (si.Nbins < 1 || !(si.Rmax > 0) || !(si.fesc >= 0)) {
+      g_create_err = "set " + std::to_string(s) + ": need Nbins >= 1, Rmax > 0, fesc >= 0";
+      delete c;
+      return SF21_E_ARG;
+    }
+    build_set(si, c->dx);
+    if (si.R.size() > 254) {
+      g_create_err = "set " + std::to_string(s) + ": more than 254 radii";
+      delete c;
+      return SF21_E_UNSUPPORTED;
+    }
+    c->sets.push_back(si);
+  }
+  const size_t box_c = sizeof(float2) * c->n3, box_f = sizeof(float) * c->n3;
+  int K = cfg->kmax > 0 ? cfg->kmax : KMAX;
+  if (K > KMAX) K = KMAX;
+  c->K = K;
+#define CREATE_CUDA(call)                                                                   \
+  do {                                                                                      \
+    cudaError_t _e = (call);                                                                \
+    if (_e != cudaSuccess) {                                                                \
+      g_create_err = std::string(#call) + " failed: " + cudaGetErrorString(_e);             \
+      free_ctx(c);                                                                          \
+      return _e == cudaErrorMemoryAllocation ? SF21_E_ALLOC : SF21_E_CUDA;                  \
+    }                                                                                       \
+  } while (0)
+  CREATE_CUDA(cudaSetDevice(c->device));
+  CREATE_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  CREATE_CUDA(fft_setup((int)N));
+  CREATE_CUDA(dilate_setup((int)N));
+  CREATE_CUDA(cudaMalloc(&c->d_delta, box_f));
+  CREATE_CUDA(cudaMalloc(&c->d_src, box_f));
+  CREATE_CUDA(cudaMalloc(&c->d_rec0, box_f));
+  CREATE_CUDA(cudaMalloc(&c->d_fres, box_f));
+  CREATE_CUDA(cudaMalloc(&c->d_xhii, box_f));
+  CREATE_CUDA(cudaMalloc(&c->d_spec, box_c));
+  CREATE_CUDA(cudaMalloc(&c->d_rc, c->n3));
+  c->d_work.assign(K, nullptr);
+  for (int k = 0; k < K; ++k) CREATE_CUDA(cudaMalloc(&c->d_work[k], box_c));
+  c->pro_blocks = prologue_blocks(c->n3);
+  CREATE_CUDA(cudaMalloc(&c->d_partials, sizeof(float) * 2 * c->pro_blocks));
+  CREATE_CUDA(cudaMalloc(&c->d_alpha, sizeof(float)));
+  CREATE_CUDA(cudaMalloc(&c->d_pa, sizeof(PrologueArgs)));
+  // twiddles exp(-2 pi i t / N) in double, rounded once
+  std::vector<float2> tw(N);
+  for (long t = 0; t < N; ++t) {
+    const double a = -2.0 * kPI * (double)t / (double)N;
+    tw[t] = make_float2((float)cos(a), (float)sin(a));
+  }
+  CREATE_CUDA(cudaMalloc(&c->d_tw, sizeof(float2) * N));
+  CREATE_CUDA(cudaMemcpy(c->d_tw, tw.data(), sizeof(float2) * N, cudaMemcpyHostToDevice));
+  for (SetInfo& s : c->sets) {
+    CREATE_CUDA(cudaMalloc(&s.d_nmax, sizeof(int) * s.nmax.size()));
+    CREATE_CUDA(cudaMemcpy(s.d_nmax, s.nmax.data(), sizeof(int) * s.nmax.size(), cudaMemcpyHostToDevice));
+  }
+#undef CREATE_CUDA
+  *out = c;
+  return SF21_OK;
+}
+
+extern "C" int sf21_hii_destroy(sf21_hii_ctx* ctx) {
+  free_ctx(ctx);
+  return SF21_OK;
+}
+
+extern "C" const char* sf21_hii_last_error(const sf21_hii_ctx* ctx) {
+  return ctx ? ctx->err.c_str() : g_create_err.c_str();
+}
+
+extern "C" int sf21_hii_radii(const sf21_hii_ctx* ctx, int set, double* R, int cap, int* n_fft) {
+  if (!ctx || set < 0 || set >= (int)ctx->sets.size()) return -SF21_E_ARG;
+  const SetInfo& s = ctx->sets[set];
+  for (int i = 0; i < (int)s.R.size() && i < cap; ++i) R[i] = s.R[i];
+  if (n_fft) *n_fft = s.n_fft;
+  return (int)s.R.size();
+}
+
+// ---- schedule pieces --------------------------------------------------------
+static int enqueue_front(sf21_hii_ctx* c, double z, int kind, const float* delta, const float* src,
+                         cudaStream_t st) {
+  PrologueArgs pa;
+  int rc = prologue_args(c, z, kind, &pa);
+  if (rc) return rc;
+  CTX_CUDA(c, cudaMemcpyAsync(c->d_pa, &pa, sizeof(pa), cudaMemcpyHostToDevice, st));
+  float2* packed = c->d_work[0];
+  const int N = (int)c->N;
+  Batch none;
+  memset(&none, 0, sizeof(none));
+  int e0 = mark(c, st);
+  CTX_CUDA(c, launch_prologue(c->n3, delta, src, c->d_pa, c->d_rec0, c->d_fres, packed, c->d_partials,
+                              c->pro_blocks, st));
+  int e1 = mark(c, st);
+  CTX_CUDA(c, launch_alpha(c->d_partials, c->pro_blocks, c->d_alpha, st));
+  int e2 = mark(c, st);
+  CTX_CUDA(c, launch_fwd_rows(N, packed, c->d_spec, c->d_alpha, c->d_tw, st));
+  int e3 = mark(c, st);
+  CTX_CUDA(c, launch_cols(N, c->d_spec, none, 1, 1, false, c->d_tw, st));
+  int e4 = mark(c, st);
+  CTX_CUDA(c, launch_cols(N, c->d_spec, none, 1, 0, false, c->d_tw, st));
+  int e5 = mark(c, st);
+  span(c, KD_PRO, e0, e1);
+  span(c, KD_ALPHA, e1, e2);
+  span(c, KD_FROWS, e2, e3);
+  span(c, KD_FCB, e3, e4);
+  span(c, KD_FCA, e4, e5);
+  return SF21_OK;
+}
+
+static int enqueue_radii(sf21_hii_ctx* c, int set, cudaStream_t st) {
+  const SetInfo& s = c->sets[set];
+  const int N = (int)c->N;
+  CTX_CUDA(c, cudaMemsetAsync(c->d_rc, RC_NONE, c->n3, st));
+  const int nr = (int)s.R.size();
+  for (int k0 = 0; k0 < nr; k0 += c->K) {
+    Batch bt;
+    memset(&bt, 0, sizeof(bt));
+    bt.K = nr - k0 < c->K ? nr - k0 : c->K;
+    bt.set = set;
+    bt.zmul = (float)s.fesc;
+    for (int k = 0; k < bt.K; ++k) {
+      bt.r[k].dkR = (float)(c->dk * s.R[k0 + k]);
+      bt.r[k].ridx = k0 + k;
+      bt.r[k].work = c->d_work[k];
+    }
+    int e0 = mark(c, st);
+    CTX_CUDA(c, launch_inv_rows_filter(N, c->d_spec, bt, c->d_tw, st));
+    int e1 = mark(c, st);
+    CTX_CUDA(c, launch_cols(N, nullptr, bt, bt.K, 1, true, c->d_tw, st));
+    int e2 = mark(c, st);
+    CTX_CUDA(c, launch_cols_a_test(N, bt, c->d_rc, c->d_alpha, c->d_tw, st));
+    int e3 = mark(c, st);
+    span(c, KD_IROWS, e0, e1);
+    span(c, KD_ICB, e1, e2);
+    span(c, KD_ICA, e2, e3);
+  }
+  return SF21_OK;
+}
+
+static int enqueue_finish(sf21_hii_ctx* c, int set, const float* src, float* xhii, cudaStream_t st) {
+  const SetInfo& s = c->sets[set];
+  const int N = (int)c->N;
+  int* dt0 = reinterpret_cast<int*>(c->d_work[0]);
+  int* dt1 = dt0 + c->n3;
+  int e0 = mark(c, st);
+  CTX_CUDA(c, launch_dt_rows(N, c->d_rc, s.d_nmax, s.vmax, dt0, st));
+  int e1 = mark(c, st);
+  CTX_CUDA(c, launch_dt_b(N, dt0, s.vmax, dt1, st));
+  int e2 = mark(c, st);
+  CTX_CUDA(c, launch_dt_a_finish(N, dt1, s.vmax, dbits(s.fesc), src, c->d_rec0, c->d_fres, c->d_pa, xhii, st));
+  int e3 = mark(c, st);
+  span(c, KD_DTR, e0, e1);
+  span(c, KD_DTB, e1, e2);
+  span(c, KD_DTA, e2, e3);
+  return SF21_OK;
+}
+
+static int check_run_args(sf21_hii_ctx* c, int kind, const void* delta, const void* src, const void* out) {
+  if (!c) return SF21_E_ARG;
+  if (!delta || !src || !out) CTX_FAIL(c, SF21_E_ARG, "null buffer");
+  if (kind != SF21_SRC_SFRD && kind != SF21_SRC_RION) CTX_FAIL(c, SF21_E_ARG, "unknown src_kind %d", kind);
+  return SF21_OK;
+}
+
+extern "C" int sf21_hii_run_z_device(sf21_hii_ctx* c, double z, int kind, const float* delta_dev,
+                                     const float* src_dev, float* xhii_dev, void* stream) {
+  int rc = check_run_args(c, kind, delta_dev, src_dev, xhii_dev);
+  if (rc) return rc;
+  CTX_CUDA(c, cudaSetDevice(c->device));
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+  if ((rc = enqueue_front(c, z, kind, delta_dev, src_dev, st))) return rc;
+  for (int s = 0; s < (int)c->sets.size(); ++s) {
+    if ((rc = enqueue_radii(c, s, st))) return rc;
+    if ((rc = enqueue_finish(c, s, src_dev, xhii_dev + (size_t)s * c->n3, st))) return rc;
+  }
+  return SF21_OK;
+}
+
+extern "C" int sf21_hii_run_z(sf21_hii_ctx* c, double z, int kind, const float* delta, const float* src,
+                              float* xhii, double* neutral) {
+  int rc = check_run_args(c, kind, delta, src, xhii);
+  if (rc) return rc;
+  CTX_CUDA(c, cudaSetDevice(c->device));
+  cudaStream_t st = c->stream;
+  const size_t bf = sizeof(float) * c->n3;
+  CTX_CUDA(c, cudaMemcpyAsync(c->d_delta, delta, bf, cudaMemcpyHostToDevice, st));
+  CTX_CUDA(c, cudaMemcpyAsync(c->d_src, src, bf, cudaMemcpyHostToDevice, st));
+  if ((rc = enqueue_front(c, z, kind, c->d_delta, c->d_src, st))) return rc;
+  // Each set's neutral fraction is the serial double sum of the reference
+  // (:473-477); it runs on a host thread while the GPU works on the next set.
+  std::vector<std::thread> sums;
+  int status = SF21_OK;
+  for (int s = 0; s < (int)c->sets.size() && status == SF21_OK; ++s) {
+    if ((status = enqueue_radii(c, s, st))) break;
+    if ((status = enqueue_finish(c, s, c->d_src, c->d_xhii, st))) break;
+    float* dst = xhii + (size_t)s * c->n3;
+    cudaError_t e = cudaMemcpyAsync(dst, c->d_xhii, bf, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+      c->err = std::string("xHII download failed: ") + cudaGetErrorString(e);
+      status = SF21_E_CUDA;
+      break;
+    }
+    if (neutral) {
+      const long n3 = c->n3;
+      double* out = neutral + s;
+      sums.emplace_back([dst, n3, out]() {
+        double acc = 0.;
+        for (long i = 0; i < n3; ++i) acc += 1.0 - dst[i];
+        *out = acc / n3;
+      });
+    }
+  }
+  for (std::thread& t : sums) t.join();
+  return status;
+}
+
+// ---- check hooks -------------------------------------------------------------
+static int upload_front(sf21_hii_ctx* c, double z, int kind, const float* delta, const float* src) {
+  int rc = check_run_args(c, kind, delta, src, delta);
+  if (rc) return rc;
+  CTX_CUDA(c, cudaSetDevice(c->device));
+  const size_t bf = sizeof(float) * c->n3;
+  CTX_CUDA(c, cudaMemcpyAsync(c->d_delta, delta, bf, cudaMemcpyHostToDevice, c->stream));
+  CTX_CUDA(c, cudaMemcpyAsync(c->d_src, src, bf, cudaMemcpyHostToDevice, c->stream));
+  return enqueue_front(c, z, kind, c->d_delta, c->d_src, c->stream);
+}
+
+extern "C" int sf21_hii_prologue(sf21_hii_ctx* c, double z, int kind, const float* delta, const float* src,
+                                 int set, float* rec0, float* fresid, float* fill0) {
+  if (!c || set < 0 || set >= (int)c->sets.size()) return SF21_E_ARG;
+  int rc = upload_front(c, z, kind, delta, src);
+  if (rc) return rc;
+  const size_t bf = sizeof(float) * c->n3;
+  CTX_CUDA(c, launch_fill0(c->n3, dbits(c->sets[set].fesc), c->d_src, c->d_rec0, c->d_pa, c->d_xhii, c->stream));
+  if (rec0) CTX_CUDA(c, cudaMemcpyAsync(rec0, c->d_rec0, bf, cudaMemcpyDeviceToHost, c->stream));
+  if (fresid) CTX_CUDA(c, cudaMemcpyAsync(fresid, c->d_fres, bf, cudaMemcpyDeviceToHost, c->stream));
+  if (fill0) CTX_CUDA(c, cudaMemcpyAsync(fill0, c->d_xhii, bf, cudaMemcpyDeviceToHost, c->stream));
+  CTX_CUDA(c, cudaStreamSynchronize(c->stream));
+  return SF21_OK;
+}
+
+extern "C" int sf21_hii_filtered(sf21_hii_ctx* c, double z, int kind, const float* delta, const float* src,
+                                 int set, int ridx, float* rec_R, float* ion_R) {
+  if (!c || set < 0 || set >= (int)c->sets.size()) return SF21_E_ARG;
+  const SetInfo& s = c->sets[set];
+  if (ridx < 0 || ridx >= (int)s.R.size() || !rec_R || !ion_R) CTX_FAIL(c, SF21_E_ARG, "bad radius index");
+  int rc = upload_front(c, z, kind, delta, src);
+  if (rc) return rc;
+  // filtered inverse transform of one radius, without the centre test
+  Batch bt;
+  memset(&bt, 0, sizeof(bt));
+  bt.K = 1;
+  bt.zmul = (float)s.fesc;
+  bt.r[0].dkR = (float)(c->dk * s.R[ridx]);
+  bt.r[0].ridx = ridx;
+  bt.r[0].work = c->d_work[0];
+  const int N = (int)c->N;
+  CTX_CUDA(c, launch_inv_rows_filter(N, c->d_spec, bt, c->d_tw, c->stream));
+  CTX_CUDA(c, launch_cols(N, c->d_work[0], bt, 1, 1, true, c->d_tw, c->stream));
+  CTX_CUDA(c, launch_cols(N, c->d_work[0], bt, 1, 0, true, c->d_tw, c->stream));
+  std::vector<float2> box(c->n3);
+  float alpha = 1.f;
+  CTX_CUDA(c, cudaMemcpyAsync(box.data(), c->d_work[0], sizeof(float2) * c->n3, cudaMemcpyDeviceToHost, c->stream));
+  CTX_CUDA(c, cudaMemcpyAsync(&alpha, c->d_alpha, sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  CTX_CUDA(c, cudaStreamSynchronize(c->stream));
+  for (long i = 0; i < c->n3; ++i) {
+    rec_R[i] = box[i].x;
+    ion_R[i] = (float)((double)box[i].y * s.fesc / alpha);
+  }
+  return SF21_OK;
+}
+
+extern "C" int sf21_hii_first_hit(sf21_hii_ctx* c, double z, int kind, const float* delta, const float* src,
+                                  int set, uint8_t* rcout) {
+  if (!c || set < 0 || set >= (int)c->sets.size() || !rcout) return SF21_E_ARG;
+  int rc = upload_front(c, z, kind, delta, src);
+  if (rc) return rc;
+  if ((rc = enqueue_radii(c, set, c->stream))) return rc;
+  CTX_CUDA(c, cudaMemcpyAsync(rcout, c->d_rc, c->n3, cudaMemcpyDeviceToHost, c->stream));
+  CTX_CUDA(c, cudaStreamSynchronize(c->stream));
+  return SF21_OK;
+}
+
+// ---- measurement hooks ---------------------------------------------------------
+extern "C" int sf21_hii_profile(sf21_hii_ctx* c, int enable) {
+  if (!c) return SF21_E_ARG;
+  c->prof = enable != 0;
+  c->ev_used = 0;
+  c->spans.clear();
+  for (int k = 0; k < KD_COUNT; ++k) {
+    c->prof_ms[k] = 0;
+    c->prof_n[k] = 0;
+  }
+  return SF21_OK;
+}
+
+extern "C" int sf21_hii_profile_read(sf21_hii_ctx* c, double* ms, long* launches, int cap) {
+  if (!c) return SF21_E_ARG;
+  CTX_CUDA(c, cudaSetDevice(c->device));
+  CTX_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (!c->spans.empty()) CTX_CUDA(c, cudaEventSynchronize(c->ev[c->spans.back().b]));
+  for (const auto& sp : c->spans) {
+    float t = 0.f;
+    CTX_CUDA(c, cudaEventElapsedTime(&t, c->ev[sp.a], c->ev[sp.b]));
+    c->prof_ms[sp.kind] += t;
+    c->prof_n[sp.kind] += 1;
+  }
+  c->spans.clear();
+  c->ev_used = 0;
+  for (int k = 0; k < KD_COUNT && k < cap; ++k) {
+    if (ms) ms[k] = c->prof_ms[k];
+    if (launches) launches[k] = c->prof_n[k];
+  }
+  return KD_COUNT;
+}
+
+extern "C" const char* sf21_hii_profile_name(int kind) {
+  return (kind >= 0 && kind < KD_COUNT) ? kKindNames[kind] : "";
+}

@@ -1,0 +1,306 @@
+// Element-wise and stencil kernels of the HII stage: the prologue
+// (get_HIIbubbles.c:216-225, 272-274), the norm balance of the packed
+// transform, and the per-set finish: dilation of the bubble centres, the
+// single-cell fill (:281-288) and the cap by the residual neutral fraction
+// (:469-471).  All per-voxel double arithmetic of the reference is
+// reproduced bit for bit with the integer soft-double routines.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "sf21_kernels.h"
+#include "softdouble.h"
+
+namespace sf21 {
+
+#define SD_ONE (0x3FF0000000000000ULL)
+
+// XHI(ratio), user_functions.c:101-106, operation by operation.
+__device__ __forceinline__ sd_t xhi_sd(sd_t r) {
+  if (sd_is_zero(r)) return 0;
+  const sd_t two_r = sd_ldexp(r, 1);               // 2.*ratio (exact)
+  const sd_t b = sd_add(two_r, SD_ONE);            // 2.*ratio + 1.
+  const sd_t c = sd_mul(b, b);                     // (..)*(..)
+  const sd_t e = sd_mul(sd_ldexp(r, 2), r);        // 4.*ratio*ratio
+  const sd_t g = sd_sqrt(sd_sub(c, e));
+  const sd_t num = sd_sub(b, g);                   // 2.*ratio + 1. - sqrt(..)
+  return sd_div(num, two_r);                       // /(2.*ratio)
+}
+
+// Rrec(overdensity, z), user_functions.c:58-65.
+__device__ __forceinline__ sd_t rrec_sd(float od, const PrologueArgs& pa) {
+  const sd_t rec2 = sd_pow(sd_div(sd_from_float(od), pa.r2), pa.r3);
+  const sd_t q = sd_div(rec2, sd_add(SD_ONE, rec2));
+  const sd_t rec3 = sd_pow(q, 0x4010000000000000ULL);  // 4.
+  return sd_div(sd_mul(sd_mul(pa.rec1, rec3), pa.dvv), pa.v_norm);
+}
+
+// Source chain before zeta, left to right as the reference multiplies.
+__device__ __forceinline__ sd_t src_chain(float s, const PrologueArgs& pa) {
+  sd_t t = sd_from_float(s);
+  for (int m = 0; m < pa.n_src_mul; ++m) t = sd_mul(t, pa.src_mul[m]);
+  return t;
+}
+
+constexpr int PRO_THREADS = 256;
+
+__global__ void __launch_bounds__(PRO_THREADS)
+k_prologue(long n3, const float* __restrict__ delta, const float* __restrict__ src,
+           const PrologueArgs* __restrict__ pap, float* __restrict__ rec0, float* __restrict__ fres,
+           float2* __restrict__ packed, float* __restrict__ partials) {
+  const PrologueArgs pa = *pap;
+  float sd2 = 0.f, sh2 = 0.f;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += (long)gridDim.x * blockDim.x) {
+    const float d = delta[i];
+    const sd_t one_d = sd_add(SD_ONE, sd_from_float(d));  // 1. + density_map[i]
+    // fresid = XHI((float)((1+d) * 1.881e-7 * pow(1+z,3) * G_H(z)))      (:220-221)
+    sd_t t = sd_mul(one_d, pa.c_resid);
+    t = sd_mul(t, pa.one_plus_z_cubed);
+    t = sd_mul(t, pa.g_h);
+    const float fr = sd_to_float(t);
+    const float fx = sd_to_float(xhi_sd(sd_from_float(fr)));
+    // density_map = (float)Rrec((float)(1 + d), z)                          (:222)
+    const float rr = sd_to_float(rrec_sd(sd_to_float(one_d), pa));
+    const float h1 = sd_to_float(src_chain(src[i], pa));
+    rec0[i] = rr;
+    fres[i] = fx;
+    packed[i] = make_float2(rr, h1);
+    sd2 += rr * rr;
+    sh2 += h1 * h1;
+  }
+  // block reduction of the two sums of squares (only their ratio is used)
+  __shared__ float red[2][PRO_THREADS / 32];
+  for (int o = 16; o > 0; o >>= 1) {
+    sd2 += __shfl_xor_sync(0xffffffffu, sd2, o);
+    sh2 += __shfl_xor_sync(0xffffffffu, sh2, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    red[0][threadIdx.x >> 5] = sd2;
+    red[1][threadIdx.x >> 5] = sh2;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float a = 0.f, b = 0.f;
+    for (int w = 0; w < PRO_THREADS / 32; ++w) {
+      a += red[0][w];
+      b += red[1][w];
+    }
+    partials[2 * blockIdx.x] = a;
+    partials[2 * blockIdx.x + 1] = b;
+  }
+}
+
+int prologue_blocks(long n3) {
+  long b = (n3 + PRO_THREADS - 1) / PRO_THREADS;
+  return (int)(b < 152 * 16 ? b : 152 * 16);
+}
+
+cudaError_t launch_prologue(long n3, const float* delta, const float* src, const PrologueArgs* pa,
+                            float* rec0, float* fres, float2* packed, float* partials, int nblocks,
+                            cudaStream_t st) {
+  k_prologue<<<nblocks, PRO_THREADS, 0, st>>>(n3, delta, src, pa, rec0, fres, packed, partials);
+  return cudaGetLastError();
+}
+
+// alpha = 2^round(log2(|rec| / |ion|)), so that the two halves of the packed
+// transform have comparable norms.
+__global__ void k_alpha(const float* __restrict__ partials, int nblocks, float* __restrict__ alpha) {
+  __shared__ float sa[256], sb[256];
+  float a = 0.f, b = 0.f;
+  for (int i = threadIdx.x; i < nblocks; i += blockDim.x) {
+    a += partials[2 * i];
+    b += partials[2 * i + 1];
+  }
+  sa[threadIdx.x] = a;
+  sb[threadIdx.x] = b;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      sa[threadIdx.x] += sa[threadIdx.x + s];
+      sb[threadIdx.x] += sb[threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    float r = 1.0f;
+    if (sa[0] > 0.f && sb[0] > 0.f && isfinite(sa[0]) && isfinite(sb[0])) {
+      float e = rintf(0.5f * log2f(sa[0] / sb[0]));
+      e = fminf(fmaxf(e, -60.f), 60.f);
+      r = exp2f(e);
+    }
+    *alpha = r;
+  }
+}
+
+cudaError_t launch_alpha(const float* partials, int nblocks, float* alpha, cudaStream_t st) {
+  k_alpha<<<1, 256, 0, st>>>(partials, nblocks, alpha);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Dilation.  A voxel y is ionised by the radius loops iff some centre x with
+// first-hit radius R_c(x) lies within the discrete ball of that radius:
+// n(x, y) <= nmax(R_c(x)), n = squared per-axis minimum-image lattice
+// distance (the sphere window of get_HIIbubbles.c:366 and the painting of
+// :440-448).  Balls of smaller radii nest, so only the first (largest) hit
+// matters.  With v(x) = nmax(R_c(x)) (-1 for no centre) the test is
+//   max_x [v(x) - n(x, y)] >= 0,
+// separable into three 1D max-plus passes with the kernel -d^2.  Values below
+// zero can never come back to >= 0, so they are clamped to -1.
+constexpr int DT_ROW_THREADS = 256;
+
+__device__ __forceinline__ int dt_window(int vmax, int N) {
+  int w = (int)sqrtf((float)vmax);
+  while ((w + 1) * (w + 1) <= vmax) ++w;
+  while (w * w > vmax) --w;
+  return w < N / 2 ? w : N / 2;
+}
+
+// pass along c (contiguous): one row per CTA iteration, input from rc.
+__global__ void __launch_bounds__(DT_ROW_THREADS)
+k_dt_rows(int N, const uint8_t* __restrict__ rc, const int* __restrict__ nmax, int vmax,
+          int* __restrict__ out) {
+  extern __shared__ int srow[];
+  const long row = blockIdx.x;
+  const uint8_t* in = rc + row * N;
+  for (int c = threadIdx.x; c < N; c += blockDim.x) {
+    const uint8_t h = in[c];
+    srow[c] = (h == RC_NONE) ? -1 : nmax[h];
+  }
+  __syncthreads();
+  const int W = dt_window(vmax, N);
+  for (int y = threadIdx.x; y < N; y += blockDim.x) {
+    int best = srow[y];
+    for (int d = 1; d <= W; ++d) {
+      const int dd = d * d;
+      int u = srow[(y + d) & (N - 1)] - dd;
+      int w = srow[(y - d) & (N - 1)] - dd;
+      best = max(best, max(u, w));
+    }
+    out[row * N + y] = best < -1 ? -1 : best;
+  }
+}
+
+// pass along b (stride N): tile N x CW for fixed a.
+constexpr int DT_CW = 16;
+__global__ void k_dt_b(int N, const int* __restrict__ in, int vmax, int* __restrict__ out) {
+  extern __shared__ int stile[];  // [N][DT_CW]
+  const int nblk = N / DT_CW;
+  const long a = blockIdx.x / nblk;
+  const int c0 = (blockIdx.x % nblk) * DT_CW;
+  const long base = a * N * N + c0;
+  for (int t = threadIdx.x; t < N * DT_CW; t += blockDim.x) {
+    const int b = t / DT_CW, c = t % DT_CW;
+    stile[t] = in[base + (long)b * N + c];
+  }
+  __syncthreads();
+  const int W = dt_window(vmax, N);
+  for (int t = threadIdx.x; t < N * DT_CW; t += blockDim.x) {
+    const int b = t / DT_CW, c = t % DT_CW;
+    int best = stile[t];
+    for (int d = 1; d <= W; ++d) {
+      const int dd = d * d;
+      best = max(best, max(stile[((b + d) & (N - 1)) * DT_CW + c] - dd,
+                           stile[((b - d) & (N - 1)) * DT_CW + c] - dd));
+    }
+    out[base + (long)b * N + c] = best < -1 ? -1 : best;
+  }
+}
+
+// pass along a (stride N^2) fused with the finish of the xHII box.
+__global__ void k_dt_a_finish(int N, const int* __restrict__ in, int vmax, sd_t zeta,
+                              const float* __restrict__ src, const float* __restrict__ rec0,
+                              const float* __restrict__ fres, const PrologueArgs* __restrict__ pap,
+                              float* __restrict__ xhii) {
+  extern __shared__ int stile[];  // [N][DT_CW]
+  const PrologueArgs pa = *pap;
+  const int nblk = N / DT_CW;
+  const long b = blockIdx.x / nblk;
+  const int c0 = (blockIdx.x % nblk) * DT_CW;
+  const long base = b * N + c0;
+  const long stride = (long)N * N;
+  for (int t = threadIdx.x; t < N * DT_CW; t += blockDim.x) {
+    const int a = t / DT_CW, c = t % DT_CW;
+    stile[t] = in[base + (long)a * stride + c];
+  }
+  __syncthreads();
+  const int W = dt_window(vmax, N);
+  for (int t = threadIdx.x; t < N * DT_CW; t += blockDim.x) {
+    const int a = t / DT_CW, c = t % DT_CW;
+    int best = stile[t];
+    for (int d = 1; d <= W && best < 0; ++d) {
+      const int dd = d * d;
+      best = max(best, max(stile[((a + d) & (N - 1)) * DT_CW + c] - dd,
+                           stile[((a - d) & (N - 1)) * DT_CW + c] - dd));
+    }
+    const long i = base + (long)a * stride + c;
+    // single-cell fill (:281-288) with h = (float)(chain(src) * zeta)
+    const float h = sd_to_float(sd_mul(src_chain(src[i], pa), zeta));
+    const float dd0 = rec0[i];
+    float f;
+    if (h > 0.0f) {
+      if (dd0 > 0.0f)
+        f = (h >= dd0) ? 1.0f : __fdiv_rn(h, dd0);
+      else
+        f = 1.0f;
+    } else {
+      f = 0.0f;
+    }
+    if (best >= 0) f = 1.0f;  // inside a bubble (:392, :448)
+    // cap: if (bubblef > 1.0 - fresid) bubblef = 1.0 - fresid   (:470)
+    const sd_t om = sd_sub(SD_ONE, sd_from_float(fres[i]));
+    if (sd_gt(sd_from_float(f), om)) f = sd_to_float(om);
+    xhii[i] = f;
+  }
+}
+
+// Single-cell fill alone (check hook): :281-288 without dilation and cap.
+__global__ void k_fill0(long n3, sd_t zeta, const float* __restrict__ src, const float* __restrict__ rec0,
+                        const PrologueArgs* __restrict__ pap, float* __restrict__ fill) {
+  const PrologueArgs pa = *pap;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += (long)gridDim.x * blockDim.x) {
+    const float h = sd_to_float(sd_mul(src_chain(src[i], pa), zeta));
+    const float d = rec0[i];
+    float f;
+    if (h > 0.0f)
+      f = (d > 0.0f) ? ((h >= d) ? 1.0f : __fdiv_rn(h, d)) : 1.0f;
+    else
+      f = 0.0f;
+    fill[i] = f;
+  }
+}
+
+cudaError_t launch_fill0(long n3, uint64_t zeta, const float* src, const float* rec0,
+                         const PrologueArgs* pa, float* fill, cudaStream_t st) {
+  k_fill0<<<prologue_blocks(n3), PRO_THREADS, 0, st>>>(n3, zeta, src, rec0, pa, fill);
+  return cudaGetLastError();
+}
+
+cudaError_t dilate_setup(int N) {
+  cudaError_t e;
+  const int tile = N * DT_CW * (int)sizeof(int);
+  if ((e = cudaFuncSetAttribute(k_dt_b, cudaFuncAttributeMaxDynamicSharedMemorySize, tile))) return e;
+  if ((e = cudaFuncSetAttribute(k_dt_a_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, tile))) return e;
+  return cudaSuccess;
+}
+
+cudaError_t launch_dt_rows(int N, const uint8_t* rc, const int* nmax, int vmax, int* out, cudaStream_t st) {
+  k_dt_rows<<<(unsigned)((long)N * N), DT_ROW_THREADS, N * sizeof(int), st>>>(N, rc, nmax, vmax, out);
+  return cudaGetLastError();
+}
+
+static unsigned dt_grid(int N) { return (unsigned)((long)N * (N / DT_CW)); }
+static int dt_threads(int N) { return N * DT_CW < 512 ? N * DT_CW : 512; }
+
+cudaError_t launch_dt_b(int N, const int* in, int vmax, int* out, cudaStream_t st) {
+  k_dt_b<<<dt_grid(N), dt_threads(N), (size_t)N * DT_CW * sizeof(int), st>>>(N, in, vmax, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dt_a_finish(int N, const int* in, int vmax, uint64_t zeta, const float* src, const float* rec0,
+                               const float* fres, const PrologueArgs* pa, float* xhii, cudaStream_t st) {
+  k_dt_a_finish<<<dt_grid(N), dt_threads(N), (size_t)N * DT_CW * sizeof(int), st>>>(N, in, vmax, zeta, src, rec0,
+                                                                                  fres, pa, xhii);
+  return cudaGetLastError();
+}
+
+}  // namespace sf21

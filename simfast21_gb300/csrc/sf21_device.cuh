@@ -1,0 +1,55 @@
+// Device-side data structures and helpers shared by the HII kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fft_line.cuh"
+
+namespace sf21 {
+
+// Max radii fused into one k-space pass (one spectrum read, K outputs).
+constexpr int KMAX = 8;
+// First-hit radius index sentinel: voxel was never a bubble centre.
+constexpr uint8_t RC_NONE = 0xFF;
+
+// One radius of a batch.
+struct RadiusArg {
+  float dkR;      // dk * R (k-space top-hat argument scale)
+  int ridx;       // index of R in its parameter set's radius list
+  float2* work;   // N^3 complex work buffer for this radius
+};
+
+struct Batch {
+  int K;          // radii in this batch (<= KMAX)
+  int set;        // parameter set
+  float zmul;     // ionisation-rate multiplier of the set (zeta)
+  RadiusArg r[KMAX];
+};
+
+// Real-space top-hat window in k-space, W(x) = 3 (sin x - x cos x) / x^3
+// (auxiliary.c:350-359).  Below x = 2 the Taylor series in x^2 (to x^14,
+// truncation < 3e-11) avoids the cancellation of the closed form in float;
+// above, the closed form with the accurate sincosf.
+__device__ __forceinline__ float w_tophat(float x) {
+  if (x < 2.0f) {
+    const float y = x * x;
+    float p = -1.3495220664131733e-13f;       // -1/7410154752000
+    p = fmaf(p, y, 3.2118561710393668e-11f);  // 1/31135104000
+    p = fmaf(p, y, -5.7812513436029994e-09f); // -1/172972800
+    p = fmaf(p, y, 7.5156266505230805e-07f);  // 1/1330560
+    p = fmaf(p, y, -6.6137566137566139e-05f); // -1/15120
+    p = fmaf(p, y, 3.5714285714285713e-03f);  // 1/280
+    p = fmaf(p, y, -0.1f);
+    p = fmaf(p, y, 1.0f);
+    return p;
+  }
+  float s, c;
+  sincosf(x, &s, &c);
+  const float ix = 1.0f / x;
+  return 3.0f * (s - x * c) * ix * ix * ix;
+}
+
+// Signed frequency index of position i on an N-point axis (:309-311).
+__device__ __forceinline__ int kfreq(int i, int N) { return i > N / 2 ? i - N : i; }
+
+}  // namespace sf21

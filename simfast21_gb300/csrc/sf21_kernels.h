@@ -1,0 +1,57 @@
+// Internal launch API between the C-ABI layer (hii_api.cu) and the kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "sf21_device.cuh"
+
+namespace sf21 {
+
+// Per-redshift scalars of the prologue, as IEEE double bit patterns computed
+// on the host exactly as the reference evaluates them.
+struct PrologueArgs {
+  uint64_t one_plus_z_cubed;  // pow(1+z, 3.0)                 (:220)
+  uint64_t g_h;               // G_H(z)                         (:220)
+  uint64_t rec1;              // 1e-24*r1*pow(1+z, r4)          (user_functions.c:59)
+  uint64_t dvv;               // pow(L*CM/N/h/(1+z), 3.0)       (user_functions.c:62)
+  uint64_t c_resid;           // 1.881e-7                       (:220)
+  uint64_t r2, r3;            // Rrec fit constants             (user_functions.c:54-55)
+  uint64_t v_norm;            // 1e45                           (user_functions.c:38)
+  uint64_t src_mul[6];        // source multipliers before zeta (:273 or :258)
+  int n_src_mul;
+};
+
+cudaError_t fft_setup(int N);
+// c-axis forward of the packed box (imag part times *alpha), in -> out
+cudaError_t launch_fwd_rows(int N, const float2* in, float2* out, const float* alpha, const float2* tw,
+                            cudaStream_t st);
+// c-axis inverse in place, no filter
+cudaError_t launch_inv_rows_plain(int N, float2* box, const float2* tw, cudaStream_t st);
+// c-axis inverse with the top-hat filter of the batch's K radii: spec -> bt.r[k].work
+cudaError_t launch_inv_rows_filter(int N, const float2* spec, const Batch& bt, const float2* tw, cudaStream_t st);
+// strided axis (1 = b, 0 = a) in place, of `box` (nbox = 1) or of the batch's work boxes
+cudaError_t launch_cols(int N, float2* box, const Batch& bt, int nbox, int axis, bool inverse, const float2* tw,
+                        cudaStream_t st);
+// a-axis inverse of the batch's work boxes + centre test + first-hit update
+cudaError_t launch_cols_a_test(int N, const Batch& bt, uint8_t* rc, const float* alpha, const float2* tw,
+                               cudaStream_t st);
+
+// pa points to device memory (so a captured graph can be replayed per z).
+cudaError_t launch_prologue(long n3, const float* delta, const float* src, const PrologueArgs* pa,
+                            float* rec0, float* fres, float2* packed, float* partials, int nblocks,
+                            cudaStream_t st);
+cudaError_t launch_alpha(const float* partials, int nblocks, float* alpha, cudaStream_t st);
+int prologue_blocks(long n3);
+
+// Dilation of the first-hit radius field and the final xHII box of one set:
+// three max-plus passes (c, b, a); the last one also applies the single-cell
+// fill and the cap.
+cudaError_t dilate_setup(int N);
+cudaError_t launch_dt_rows(int N, const uint8_t* rc, const int* nmax, int vmax, int* out, cudaStream_t st);
+cudaError_t launch_dt_b(int N, const int* in, int vmax, int* out, cudaStream_t st);
+cudaError_t launch_dt_a_finish(int N, const int* in, int vmax, uint64_t zeta, const float* src, const float* rec0,
+                               const float* fres, const PrologueArgs* pa, float* xhii, cudaStream_t st);
+cudaError_t launch_fill0(long n3, uint64_t zeta, const float* src, const float* rec0,
+                         const PrologueArgs* pa, float* fill, cudaStream_t st);
+
+}  // namespace sf21

@@ -1,0 +1,376 @@
+// IEEE-754 binary64 arithmetic on 64-bit integers (round to nearest even).
+//
+// The HII prologue (get_HIIbubbles.c:216-225, 272-274, 281-288 and
+// user_functions.c:58-106) computes every per-voxel quantity in double and
+// rounds the result to float.  The GPU product path must not use FP64
+// arithmetic, so these routines reproduce the same double operations bit for
+// bit with integer instructions: add, sub, mul, div and sqrt are correctly
+// rounded exactly like the hardware double unit of the reference's CPU.
+// pow() is not an IEEE basic operation: sd_pow evaluates it in 64+ bit fixed
+// point (error below 2^-59 relative) and rounds once, which returns the same
+// double as a correctly rounded libm pow except in rare near-tie cases; the
+// prologue rounds its results to float afterwards, which hides those cases.
+//
+// Domain handled: finite normal operands and zeros (the prologue never meets
+// subnormal doubles, infinities or NaNs); sd_pow needs x >= 0 with a binary
+// exponent in [-60, 60] and |y| < 64.  Outside it returns a quiet NaN so a
+// violation is visible in the output instead of silently wrong.
+//
+// The same header compiles as host C++ (g++) so it can be checked against
+// the CPU's native double unit without a GPU.
+#pragma once
+#include <stdint.h>
+
+#if defined(__CUDACC__)
+#define SD_HD __host__ __device__ __forceinline__
+#else
+#define SD_HD static inline
+#endif
+
+typedef uint64_t sd_t;
+typedef unsigned __int128 sd_u128;
+typedef __int128 sd_i128;
+
+#define SD_SIGN (0x8000000000000000ULL)
+#define SD_QNAN (0x7ff8000000000000ULL)
+
+#include "pow_tables.h"
+
+SD_HD int sd_clz64(uint64_t x) {
+#if defined(__CUDA_ARCH__)
+  return __clzll((long long)x);
+#else
+  return x ? __builtin_clzll(x) : 64;
+#endif
+}
+
+SD_HD int sd_clz128(sd_u128 x) {
+  uint64_t hi = (uint64_t)(x >> 64);
+  if (hi) return sd_clz64(hi);
+  return 64 + sd_clz64((uint64_t)x);
+}
+
+// Shift right with sticky bit (OR of the shifted-out bits) in bit 0.
+SD_HD uint64_t sd_shr_sticky(uint64_t x, int s) {
+  if (s <= 0) return x;
+  if (s >= 64) return x != 0;
+  return (x >> s) | ((x & ((1ULL << s) - 1)) != 0);
+}
+
+// Pack sign, unbiased exponent e and a significand m with its leading one at
+// bit 62 (bits 61..10 fraction, 9..0 guard/sticky) into a rounded double.
+// Results are assumed to stay in the normal range.
+SD_HD sd_t sd_round_pack(uint64_t sign, int e, uint64_t m) {
+  // m: leading one at bit 62.  Keep 53 bits (62..10), round on bits 9..0.
+  uint64_t rest = m & 0x3FFULL;
+  uint64_t q = m >> 10;  // 53 bits, leading one at bit 52
+  if (rest > 0x200ULL || (rest == 0x200ULL && (q & 1))) {
+    q += 1;
+    if (q >> 53) {  // carry out: 1.111..1 + ulp = 10.0
+      q >>= 1;
+      e += 1;
+    }
+  }
+  return sign | ((uint64_t)(e + 1023) << 52) | (q & 0xFFFFFFFFFFFFFULL);
+}
+
+SD_HD sd_t sd_from_float(float f) {
+  union {
+    float f;
+    uint32_t u;
+  } c;
+  c.f = f;
+  uint32_t u = c.u;
+  uint64_t sign = (uint64_t)(u >> 31) << 63;
+  uint32_t ex = (u >> 23) & 0xFF;
+  uint32_t fr = u & 0x7FFFFF;
+  if (ex == 0) {
+    if (fr == 0) return sign;
+    // subnormal float: normalise
+    int sh = sd_clz64((uint64_t)fr) - 40;  // leading one to bit 23
+    fr <<= sh;
+    int e = -126 - sh;
+    return sign | ((uint64_t)(e + 1023) << 52) | ((uint64_t)(fr & 0x7FFFFF) << 29);
+  }
+  if (ex == 0xFF) return sign | 0x7FF0000000000000ULL | ((uint64_t)fr << 29);
+  return sign | ((uint64_t)(ex - 127 + 1023) << 52) | ((uint64_t)fr << 29);
+}
+
+SD_HD sd_t sd_from_int(int64_t v) {
+  if (v == 0) return 0;
+  uint64_t sign = v < 0 ? SD_SIGN : 0;
+  uint64_t a = v < 0 ? (uint64_t)(-v) : (uint64_t)v;
+  int lz = sd_clz64(a);
+  int e = 63 - lz;
+  uint64_t m = a << lz;  // leading one at bit 63
+  m = sd_shr_sticky(m, 1);
+  return sd_round_pack(sign, e, m);
+}
+
+// Round a double to the nearest float (ties to even), with float subnormals.
+SD_HD float sd_to_float(sd_t d) {
+  uint32_t sign = (uint32_t)(d >> 63) << 31;
+  int ex = (int)((d >> 52) & 0x7FF);
+  uint64_t fr = d & 0xFFFFFFFFFFFFFULL;
+  uint32_t out;
+  if (ex == 0x7FF) {
+    out = sign | 0x7F800000u | (fr ? 0x400000u : 0u);
+  } else if (ex == 0) {
+    out = sign;  // double subnormals underflow to zero in float
+  } else {
+    int e = ex - 1023;
+    uint64_t m = fr | (1ULL << 52);  // 53-bit significand
+    if (e > 127) {
+      out = sign | 0x7F800000u;
+    } else {
+      int shift;      // bits to drop from the 53-bit significand
+      int fe;         // float biased exponent for the result (0 = subnormal)
+      if (e >= -126) {
+        shift = 29;
+        fe = e + 127;
+      } else {
+        shift = 29 + (-126 - e);
+        fe = 0;
+      }
+      uint64_t q, rem, half;
+      if (shift >= 64) {
+        q = 0;
+        rem = m;
+        half = 0;  // m < 2^53 < half: always rounds down
+        out = sign;
+      } else {
+        q = m >> shift;
+        rem = m & ((1ULL << shift) - 1);
+        half = 1ULL << (shift - 1);
+        if (rem > half || (rem == half && (q & 1))) q += 1;
+        if (fe == 0) {
+          // subnormal (q may round up into the smallest normal: bit 23)
+          out = sign | (uint32_t)q;
+        } else {
+          if (q >> 24) {
+            q >>= 1;
+            fe += 1;
+          }
+          if (fe >= 255)
+            out = sign | 0x7F800000u;
+          else
+            out = sign | ((uint32_t)fe << 23) | ((uint32_t)q & 0x7FFFFFu);
+        }
+      }
+    }
+  }
+  union {
+    uint32_t u;
+    float f;
+  } c;
+  c.u = out;
+  return c.f;
+}
+
+SD_HD bool sd_is_zero(sd_t a) { return (a & ~SD_SIGN) == 0; }
+SD_HD sd_t sd_neg(sd_t a) { return a ^ SD_SIGN; }
+
+// Total order on finite values: a < b
+SD_HD bool sd_lt(sd_t a, sd_t b) {
+  if (sd_is_zero(a) && sd_is_zero(b)) return false;
+  bool sa = a >> 63, sb = b >> 63;
+  if (sa != sb) return sa;
+  if (!sa) return a < b;
+  return a > b;
+}
+SD_HD bool sd_gt(sd_t a, sd_t b) { return sd_lt(b, a); }
+SD_HD bool sd_ge(sd_t a, sd_t b) { return !sd_lt(a, b); }
+
+SD_HD sd_t sd_add(sd_t a, sd_t b) {
+  if (sd_is_zero(a)) return sd_is_zero(b) ? (a & b) : b;
+  if (sd_is_zero(b)) return a;
+  int ea = (int)((a >> 52) & 0x7FF), eb = (int)((b >> 52) & 0x7FF);
+  if (ea == 0x7FF || eb == 0x7FF || ea == 0 || eb == 0) return SD_QNAN;
+  uint64_t sa = a & SD_SIGN, sb = b & SD_SIGN;
+  // significands with the leading one at bit 61: value = m * 2^(e - 61)
+  uint64_t ma = ((a & 0xFFFFFFFFFFFFFULL) | (1ULL << 52)) << 9;
+  uint64_t mb = ((b & 0xFFFFFFFFFFFFFULL) | (1ULL << 52)) << 9;
+  if (ea < eb || (ea == eb && ma < mb)) {  // make |a| >= |b|
+    uint64_t t = ma; ma = mb; mb = t;
+    int te = ea; ea = eb; eb = te;
+    uint64_t ts = sa; sa = sb; sb = ts;
+  }
+  mb = sd_shr_sticky(mb, ea - eb);
+  // sd_round_pack wants value = m * 2^(e - 62) with the leading one at 62
+  int e = ea - 1023 + 1;
+  uint64_t m;
+  if (sa == sb) {
+    m = ma + mb;  // < 2^63
+    if (!(m >> 62)) {
+      m <<= 1;
+      e -= 1;
+    }
+  } else {
+    m = ma - mb;
+    if (m == 0) return 0;  // exact cancellation: +0 under round-to-nearest
+    int sh = sd_clz64(m) - 1;  // bring the leading one to bit 62
+    m <<= sh;
+    e -= sh;
+  }
+  return sd_round_pack(sa, e, m);
+}
+
+SD_HD sd_t sd_sub(sd_t a, sd_t b) { return sd_add(a, sd_neg(b)); }
+
+SD_HD sd_t sd_mul(sd_t a, sd_t b) {
+  uint64_t sign = (a ^ b) & SD_SIGN;
+  if (sd_is_zero(a) || sd_is_zero(b)) return sign;
+  int ea = (int)((a >> 52) & 0x7FF), eb = (int)((b >> 52) & 0x7FF);
+  if (ea == 0x7FF || eb == 0x7FF || ea == 0 || eb == 0) return SD_QNAN;
+  uint64_t ma = (a & 0xFFFFFFFFFFFFFULL) | (1ULL << 52);
+  uint64_t mb = (b & 0xFFFFFFFFFFFFFULL) | (1ULL << 52);
+  sd_u128 p = (sd_u128)ma * mb;  // leading one at bit 104 or 105
+  int e = (ea - 1023) + (eb - 1023);
+  // bring leading one to bit 62 of a 64-bit word with sticky
+  int lead = 127 - sd_clz128(p);  // 104 or 105
+  int sh = lead - 62;
+  uint64_t hi = (uint64_t)(p >> sh);
+  uint64_t sticky = (p & (((sd_u128)1 << sh) - 1)) != 0;
+  e += lead - 104;
+  return sd_round_pack(sign, e, hi | sticky);
+}
+
+SD_HD sd_t sd_div(sd_t a, sd_t b) {
+  uint64_t sign = (a ^ b) & SD_SIGN;
+  if (sd_is_zero(b)) return SD_QNAN;
+  if (sd_is_zero(a)) return sign;
+  int ea = (int)((a >> 52) & 0x7FF), eb = (int)((b >> 52) & 0x7FF);
+  if (ea == 0x7FF || eb == 0x7FF || ea == 0 || eb == 0) return SD_QNAN;
+  uint64_t ma = (a & 0xFFFFFFFFFFFFFULL) | (1ULL << 52);
+  uint64_t mb = (b & 0xFFFFFFFFFFFFFULL) | (1ULL << 52);
+  int e = (ea - 1023) - (eb - 1023);
+  if (ma < mb) {
+    ma <<= 1;
+    e -= 1;
+  }
+  // quotient ma/mb in [1, 2): produce 63 bits (leading one at bit 62)
+  sd_u128 num = (sd_u128)ma << 62;
+  uint64_t q = (uint64_t)(num / mb);
+  uint64_t r = (uint64_t)(num - (sd_u128)q * mb);
+  return sd_round_pack(sign, e, q | (r != 0));
+}
+
+SD_HD sd_t sd_sqrt(sd_t a) {
+  if (sd_is_zero(a)) return a;
+  if (a >> 63) return SD_QNAN;
+  int ea = (int)((a >> 52) & 0x7FF);
+  if (ea == 0x7FF || ea == 0) return SD_QNAN;
+  uint64_t m = (a & 0xFFFFFFFFFFFFFULL) | (1ULL << 52);
+  int e = ea - 1023;
+  if (e & 1) {
+    m <<= 1;
+    e -= 1;
+  }
+  // sqrt(m * 2^-52) * 2^(e/2); want 63-bit root of m * 2^(124-52) = m << 72
+  sd_u128 x = (sd_u128)m << 72;  // value in [2^124, 2^126)
+  // integer sqrt, bit by bit
+  sd_u128 res = 0, bit = (sd_u128)1 << 126;
+  while (bit > x) bit >>= 2;
+  while (bit != 0) {
+    if (x >= res + bit) {
+      x -= res + bit;
+      res = (res >> 1) + bit;
+    } else {
+      res >>= 1;
+    }
+    bit >>= 2;
+  }
+  uint64_t r = (uint64_t)res;  // leading one at bit 62
+  return sd_round_pack(0, e / 2, r | (x != 0));
+}
+
+// Exact multiplication by 2^k for normal results.
+SD_HD sd_t sd_ldexp(sd_t a, int k) {
+  if (sd_is_zero(a)) return a;
+  return a + ((uint64_t)(int64_t)k << 52);
+}
+
+// ---- pow(x, y) for x >= 0 via fixed point log2 / exp2 --------------------
+// (a * b) >> 124 for signed fixed-point values with |a|, |b| < 2^126 and a
+// result below 2^127, computed with 62-bit limbs so that no partial product
+// exceeds 128 bits.  Truncation error: a few units of 2^-124.
+SD_HD sd_i128 sd_mulq124(sd_i128 a, sd_i128 b) {
+  bool neg = (a < 0) != (b < 0);
+  sd_u128 ua = a < 0 ? (sd_u128)(-a) : (sd_u128)a;
+  sd_u128 ub = b < 0 ? (sd_u128)(-b) : (sd_u128)b;
+  const sd_u128 mask62 = (((sd_u128)1) << 62) - 1;
+  uint64_t a0 = (uint64_t)(ua & mask62), a1 = (uint64_t)(ua >> 62);
+  uint64_t b0 = (uint64_t)(ub & mask62), b1 = (uint64_t)(ub >> 62);
+  sd_u128 p11 = (sd_u128)a1 * b1;                     // weight 2^124
+  sd_u128 p10 = (sd_u128)a1 * b0 + (sd_u128)a0 * b1;  // weight 2^62
+  sd_u128 p00 = (sd_u128)a0 * b0;                     // weight 1
+  sd_u128 r = p11 + (p10 >> 62) + (((p10 & mask62) + (p00 >> 62)) >> 62);
+  return neg ? -(sd_i128)r : (sd_i128)r;
+}
+
+#define SD_Q124(hi, lo) ((sd_i128)((((sd_u128)(hi)) << 64) | (sd_u128)(lo)))
+
+// log2(x) = e + log2(c_j) + ln(1 + t)/ln 2 with c_j = 2^62 / SD_POW_INV[j]
+// (j = top 7 fraction bits of x) and t = m/c_j - 1 exactly, |t| <= 2^-8; the
+// series for ln(1 + t) to t^9 leaves < 2^-83.  w = y log2(x) is kept in Q.96
+// and 2^w = 2^n 2^(j2/128) e^u with u = r ln 2 < 2^-7.5 and e^u to u^10.
+// Every constant is a Q.124 (or Q.96) fixed-point number, so the relative
+// error of the result before the final rounding is far below 2^-80.
+SD_HD sd_t sd_pow(sd_t x, sd_t y) {
+  if (sd_is_zero(y)) return 0x3FF0000000000000ULL;
+  if (sd_is_zero(x)) return (y >> 63) ? 0x7FF0000000000000ULL : 0;
+  if (x >> 63) return SD_QNAN;
+  const int ex = (int)((x >> 52) & 0x7FF) - 1023;
+  const int ey = (int)((y >> 52) & 0x7FF) - 1023;
+  if (ex < -60 || ex > 60 || ey > 5 || ey < -60) return SD_QNAN;
+  const uint64_t M = (x & 0xFFFFFFFFFFFFFULL) | (1ULL << 52);
+  const int j = (int)((M >> 45) & 127);
+  // m/c_j = M * INV[j] / 2^114 (exact); t in Q.124
+  const sd_u128 P = (sd_u128)M * SD_POW_INV[j];
+  const sd_i128 T = (sd_i128)(P << 10) - (((sd_i128)1) << 124);
+  sd_i128 acc = SD_Q124(SD_POW_RCP_HI[9], SD_POW_RCP_LO[9]);
+  for (int k = 8; k >= 1; --k)
+    acc = SD_Q124(SD_POW_RCP_HI[k], SD_POW_RCP_LO[k]) - sd_mulq124(T, acc);
+  const sd_i128 lnp = sd_mulq124(T, acc);  // ln(1 + t), Q.124, |lnp| < 2^117
+  // log2(x) in Q.96
+  sd_i128 l2 = sd_mulq124(lnp, SD_Q124(SD_POW_INV_LN2_HI, SD_POW_INV_LN2_LO)) >> 28;
+  l2 += (sd_i128)(((sd_u128)SD_POW_L2C_HI[j] << 64) | SD_POW_L2C_LO[j]);
+  l2 += ((sd_i128)ex) << 96;  // |l2| < 2^103
+  // w = y * l2 in Q.96, y = my * 2^(ey - 52)
+  const uint64_t my = (y & 0xFFFFFFFFFFFFFULL) | (1ULL << 52);
+  const bool wneg = ((y >> 63) != 0) != (l2 < 0);
+  const sd_u128 ul2 = l2 < 0 ? (sd_u128)(-l2) : (sd_u128)l2;
+  const uint64_t u0 = (uint64_t)ul2, u1 = (uint64_t)(ul2 >> 64);  // u1 < 2^39
+  const sd_u128 q0 = (sd_u128)u0 * my;  // weight 1
+  const sd_u128 q1 = (sd_u128)u1 * my;  // weight 2^64, < 2^92
+  const int s = 52 - ey;                // >= 47
+  sd_u128 w;                            // |w| in Q.96
+  if (s <= 64)
+    w = (q1 << (64 - s)) + (q0 >> s);
+  else
+    w = (q1 >> (s - 64)) + (s < 128 ? (q0 >> s) : 0);
+  int64_t n = (int64_t)(w >> 96);
+  sd_u128 f = w & ((((sd_u128)1) << 96) - 1);
+  if (wneg) {
+    if (f != 0) {
+      n = -n - 1;
+      f = (((sd_u128)1) << 96) - f;
+    } else {
+      n = -n;
+    }
+  }
+  if (n > 1000 || n < -1000) return SD_QNAN;
+  const int j2 = (int)(f >> 89);
+  const sd_i128 r = (sd_i128)((f & ((((sd_u128)1) << 89) - 1)) << 28);  // Q.124, < 2^-7
+  const sd_i128 u = sd_mulq124(r, SD_Q124(SD_POW_LN2_HI, SD_POW_LN2_LO));
+  sd_i128 ex_u = SD_Q124(SD_POW_IFACT_HI[10], SD_POW_IFACT_LO[10]);
+  for (int k = 9; k >= 0; --k)
+    ex_u = SD_Q124(SD_POW_IFACT_HI[k], SD_POW_IFACT_LO[k]) + sd_mulq124(u, ex_u);
+  // significand 2^(j2/128) e^u, Q.124, value in [1, 2.02)
+  const sd_u128 mm =
+      (sd_u128)sd_mulq124(SD_Q124(SD_POW_EXP2T_HI[j2], SD_POW_EXP2T_LO[j2]), ex_u);
+  const int lead = (mm >> 125) ? 125 : 124;
+  const int sh = lead - 62;
+  const uint64_t m = (uint64_t)(mm >> sh) | ((mm & ((((sd_u128)1) << sh) - 1)) != 0);
+  return sd_round_pack(0, (int)n + (lead - 124), m);
+}

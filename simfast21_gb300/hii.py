@@ -1,0 +1,195 @@
+"""Host-side Python mirror of the HII stage over the C-ABI (include/sf21_hii.h).
+
+``FilterBank`` wraps one sf21_hii context: construct it with the box and the
+parameter sets (what get_HIIbubbles.c:98-194 sets up), then call ``run_z``
+per redshift (the loop body, :215-477).  Arrays are numpy float32 boxes in C
+order, or device pointers (``run_z_device``).  There is no CPU fallback:
+without libsf21hii.so or without a GPU the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libsf21hii.so")
+
+SF21_SRC_SFRD = 0
+SF21_SRC_RION = 1
+
+_STATUS = {0: "SF21_OK", 1: "SF21_E_ARG", 2: "SF21_E_ALLOC", 3: "SF21_E_CUDA",
+           4: "SF21_E_TIMEOUT", 5: "SF21_E_UNSUPPORTED"}
+
+# Every entry point declared in include/sf21_hii.h.
+EXPORTS = [
+    "sf21_hii_create", "sf21_hii_destroy", "sf21_hii_last_error", "sf21_hii_run_z",
+    "sf21_hii_run_z_device", "sf21_hii_radii", "sf21_hii_prologue", "sf21_hii_filtered",
+    "sf21_hii_first_hit", "sf21_hii_profile", "sf21_hii_profile_read", "sf21_hii_profile_name",
+]
+
+
+class HIIError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{_STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class _Set(ctypes.Structure):
+    _fields_ = [("fesc", ctypes.c_double), ("Rmax", ctypes.c_double), ("Nbins", ctypes.c_int)]
+
+
+class _Config(ctypes.Structure):
+    _fields_ = [("N", ctypes.c_long), ("N_halo", ctypes.c_long), ("L", ctypes.c_double),
+                ("hubble", ctypes.c_double), ("device", ctypes.c_int), ("nsets", ctypes.c_int),
+                ("sets", ctypes.POINTER(_Set)), ("kmax", ctypes.c_int)]
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Load libsf21hii.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise OSError(f"{path} not found: build it with simfast21_gb300.build.build()")
+    L = ctypes.CDLL(path)
+    vp, dp, fp = ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_void_p
+    L.sf21_hii_create.argtypes = [ctypes.POINTER(_Config), ctypes.POINTER(ctypes.c_void_p)]
+    L.sf21_hii_destroy.argtypes = [vp]
+    L.sf21_hii_last_error.argtypes = [vp]
+    L.sf21_hii_last_error.restype = ctypes.c_char_p
+    L.sf21_hii_run_z.argtypes = [vp, ctypes.c_double, ctypes.c_int, fp, fp, fp, dp]
+    L.sf21_hii_run_z_device.argtypes = [vp, ctypes.c_double, ctypes.c_int, vp, vp, vp, vp]
+    L.sf21_hii_radii.argtypes = [vp, ctypes.c_int, dp, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+    L.sf21_hii_prologue.argtypes = [vp, ctypes.c_double, ctypes.c_int, fp, fp, ctypes.c_int, fp, fp, fp]
+    L.sf21_hii_filtered.argtypes = [vp, ctypes.c_double, ctypes.c_int, fp, fp, ctypes.c_int,
+                                    ctypes.c_int, fp, fp]
+    L.sf21_hii_first_hit.argtypes = [vp, ctypes.c_double, ctypes.c_int, fp, fp, ctypes.c_int, fp]
+    L.sf21_hii_profile.argtypes = [vp, ctypes.c_int]
+    L.sf21_hii_profile_read.argtypes = [vp, dp, ctypes.POINTER(ctypes.c_long), ctypes.c_int]
+    L.sf21_hii_profile_name.argtypes = [ctypes.c_int]
+    L.sf21_hii_profile_name.restype = ctypes.c_char_p
+    _lib = L
+    return L
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+def _f32(a, n3):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    if a.size != n3:
+        raise ValueError(f"box has {a.size} elements, expected {n3}")
+    return a
+
+
+@dataclass
+class ParamSet:
+    fesc: float
+    Rmax: float  # Mpc/h, clamped to L/2 by the caller (Input_variables.c:124)
+    Nbins: int
+
+
+class FilterBank:
+    """One GPU context for a box size and a list of parameter sets."""
+
+    def __init__(self, N: int, L: float, hubble: float, sets, N_halo: int = 0, device: int = 0,
+                 kmax: int = 0):
+        self._lib = load_library()
+        self.N = int(N)
+        self.n3 = self.N ** 3
+        self.sets = [s if isinstance(s, ParamSet) else ParamSet(*s) for s in sets]
+        arr = (_Set * len(self.sets))(*[_Set(s.fesc, s.Rmax, s.Nbins) for s in self.sets])
+        self._arr = arr
+        cfg = _Config(N=self.N, N_halo=N_halo or self.N, L=L, hubble=hubble, device=device,
+                      nsets=len(self.sets), sets=arr, kmax=kmax)
+        h = ctypes.c_void_p()
+        rc = self._lib.sf21_hii_create(ctypes.byref(cfg), ctypes.byref(h))
+        if rc != 0:
+            raise HIIError(rc, self._lib.sf21_hii_last_error(None).decode())
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.sf21_hii_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != 0:
+            raise HIIError(rc, self._lib.sf21_hii_last_error(self._h).decode())
+
+    def radii(self, s: int = 0):
+        buf = (ctypes.c_double * 512)()
+        nf = ctypes.c_int(0)
+        n = self._lib.sf21_hii_radii(self._h, s, buf, 512, ctypes.byref(nf))
+        if n < 0:
+            raise HIIError(-n, "bad set index")
+        return [buf[i] for i in range(n)], nf.value
+
+    def run_z(self, z: float, delta, src, src_kind: int = SF21_SRC_SFRD):
+        """xHII boxes (nsets, N, N, N) and neutral fractions (nsets,)."""
+        d = _f32(delta, self.n3)
+        s = _f32(src, self.n3)
+        out = np.empty((len(self.sets), self.N, self.N, self.N), np.float32)
+        neutral = (ctypes.c_double * len(self.sets))()
+        self._check(self._lib.sf21_hii_run_z(self._h, z, src_kind, _ptr(d), _ptr(s), _ptr(out), neutral))
+        return out, np.array(neutral[:], dtype=np.float64)
+
+    def run_z_device(self, z: float, delta_ptr: int, src_ptr: int, xhii_ptr: int,
+                     src_kind: int = SF21_SRC_SFRD, stream: int = 0):
+        """Device-resident variant: raw device pointers (e.g. torch tensor
+        .data_ptr()); enqueues on `stream` (0 = the context's own stream)."""
+        self._check(self._lib.sf21_hii_run_z_device(self._h, z, src_kind, ctypes.c_void_p(delta_ptr),
+                                                    ctypes.c_void_p(src_ptr), ctypes.c_void_p(xhii_ptr),
+                                                    ctypes.c_void_p(stream or None)))
+
+    def prologue(self, z: float, delta, src, s: int = 0, src_kind: int = SF21_SRC_SFRD):
+        d = _f32(delta, self.n3)
+        sr = _f32(src, self.n3)
+        shp = (self.N,) * 3
+        rec0, fres, fill0 = (np.empty(shp, np.float32) for _ in range(3))
+        self._check(self._lib.sf21_hii_prologue(self._h, z, src_kind, _ptr(d), _ptr(sr), s,
+                                                _ptr(rec0), _ptr(fres), _ptr(fill0)))
+        return rec0, fres, fill0
+
+    def filtered(self, z: float, delta, src, ridx: int, s: int = 0, src_kind: int = SF21_SRC_SFRD):
+        d = _f32(delta, self.n3)
+        sr = _f32(src, self.n3)
+        shp = (self.N,) * 3
+        rec, ion = np.empty(shp, np.float32), np.empty(shp, np.float32)
+        self._check(self._lib.sf21_hii_filtered(self._h, z, src_kind, _ptr(d), _ptr(sr), s, ridx,
+                                                _ptr(rec), _ptr(ion)))
+        return rec, ion
+
+    def first_hit(self, z: float, delta, src, s: int = 0, src_kind: int = SF21_SRC_SFRD):
+        d = _f32(delta, self.n3)
+        sr = _f32(src, self.n3)
+        rc = np.empty((self.N,) * 3, np.uint8)
+        self._check(self._lib.sf21_hii_first_hit(self._h, z, src_kind, _ptr(d), _ptr(sr), s, _ptr(rc)))
+        return rc
+
+    # ---- measurement hooks -------------------------------------------------
+    def profile(self, enable: bool = True):
+        """Start (and reset) per-kernel CUDA-event timing on the launch stream."""
+        self._check(self._lib.sf21_hii_profile(self._h, 1 if enable else 0))
+
+    def profile_read(self):
+        """{kernel kind: (total ms, launches)} since profile(True)."""
+        ms = (ctypes.c_double * 32)()
+        n = (ctypes.c_long * 32)()
+        k = self._lib.sf21_hii_profile_read(self._h, ms, n, 32)
+        if k < 0:
+            self._check(-k)
+        return {self._lib.sf21_hii_profile_name(i).decode(): (ms[i], n[i]) for i in range(k)}

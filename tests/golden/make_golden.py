@@ -1,0 +1,96 @@
+"""Generate the golden fixtures of the HII stage from the reference itself.
+
+Runs the reference's own get_HIIbubbles.c, compiled unmodified from its
+sources by ``make -C oracle ref`` (against the FFTW-API shim and a GSL stub),
+on seeded synthetic base directories, and stores inputs and outputs as
+compressed .npz files next to this script:
+
+  hii_n32_sfr.npz   N=32,  L=25 Mpc/h, z = 7, 8 (SFR boxes, use_SFR = T)
+  hii_n64_sfr.npz   N=64,  L=50 Mpc/h, z = 8
+  hii_n32_halo.npz  N=32 (N_halo=64), L=25 Mpc/h, z = 8 (halo catalogue, use_SFR = F)
+
+Each holds the ini values, the input boxes per redshift, the xHII boxes the
+reference wrote, and its x_HI text output.  Needs the reference sources (only
+in the build container); the GPU tests read the committed .npz files.
+Usage: python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.abspath(os.path.join(HERE, "..", ".."))
+sys.path.insert(0, ROOT)
+
+from oracle import oracle as O  # noqa: E402
+from simfast21_gb300 import params as P  # noqa: E402
+from simfast21_gb300 import synth  # noqa: E402
+
+
+def run_ref(base: str):
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True)
+    r = subprocess.run([O.REF_EXE, base], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(r.stdout + r.stderr)
+    return r.stdout
+
+
+def case_sfr(name: str, N: int, L: float, zmin: float, zmax: float, seed: int):
+    w = synth.Workload(N=N, L=L, zs=[], zeta=30.0, Rmax=L / 2, factor=1.1, seed=seed)
+    base = tempfile.mkdtemp(prefix="sf21gold_")
+    try:
+        zs = synth.write_base_dir(base, w, zmin, zmax, 1.0, nthreads=4)
+        log = run_ref(base)
+        sp = P.derive(P.read_ini(os.path.join(base, "simfast21.ini")))
+        out = {"ini": open(os.path.join(base, "simfast21.ini")).read(), "zs": np.array(zs)}
+        for i, z in enumerate(zs):
+            for kind in ("delta", "sfrd", "xHII"):
+                out[f"{kind}_{i}"] = np.fromfile(os.path.join(base, synth.box_name(kind, z, N, sp.L_file)),
+                                                 np.float32).reshape(N, N, N)
+        xhi = open(os.path.join(base, "Output_text_files", f"x_HI_N{N}_L{sp.L_file:.1f}.dat")).read()
+        out["x_HI_txt"] = xhi
+        out["stdout"] = log
+        np.savez_compressed(os.path.join(HERE, name), **out)
+        print(name, "z =", zs, "x_HI =", xhi.split())
+    finally:
+        shutil.rmtree(base)
+
+
+def case_halo(name: str, N: int, N_halo: int, L: float, z: float, seed: int):
+    w = synth.Workload(N=N, L=L, zs=[z], zeta=0.6, Rmax=L / 2, factor=1.1, seed=seed)
+    base = tempfile.mkdtemp(prefix="sf21gold_")
+    try:
+        os.makedirs(os.path.join(base, "delta"))
+        os.makedirs(os.path.join(base, "Halos"))
+        with open(os.path.join(base, "simfast21.ini"), "w") as f:
+            f.write(synth.ini_text(w, z, z, 1.0, nthreads=4, use_sfr=False, n_halo=N_halo))
+        sp = P.derive(P.read_ini(os.path.join(base, "simfast21.ini")))
+        g = synth.gaussian_field(N, seed)
+        delta = synth.lognormal_delta(g, w.sigma)
+        cat = synth.halo_catalogue(delta, seed + 1, n_halo=N_halo)
+        delta.tofile(os.path.join(base, synth.box_name("delta", z, N, sp.L_file)))
+        cname = f"Halos/halonl_z{z:.3f}_N{N_halo}_L{sp.L_file:.1f}.dat.catalog"
+        with open(os.path.join(base, cname), "wb") as f:
+            np.array([len(cat)], dtype=np.int64).tofile(f)
+            cat.tofile(f)
+        log = run_ref(base)
+        xhii = np.fromfile(os.path.join(base, synth.box_name("xHII", z, N, sp.L_file)), np.float32)
+        xhi = open(os.path.join(base, "Output_text_files", f"x_HI_N{N}_L{sp.L_file:.1f}.dat")).read()
+        np.savez_compressed(os.path.join(HERE, name), ini=open(os.path.join(base, "simfast21.ini")).read(),
+                            zs=np.array([z]), delta_0=delta, catalogue=cat,
+                            xHII_0=xhii.reshape(N, N, N), x_HI_txt=xhi, stdout=log)
+        print(name, "halos", len(cat), "x_HI =", xhi.split())
+    finally:
+        shutil.rmtree(base)
+
+
+if __name__ == "__main__":
+    case_sfr("hii_n32_sfr.npz", 32, 25.0, 7.0, 8.0, seed=101)
+    case_sfr("hii_n64_sfr.npz", 64, 50.0, 8.0, 8.0, seed=202)
+    case_halo("hii_n32_halo.npz", 32, 64, 25.0, 8.0, seed=303)

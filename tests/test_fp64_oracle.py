@@ -1,0 +1,49 @@
+"""The exact dilation of the FP64 oracle against the reference algorithm."""
+import numpy as np
+
+from helpers import load_golden, oracle_params
+from oracle import fp64_oracle as F
+from simfast21_gb300 import params as P
+
+
+def test_dilate_matches_brute_force():
+    rng = np.random.default_rng(3)
+    N = 12
+    v = np.full((N, N, N), -1, np.int64)
+    idx = rng.integers(0, N, size=(6, 3))
+    vals = rng.integers(0, 30, size=6)
+    for (a, b, c), val in zip(idx, vals):
+        v[a, b, c] = val
+    got = F.dilate(v)
+    ax = np.arange(N)
+    dmin = lambda u, w: np.minimum(np.abs(u - w), N - np.abs(u - w))
+    want = np.zeros((N, N, N), bool)
+    for (a, b, c), val in zip(idx, vals):
+        n = dmin(ax, a)[:, None, None] ** 2 + dmin(ax, b)[None, :, None] ** 2 + dmin(ax, c)[None, None, :] ** 2
+        want |= n <= val
+    assert np.array_equal(got, want)
+
+
+def test_exact_dilation_reproduces_reference(oracle_lib):
+    """On every voxel whose outcome no near-threshold decision can change, the
+    reference's FP32 FFT convolution and painting give the exact dilation."""
+    O = oracle_lib
+    g = load_golden("hii_n64_sfr.npz")
+    sp = g["params"]
+    p = oracle_params(O, sp)
+    out = O.run_z_sfr(p, float(g["zs"][0]), g["delta_0"], g["sfrd_0"], extras=True)
+    radii, _ = P.radii(sp.Rmax, sp.dx, sp.Nbins)
+    b = F.bands(out["rec0"], out["ion0"], radii, sp.dx, sp.dk)
+    lo = F.finish(b["ionised_lo"], out["fill0"], out["fresid"])
+    hi = F.finish(b["ionised_hi"], out["fill0"], out["fresid"])
+    x = g["xHII_0"]
+    assert np.all((x == lo) | (x == hi))
+    certain = b["ionised_lo"] == b["ionised_hi"]
+    assert certain.mean() > 0.999
+
+
+def test_nmax_definition():
+    dx = 0.7
+    for R in (0.7, 1.0, 1.39, 2.1, 7.77, 30.0):
+        n = P.nmax(R, dx)
+        assert np.sqrt(float(n)) * dx <= R and not (np.sqrt(float(n + 1)) * dx <= R)

@@ -1,0 +1,144 @@
+"""Parity of the CUDA library (through its C-ABI) with the oracle.
+
+* prologue boxes bit-exact with the CPU restatement (which is byte-identical
+  to the reference's own get_HIIbubbles.c on the golden fixtures);
+* filtered fields within 1e-5 of the field's max |value| of the FP64 oracle;
+* first-hit radius inside the FP64 oracle's certain/possible bounds;
+* xHII bit-identical with the reference's output on every voxel whose outcome
+  no centre decision within 1e-5 relative of the threshold can change; the
+  remaining (band) voxels equal one of the two admissible outcomes.
+"""
+import numpy as np
+import pytest
+
+from helpers import load_golden, oracle_params
+from oracle import fp64_oracle as F
+from simfast21_gb300 import params as P, synth
+
+pytestmark = pytest.mark.gpu
+
+TOL_BAND = 1e-5   # relative distance of h/d from 1 (spec tolerance band)
+TOL_FIELD = 1e-5  # filtered fields, relative to the field's max |value|
+
+
+def _bank(H, sp, sets=None):
+    sets = sets or [(sp.fesc, sp.Rmax, sp.Nbins)]
+    return H.FilterBank(sp.N, sp.L, sp.hubble, sets, N_halo=sp.N_halo)
+
+
+def _case(name):
+    g = load_golden(name)
+    return g, g["params"]
+
+
+@pytest.mark.parametrize("name", ["hii_n32_sfr.npz", "hii_n64_sfr.npz"])
+def test_prologue_bit_exact(hii, oracle_lib, name):
+    g, sp = _case(name)
+    fb = _bank(hii, sp)
+    p = oracle_params(oracle_lib, sp)
+    for i, z in enumerate(g["zs"]):
+        rec0, fres, fill0 = fb.prologue(float(z), g[f"delta_{i}"], g[f"sfrd_{i}"])
+        ref = oracle_lib.run_z_sfr(p, float(z), g[f"delta_{i}"], g[f"sfrd_{i}"], extras=True)
+        for got, want in ((rec0, ref["rec0"]), (fres, ref["fresid"]), (fill0, ref["fill0"])):
+            assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+def test_filtered_fields_vs_fp64(hii, oracle_lib):
+    g, sp = _case("hii_n64_sfr.npz")
+    fb = _bank(hii, sp)
+    z = float(g["zs"][0])
+    ref = oracle_lib.run_z_sfr(oracle_params(oracle_lib, sp), z, g["delta_0"], g["sfrd_0"], extras=True)
+    radii, nf = fb.radii()
+    for ridx in sorted({0, nf // 2, nf - 1, nf, len(radii) - 1}):
+        rec, ion = fb.filtered(z, g["delta_0"], g["sfrd_0"], ridx)
+        d64, h64 = F.filtered_fields(ref["rec0"], ref["ion0"], radii[ridx], sp.dk)
+        assert np.abs(rec - d64).max() <= TOL_FIELD * np.abs(d64).max()
+        assert np.abs(ion - h64).max() <= TOL_FIELD * np.abs(h64).max()
+
+
+def _bounds(oracle_lib, sp, z, delta, sfrd):
+    ref = oracle_lib.run_z_sfr(oracle_params(oracle_lib, sp), z, delta, sfrd, extras=True)
+    radii, _ = P.radii(sp.Rmax, sp.dx, sp.Nbins)
+    b = F.bands(ref["rec0"], ref["ion0"], radii, sp.dx, sp.dk, tol=TOL_BAND)
+    lo = F.finish(b["ionised_lo"], ref["fill0"], ref["fresid"])
+    hi = F.finish(b["ionised_hi"], ref["fill0"], ref["fresid"])
+    return ref, b, lo, hi
+
+
+@pytest.mark.parametrize("name", ["hii_n32_sfr.npz", "hii_n64_sfr.npz"])
+def test_xhii_matches_reference_outside_band(hii, oracle_lib, name):
+    g, sp = _case(name)
+    fb = _bank(hii, sp)
+    xhi_ref = [float(v) for v in str(g["x_HI_txt"]).split()][::-1]
+    for i, z in enumerate(g["zs"]):
+        z = float(z)
+        x, neutral = fb.run_z(z, g[f"delta_{i}"], g[f"sfrd_{i}"])
+        x = x[0]
+        ref_x = g[f"xHII_{i}"]
+        _, b, lo, hi = _bounds(oracle_lib, sp, z, g[f"delta_{i}"], g[f"sfrd_{i}"])
+        certain = b["ionised_lo"] == b["ionised_hi"]
+        assert np.array_equal(x[certain].view(np.uint32), ref_x[certain].view(np.uint32))
+        assert np.all((x == lo) | (x == hi))
+        n_diff = int((x != ref_x).sum())
+        assert n_diff <= int((~certain).sum())
+        if n_diff == 0:
+            assert "%f" % neutral[0] == "%f" % xhi_ref[i]
+
+
+@pytest.mark.parametrize("name", ["hii_n32_sfr.npz", "hii_n64_sfr.npz"])
+def test_first_hit_within_bounds(hii, oracle_lib, name):
+    g, sp = _case(name)
+    fb = _bank(hii, sp)
+    z = float(g["zs"][0])
+    rc = fb.first_hit(z, g["delta_0"], g["sfrd_0"])
+    _, b, _, _ = _bounds(oracle_lib, sp, z, g["delta_0"], g["sfrd_0"])
+    # possible centres come first: rc_hi <= rc <= rc_lo (255 = never)
+    assert np.all(b["rc_hi"] <= rc) and np.all(rc <= b["rc_lo"])
+
+
+def test_xhii_128_vs_cpu_restatement(hii, oracle_lib):
+    """Plain-method box (128^3, L=100 Mpc/h, zeta=30, z=8, Rmax=50, factor 1.1)."""
+    w = synth.Workload(N=128, L=100.0, zs=[8.0], zeta=30.0, Rmax=50.0, factor=1.1, seed=1235)
+    delta, sfrd = synth.make_boxes(w, 8.0)
+    sp = P.StageParams(nthreads=8, zmin=8.0, zmax=8.0, dz=1.0, L=100.0, hubble=0.71, N_halo=128, N=128,
+                       fesc=30.0, xHlim=0.999, Rmax=50.0, Nbins=w.Nbins, use_sfr=True)
+    fb = _bank(hii, sp)
+    x, neutral = fb.run_z(8.0, delta, sfrd)
+    ref, b, lo, hi = _bounds(oracle_lib, sp, 8.0, delta, sfrd)
+    certain = b["ionised_lo"] == b["ionised_hi"]
+    assert np.array_equal(x[0][certain].view(np.uint32), ref["xhii"][certain].view(np.uint32))
+    assert np.all((x[0] == lo) | (x[0] == hi))
+
+
+def test_parameter_sets_share_one_transform(hii):
+    """A multi-set context gives each set exactly its single-set result."""
+    w = synth.Workload(N=64, L=50.0, zs=[7.0], zeta=30.0, Rmax=25.0, factor=1.05, seed=9)
+    delta, sfrd = synth.make_boxes(w, 7.0)
+    sets = [(12.0, 10.0, 20), (30.0, 20.0, 33), (80.0, 25.0, 41)]
+    fb = hii.FilterBank(64, 50.0, 0.71, sets)
+    x_all, n_all = fb.run_z(7.0, delta, sfrd)
+    for s, st in enumerate(sets):
+        one = hii.FilterBank(64, 50.0, 0.71, [st])
+        x1, n1 = one.run_z(7.0, delta, sfrd)
+        assert np.array_equal(x_all[s].view(np.uint32), x1[0].view(np.uint32))
+        assert n_all[s] == n1[0]
+
+
+def test_halo_catalogue_branch(hii, oracle_lib):
+    g, sp = _case("hii_n32_halo.npz")
+    p = oracle_params(oracle_lib, sp)
+    z = float(g["zs"][0])
+    smoothed = oracle_lib.halo_smoothed(p, z, g["catalogue"])
+    fb = _bank(hii, sp)
+    x, _ = fb.run_z(z, g["delta_0"], smoothed, src_kind=hii.SF21_SRC_RION)
+    ref_x = g["xHII_0"]
+    rion = oracle_lib.halo_source(p, z, g["catalogue"])
+    ref = oracle_lib.run_z_sfr  # noqa: F841  (kept for symmetry)
+    o = oracle_lib.run_z_rion(p, z, g["delta_0"], rion)
+    assert np.array_equal(o["xhii"].view(np.uint32), ref_x.view(np.uint32))
+    # GPU vs reference outside the band
+    radii, _ = P.radii(sp.Rmax, sp.dx, sp.Nbins)
+    rec0, fres, fill0 = fb.prologue(z, g["delta_0"], smoothed, src_kind=hii.SF21_SRC_RION)
+    b = F.bands(rec0, rion, radii, sp.dx, sp.dk, tol=TOL_BAND)
+    certain = b["ionised_lo"] == b["ionised_hi"]
+    assert np.array_equal(x[0][certain].view(np.uint32), ref_x[certain].view(np.uint32))
