@@ -200,7 +200,8 @@ def run_ours(args, w, rank, world):
     d_delta = torch.from_numpy(delta).cuda()
     d_src = torch.from_numpy(sfrd).cuda()
     d_x = torch.empty((nsets, N, N, N), dtype=torch.float32, device="cuda")
-    stream = torch.cuda.current_stream()
+    # a dedicated stream: the library's kernels and the timing events share it
+    stream = torch.cuda.Stream()
     sptr = stream.cuda_stream
 
     def step():
@@ -210,6 +211,7 @@ def run_ours(args, w, rank, world):
         if world > 1:
             torch.distributed.barrier()
 
+    torch.cuda.synchronize()
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()

@@ -10,8 +10,9 @@ min-image metric, of a centre at R) -- the set the reference's threshold at
 :391-392 selects whenever its FP32 rounding stays below 0.01 of a count.
 
 ``bands`` classifies each (voxel, radius) decision by how far the criterion
-h/d is from its threshold 1: outside the relative band ``tol`` the decision
-is certain; inside it either answer is acceptable.  From the certain and the
+is from its threshold: h/d within ``tol`` (relative) of 1, or a sign test on
+a field value within ``field_tol`` of the field's max |value| of 0, makes
+the decision uncertain and either answer is acceptable.  From the certain and the
 possible centres it builds the lowest and highest first-hit radius index per
 voxel and the dilations of both, which bound every FP32 realisation (GPU or
 CPU) of the stage.
@@ -84,14 +85,21 @@ def dilate(v: np.ndarray) -> np.ndarray:
     return cur >= 0
 
 
-def bands(rec0, ion0, radii, dx: float, dk: float, tol: float = 1e-5, keep_fields: bool = False):
+def bands(rec0, ion0, radii, dx: float, dk: float, tol: float = 1e-5, field_tol: float = 1e-6,
+          keep_fields: bool = False):
     """Certain / possible first-hit radius indices and dilations.
+
+    A centre decision (h > 0 and (d <= 0 or h/d >= 1), :339-348) is evaluated
+    over every realisation within the tolerances: h and d each within
+    field_tol * max|field| of the float64 value (the FP32 rounding of any
+    transform, the reference's FFTW one included), and the ratio h/d within
+    tol (relative) of its threshold 1.  `certain` holds for all of them,
+    `possible` for at least one.
 
     Returns dict with rc_lo (index of the first certain centre, 255 = none),
     rc_hi (first possible centre), ionised_lo, ionised_hi (bool boxes),
-    n_band (number of (voxel, radius) decisions inside the band) and, if
-    keep_fields, the float64 filtered fields per radius."""
-    N = rec0.shape[0]
+    n_band (number of (voxel, radius) decisions that are possible but not
+    certain) and, if keep_fields, the float64 filtered fields per radius."""
     rc_lo = np.full(rec0.shape, 255, np.uint8)
     rc_hi = np.full(rec0.shape, 255, np.uint8)
     n_band = 0
@@ -100,10 +108,10 @@ def bands(rec0, ion0, radii, dx: float, dk: float, tol: float = 1e-5, keep_field
         d, h = filtered_fields(rec0, ion0, R, dk)
         if keep_fields:
             fields.append((d, h))
-        with np.errstate(divide="ignore", invalid="ignore"):
-            ratio = np.where(d > 0, h / d, np.inf)
-        certain = (h > 0) & ((d <= 0) | (ratio >= 1.0 + tol))
-        possible = (h > 0) & ((d <= 0) | (ratio >= 1.0 - tol))
+        eh = field_tol * float(np.abs(h).max())
+        ed = field_tol * float(np.abs(d).max())
+        possible = (h + eh > 0) & ((d - ed <= 0) | (h + eh >= (d - ed) * (1.0 - tol)))
+        certain = (h - eh > 0) & ((d + ed <= 0) | (h - eh >= (d + ed) * (1.0 + tol)))
         n_band += int((possible & ~certain).sum())
         rc_lo[(rc_lo == 255) & certain] = i
         rc_hi[(rc_hi == 255) & possible] = i

@@ -17,6 +17,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libsf21hii.so")
+DRIVER = os.path.join(HERE, "sf21_hii")
+DRIVER_SRC = [os.path.join(HERE, "driver", f) for f in ("sf21_hii_main.c", "sf21_stage.c")]
 SOURCES = ["kernels_fft.cu", "kernels_elem.cu", "hii_api.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3"]
@@ -29,18 +31,39 @@ def nvcc() -> str:
     raise RuntimeError("nvcc not found (CUDA toolkit required to build libsf21hii.so)")
 
 
-def _deps_mtime() -> float:
+def _deps_mtime(roots=None) -> float:
     t = 0.0
-    for root in (CSRC, os.path.join(HERE, "..", "include")):
+    for root in roots or (CSRC, os.path.join(HERE, "..", "include")):
         for f in os.listdir(root):
-            if f.endswith((".cu", ".cuh", ".h")):
+            if f.endswith((".cu", ".cuh", ".h", ".c")):
                 t = max(t, os.path.getmtime(os.path.join(root, f)))
     return t
 
 
+def build_driver(force: bool = False) -> str:
+    """The sf21_hii executable (drop-in for get_HIIbubbles.x), linked to the
+    library with an $ORIGIN rpath."""
+    deps = max(_deps_mtime([os.path.join(HERE, "driver"), os.path.join(HERE, "..", "include")]),
+               os.path.getmtime(LIB))
+    if not force and os.path.exists(DRIVER) and os.path.getmtime(DRIVER) >= deps:
+        return DRIVER
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        raise RuntimeError("no C compiler for the sf21_hii driver")
+    cmd = [cc, "-O2", "-std=c99", "-ffp-contract=off", "-Wall", "-I", os.path.join(HERE, "..", "include"),
+           *DRIVER_SRC, "-o", DRIVER + ".tmp", "-L", HERE, "-lsf21hii", "-Wl,-rpath,$ORIGIN", "-lm"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"driver build failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(DRIVER + ".tmp", DRIVER)
+    return DRIVER
+
+
 def build(force: bool = False, verbose: bool = False) -> str:
-    """Compile and link libsf21hii.so; returns its path."""
+    """Compile and link libsf21hii.so and the sf21_hii driver; returns the
+    library path."""
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _deps_mtime():
+        build_driver()
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     cc = nvcc()
@@ -63,6 +86,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_driver(force=True)
     return LIB
 
 

@@ -72,7 +72,7 @@ struct sf21_hii_ctx {
   float2 *d_spec = nullptr, *d_tw = nullptr;
   std::vector<float2*> d_work;
   uint8_t* d_rc = nullptr;
-  PrologueArgs* d_pa = nullptr;
+  PrologueArgs pa;   // scalars of the redshift being processed (kernel arguments)
   int pro_blocks = 0;
   std::string err;
   // optional per-kernel timing (CUDA events on the launch stream)
@@ -158,7 +158,7 @@ static void free_ctx(sf21_hii_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
   void* ptrs[] = {c->d_delta, c->d_src, c->d_rec0, c->d_fres, c->d_partials, c->d_alpha,
-                  c->d_xhii, c->d_spec, c->d_tw, c->d_rc, c->d_pa};
+                  c->d_xhii, c->d_spec, c->d_tw, c->d_rc};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (float2* w : c->d_work)
@@ -269,7 +269,6 @@ extern "C" int sf21_hii_create(const sf21_hii_config* cfg, sf21_hii_ctx** out) {
   c->pro_blocks = prologue_blocks(c->n3);
   CREATE_CUDA(cudaMalloc(&c->d_partials, sizeof(float) * 2 * c->pro_blocks));
   CREATE_CUDA(cudaMalloc(&c->d_alpha, sizeof(float)));
-  CREATE_CUDA(cudaMalloc(&c->d_pa, sizeof(PrologueArgs)));
   // twiddles exp(-2 pi i t / N) in double, rounded once
   std::vector<float2> tw(N);
   for (long t = 0; t < N; ++t) {
@@ -307,16 +306,14 @@ extern "C" int sf21_hii_radii(const sf21_hii_ctx* ctx, int set, double* R, int c
 // ---- schedule pieces --------------------------------------------------------
 static int enqueue_front(sf21_hii_ctx* c, double z, int kind, const float* delta, const float* src,
                          cudaStream_t st) {
-  PrologueArgs pa;
-  int rc = prologue_args(c, z, kind, &pa);
+  int rc = prologue_args(c, z, kind, &c->pa);
   if (rc) return rc;
-  CTX_CUDA(c, cudaMemcpyAsync(c->d_pa, &pa, sizeof(pa), cudaMemcpyHostToDevice, st));
   float2* packed = c->d_work[0];
   const int N = (int)c->N;
   Batch none;
   memset(&none, 0, sizeof(none));
   int e0 = mark(c, st);
-  CTX_CUDA(c, launch_prologue(c->n3, delta, src, c->d_pa, c->d_rec0, c->d_fres, packed, c->d_partials,
+  CTX_CUDA(c, launch_prologue(c->n3, delta, src, c->pa, c->d_rec0, c->d_fres, packed, c->d_partials,
                               c->pro_blocks, st));
   int e1 = mark(c, st);
   CTX_CUDA(c, launch_alpha(c->d_partials, c->pro_blocks, c->d_alpha, st));
@@ -375,7 +372,7 @@ static int enqueue_finish(sf21_hii_ctx* c, int set, const float* src, float* xhi
   int e1 = mark(c, st);
   CTX_CUDA(c, launch_dt_b(N, dt0, s.vmax, dt1, st));
   int e2 = mark(c, st);
-  CTX_CUDA(c, launch_dt_a_finish(N, dt1, s.vmax, dbits(s.fesc), src, c->d_rec0, c->d_fres, c->d_pa, xhii, st));
+  CTX_CUDA(c, launch_dt_a_finish(N, dt1, s.vmax, dbits(s.fesc), src, c->d_rec0, c->d_fres, c->pa, xhii, st));
   int e3 = mark(c, st);
   span(c, KD_DTR, e0, e1);
   span(c, KD_DTB, e1, e2);
@@ -460,7 +457,7 @@ extern "C" int sf21_hii_prologue(sf21_hii_ctx* c, double z, int kind, const floa
   int rc = upload_front(c, z, kind, delta, src);
   if (rc) return rc;
   const size_t bf = sizeof(float) * c->n3;
-  CTX_CUDA(c, launch_fill0(c->n3, dbits(c->sets[set].fesc), c->d_src, c->d_rec0, c->d_pa, c->d_xhii, c->stream));
+  CTX_CUDA(c, launch_fill0(c->n3, dbits(c->sets[set].fesc), c->d_src, c->d_rec0, c->pa, c->d_xhii, c->stream));
   if (rec0) CTX_CUDA(c, cudaMemcpyAsync(rec0, c->d_rec0, bf, cudaMemcpyDeviceToHost, c->stream));
   if (fresid) CTX_CUDA(c, cudaMemcpyAsync(fresid, c->d_fres, bf, cudaMemcpyDeviceToHost, c->stream));
   if (fill0) CTX_CUDA(c, cudaMemcpyAsync(fill0, c->d_xhii, bf, cudaMemcpyDeviceToHost, c->stream));

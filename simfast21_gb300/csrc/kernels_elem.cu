@@ -45,9 +45,8 @@ constexpr int PRO_THREADS = 256;
 
 __global__ void __launch_bounds__(PRO_THREADS)
 k_prologue(long n3, const float* __restrict__ delta, const float* __restrict__ src,
-           const PrologueArgs* __restrict__ pap, float* __restrict__ rec0, float* __restrict__ fres,
+           const PrologueArgs pa, float* __restrict__ rec0, float* __restrict__ fres,
            float2* __restrict__ packed, float* __restrict__ partials) {
-  const PrologueArgs pa = *pap;
   float sd2 = 0.f, sh2 = 0.f;
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += (long)gridDim.x * blockDim.x) {
     const float d = delta[i];
@@ -94,7 +93,7 @@ int prologue_blocks(long n3) {
   return (int)(b < 152 * 16 ? b : 152 * 16);
 }
 
-cudaError_t launch_prologue(long n3, const float* delta, const float* src, const PrologueArgs* pa,
+cudaError_t launch_prologue(long n3, const float* delta, const float* src, const PrologueArgs& pa,
                             float* rec0, float* fres, float2* packed, float* partials, int nblocks,
                             cudaStream_t st) {
   k_prologue<<<nblocks, PRO_THREADS, 0, st>>>(n3, delta, src, pa, rec0, fres, packed, partials);
@@ -209,10 +208,9 @@ __global__ void k_dt_b(int N, const int* __restrict__ in, int vmax, int* __restr
 // pass along a (stride N^2) fused with the finish of the xHII box.
 __global__ void k_dt_a_finish(int N, const int* __restrict__ in, int vmax, sd_t zeta,
                               const float* __restrict__ src, const float* __restrict__ rec0,
-                              const float* __restrict__ fres, const PrologueArgs* __restrict__ pap,
+                              const float* __restrict__ fres, const PrologueArgs pa,
                               float* __restrict__ xhii) {
   extern __shared__ int stile[];  // [N][DT_CW]
-  const PrologueArgs pa = *pap;
   const int nblk = N / DT_CW;
   const long b = blockIdx.x / nblk;
   const int c0 = (blockIdx.x % nblk) * DT_CW;
@@ -255,8 +253,7 @@ __global__ void k_dt_a_finish(int N, const int* __restrict__ in, int vmax, sd_t 
 
 // Single-cell fill alone (check hook): :281-288 without dilation and cap.
 __global__ void k_fill0(long n3, sd_t zeta, const float* __restrict__ src, const float* __restrict__ rec0,
-                        const PrologueArgs* __restrict__ pap, float* __restrict__ fill) {
-  const PrologueArgs pa = *pap;
+                        const PrologueArgs pa, float* __restrict__ fill) {
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += (long)gridDim.x * blockDim.x) {
     const float h = sd_to_float(sd_mul(src_chain(src[i], pa), zeta));
     const float d = rec0[i];
@@ -270,7 +267,7 @@ __global__ void k_fill0(long n3, sd_t zeta, const float* __restrict__ src, const
 }
 
 cudaError_t launch_fill0(long n3, uint64_t zeta, const float* src, const float* rec0,
-                         const PrologueArgs* pa, float* fill, cudaStream_t st) {
+                         const PrologueArgs& pa, float* fill, cudaStream_t st) {
   k_fill0<<<prologue_blocks(n3), PRO_THREADS, 0, st>>>(n3, zeta, src, rec0, pa, fill);
   return cudaGetLastError();
 }
@@ -297,7 +294,7 @@ cudaError_t launch_dt_b(int N, const int* in, int vmax, int* out, cudaStream_t s
 }
 
 cudaError_t launch_dt_a_finish(int N, const int* in, int vmax, uint64_t zeta, const float* src, const float* rec0,
-                               const float* fres, const PrologueArgs* pa, float* xhii, cudaStream_t st) {
+                               const float* fres, const PrologueArgs& pa, float* xhii, cudaStream_t st) {
   k_dt_a_finish<<<dt_grid(N), dt_threads(N), (size_t)N * DT_CW * sizeof(int), st>>>(N, in, vmax, zeta, src, rec0,
                                                                                   fres, pa, xhii);
   return cudaGetLastError();

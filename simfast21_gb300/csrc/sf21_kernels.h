@@ -36,8 +36,7 @@ cudaError_t launch_cols(int N, float2* box, const Batch& bt, int nbox, int axis,
 cudaError_t launch_cols_a_test(int N, const Batch& bt, uint8_t* rc, const float* alpha, const float2* tw,
                                cudaStream_t st);
 
-// pa points to device memory (so a captured graph can be replayed per z).
-cudaError_t launch_prologue(long n3, const float* delta, const float* src, const PrologueArgs* pa,
+cudaError_t launch_prologue(long n3, const float* delta, const float* src, const PrologueArgs& pa,
                             float* rec0, float* fres, float2* packed, float* partials, int nblocks,
                             cudaStream_t st);
 cudaError_t launch_alpha(const float* partials, int nblocks, float* alpha, cudaStream_t st);
@@ -50,8 +49,8 @@ cudaError_t dilate_setup(int N);
 cudaError_t launch_dt_rows(int N, const uint8_t* rc, const int* nmax, int vmax, int* out, cudaStream_t st);
 cudaError_t launch_dt_b(int N, const int* in, int vmax, int* out, cudaStream_t st);
 cudaError_t launch_dt_a_finish(int N, const int* in, int vmax, uint64_t zeta, const float* src, const float* rec0,
-                               const float* fres, const PrologueArgs* pa, float* xhii, cudaStream_t st);
+                               const float* fres, const PrologueArgs& pa, float* xhii, cudaStream_t st);
 cudaError_t launch_fill0(long n3, uint64_t zeta, const float* src, const float* rec0,
-                         const PrologueArgs* pa, float* fill, cudaStream_t st);
+                         const PrologueArgs& pa, float* fill, cudaStream_t st);
 
 }  // namespace sf21
