@@ -267,7 +267,24 @@ def run_ours(args, w, rank, world):
     pipe_ms = sum(kinds.get(k, (0, 0))[0] for k in ("inv_rows_filter", "inv_cols_b", "inv_cols_a_test"))
     pipe_gbs = 16.0 * units * steps / (pipe_ms / 1e3) / 1e9 if pipe_ms else None
 
-    # plain-form and CPU baseline (rank 0 only)
+    # the plain one-radius-per-launch form on one parameter set (same box)
+    d_plain = torch.empty((N, N, N), dtype=torch.float32, device="cuda")
+    plain_set = 0
+    fb.run_z_plain_device(w["z"], d_delta.data_ptr(), d_src.data_ptr(), d_plain.data_ptr(), s=plain_set, stream=sptr)
+    torch.cuda.synchronize()
+    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    p0.record(stream)
+    fb.run_z_plain_device(w["z"], d_delta.data_ptr(), d_src.data_ptr(), d_plain.data_ptr(), s=plain_set, stream=sptr)
+    p1.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = p0.elapsed_time(p1)
+    plain_units = float(n3) * len(fb.radii(plain_set)[0])
+    plain = {"value": plain_units / (plain_ms / 1e3), "unit": "voxel*radii/s", "ms": plain_ms,
+             "set": plain_set, "radii": len(fb.radii(plain_set)[0]),
+             "batched_per_set_speedup": (value / world) / (plain_units / (plain_ms / 1e3))}
+    del d_plain
+
+    # CPU baseline (rank 0 only)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         ncpu = os.cpu_count() or 1
@@ -297,6 +314,7 @@ def run_ours(args, w, rank, world):
                          "pipeline_frac": (pipe_gbs / hbm) if pipe_gbs else None},
             "kernels_ms_per_step": {k: round(v[0] / steps, 3) for k, v in kinds.items()},
             "clocks": clk.summary(),
+            "plain_gpu": plain,
             "cpu_baseline": cpu,
         }
         print(json.dumps(out))

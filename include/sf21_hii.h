@@ -91,6 +91,16 @@ int sf21_hii_run_z(sf21_hii_ctx *ctx, double z, int src_kind, const float *delta
 int sf21_hii_run_z_device(sf21_hii_ctx *ctx, double z, int src_kind, const float *delta_dev,
                           const float *src_dev, float *xhii_dev, void *stream);
 
+/* The plain form of one set, device buffers: the reference's per-radius
+ * structure on the GPU, one radius per launch sequence -- filtered inverse
+ * transform, centre mask, and for R >= 2 dx the FP32 FFT convolution of the
+ * centres with the discrete sphere thresholded at 1/100 (:358-393), for
+ * R < 2 dx the ball painting (:427-458).  Same outputs as sf21_hii_run_z for
+ * that set (up to the reference's own FP32 convolution rounding).  Used as
+ * the comparison baseline of the batched form. */
+int sf21_hii_run_z_plain_device(sf21_hii_ctx *ctx, double z, int src_kind, const float *delta_dev,
+                                const float *src_dev, int set, float *xhii_dev, void *stream);
+
 /* Radius list of a set exactly as the reference iterates it (:192, 298-461):
  * writes up to cap radii (Mpc/h, descending), returns the count (or <0 on
  * error); *n_fft receives how many take the FFT branch (R >= 2 dx). */

@@ -69,6 +69,10 @@ struct sf21_hii_ctx {
   cudaStream_t stream = nullptr;
   float *d_delta = nullptr, *d_src = nullptr, *d_rec0 = nullptr, *d_fres = nullptr;
   float *d_partials = nullptr, *d_alpha = nullptr, *d_xhii = nullptr;
+  // plain-form buffers (allocated on first use)
+  float* d_mask = nullptr;
+  int* d_flag = nullptr;
+  float2* d_box2 = nullptr;
   float2 *d_spec = nullptr, *d_tw = nullptr;
   std::vector<float2*> d_work;
   uint8_t* d_rc = nullptr;
@@ -158,7 +162,7 @@ static void free_ctx(sf21_hii_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
   void* ptrs[] = {c->d_delta, c->d_src, c->d_rec0, c->d_fres, c->d_partials, c->d_alpha,
-                  c->d_xhii, c->d_spec, c->d_tw, c->d_rc};
+                  c->d_xhii, c->d_spec, c->d_tw, c->d_rc, c->d_mask, c->d_flag, c->d_box2};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (float2* w : c->d_work)
@@ -542,4 +546,58 @@ extern "C" int sf21_hii_profile_read(sf21_hii_ctx* c, double* ms, long* launches
 
 extern "C" const char* sf21_hii_profile_name(int kind) {
   return (kind >= 0 && kind < KD_COUNT) ? kKindNames[kind] : "";
+}
+
+// ---- plain form: one radius per launch sequence, reference structure ----------
+extern "C" int sf21_hii_run_z_plain_device(sf21_hii_ctx* c, double z, int kind, const float* delta_dev,
+                                           const float* src_dev, int set, float* xhii_dev, void* stream) {
+  int rc = check_run_args(c, kind, delta_dev, src_dev, xhii_dev);
+  if (rc) return rc;
+  if (set < 0 || set >= (int)c->sets.size()) CTX_FAIL(c, SF21_E_ARG, "bad set index %d", set);
+  CTX_CUDA(c, cudaSetDevice(c->device));
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+  const int N = (int)c->N;
+  const long n3 = c->n3;
+  if (!c->d_mask) CTX_CUDA(c, cudaMalloc(&c->d_mask, sizeof(float) * n3));
+  if (!c->d_flag) CTX_CUDA(c, cudaMalloc(&c->d_flag, sizeof(int)));
+  if (!c->d_box2) CTX_CUDA(c, cudaMalloc(&c->d_box2, sizeof(float2) * n3));
+  if ((rc = enqueue_front(c, z, kind, delta_dev, src_dev, st))) return rc;
+  const SetInfo& s = c->sets[set];
+  // single-cell fill (:281-288) into the output box
+  CTX_CUDA(c, launch_fill0(n3, dbits(s.fesc), src_dev, c->d_rec0, c->pa, xhii_dev, st));
+  float2* box = c->d_work[0];
+  Batch none;
+  memset(&none, 0, sizeof(none));
+  for (int i = 0; i < (int)s.R.size(); ++i) {
+    Batch bt;
+    memset(&bt, 0, sizeof(bt));
+    bt.K = 1;
+    bt.zmul = (float)s.fesc;
+    bt.r[0].dkR = (float)(c->dk * s.R[i]);
+    bt.r[0].ridx = i;
+    bt.r[0].work = box;
+    // filtered fields (:305-325)
+    CTX_CUDA(c, launch_inv_rows_filter(N, c->d_spec, bt, c->d_tw, st));
+    CTX_CUDA(c, launch_cols(N, box, none, 1, 1, true, c->d_tw, st));
+    CTX_CUDA(c, launch_cols(N, box, none, 1, 0, true, c->d_tw, st));
+    CTX_CUDA(c, cudaMemsetAsync(c->d_flag, 0, sizeof(int), st));
+    CTX_CUDA(c, launch_plain_centres(n3, box, c->d_alpha, (float)s.fesc, c->d_mask, c->d_flag, st));
+    if (i < s.n_fft) {
+      // FFT convolution with the discrete sphere (:358-393)
+      CTX_CUDA(c, launch_plain_pack_sphere(N, s.nmax[i], c->d_mask, c->d_flag, c->d_box2, st));
+      CTX_CUDA(c, launch_fwd_rows(N, c->d_box2, c->d_box2, nullptr, c->d_tw, st));
+      CTX_CUDA(c, launch_cols(N, c->d_box2, none, 1, 1, false, c->d_tw, st));
+      CTX_CUDA(c, launch_cols(N, c->d_box2, none, 1, 0, false, c->d_tw, st));
+      CTX_CUDA(c, launch_plain_product(N, c->d_box2, c->d_flag, box, st));
+      CTX_CUDA(c, launch_inv_rows_plain(N, box, c->d_tw, st));
+      CTX_CUDA(c, launch_cols(N, box, none, 1, 1, true, c->d_tw, st));
+      CTX_CUDA(c, launch_cols(N, box, none, 1, 0, true, c->d_tw, st));
+      CTX_CUDA(c, launch_plain_threshold(n3, box, c->d_flag, xhii_dev, st));
+    } else {
+      // ball painting (:427-458)
+      CTX_CUDA(c, launch_plain_paint(N, (int)(long)(s.R[i] / c->dx), s.nmax[i], c->d_mask, xhii_dev, st));
+    }
+  }
+  CTX_CUDA(c, launch_plain_cap(n3, c->d_fres, xhii_dev, st));
+  return SF21_OK;
 }

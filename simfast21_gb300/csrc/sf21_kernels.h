@@ -53,4 +53,14 @@ cudaError_t launch_dt_a_finish(int N, const int* in, int vmax, uint64_t zeta, co
 cudaError_t launch_fill0(long n3, uint64_t zeta, const float* src, const float* rec0,
                          const PrologueArgs& pa, float* fill, cudaStream_t st);
 
+// Plain form (kernels_plain.cu).
+cudaError_t launch_plain_centres(long n3, const float2* box, const float* alpha, float zmul, float* mask, int* flag,
+                                 cudaStream_t st);
+cudaError_t launch_plain_pack_sphere(int N, int nmax, const float* mask, const int* flag, float2* out,
+                                     cudaStream_t st);
+cudaError_t launch_plain_product(int N, const float2* Z, const int* flag, float2* P, cudaStream_t st);
+cudaError_t launch_plain_threshold(long n3, const float2* conv, const int* flag, float* bubblef, cudaStream_t st);
+cudaError_t launch_plain_paint(int N, int nc, int nmax, const float* mask, float* bubblef, cudaStream_t st);
+cudaError_t launch_plain_cap(long n3, const float* fres, float* bubblef, cudaStream_t st);
+
 }  // namespace sf21

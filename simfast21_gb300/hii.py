@@ -27,7 +27,7 @@ _STATUS = {0: "SF21_OK", 1: "SF21_E_ARG", 2: "SF21_E_ALLOC", 3: "SF21_E_CUDA",
 EXPORTS = [
     "sf21_hii_create", "sf21_hii_destroy", "sf21_hii_last_error", "sf21_hii_run_z",
     "sf21_hii_run_z_device", "sf21_hii_radii", "sf21_hii_prologue", "sf21_hii_filtered",
-    "sf21_hii_first_hit", "sf21_hii_profile", "sf21_hii_profile_read", "sf21_hii_profile_name",
+    "sf21_hii_first_hit", "sf21_hii_run_z_plain_device", "sf21_hii_profile", "sf21_hii_profile_read", "sf21_hii_profile_name",
 ]
 
 
@@ -70,6 +70,7 @@ def load_library(path: str = LIB_PATH):
     L.sf21_hii_filtered.argtypes = [vp, ctypes.c_double, ctypes.c_int, fp, fp, ctypes.c_int,
                                     ctypes.c_int, fp, fp]
     L.sf21_hii_first_hit.argtypes = [vp, ctypes.c_double, ctypes.c_int, fp, fp, ctypes.c_int, fp]
+    L.sf21_hii_run_z_plain_device.argtypes = [vp, ctypes.c_double, ctypes.c_int, vp, vp, ctypes.c_int, vp, vp]
     L.sf21_hii_profile.argtypes = [vp, ctypes.c_int]
     L.sf21_hii_profile_read.argtypes = [vp, dp, ctypes.POINTER(ctypes.c_long), ctypes.c_int]
     L.sf21_hii_profile_name.argtypes = [ctypes.c_int]
@@ -154,6 +155,13 @@ class FilterBank:
         self._check(self._lib.sf21_hii_run_z_device(self._h, z, src_kind, ctypes.c_void_p(delta_ptr),
                                                     ctypes.c_void_p(src_ptr), ctypes.c_void_p(xhii_ptr),
                                                     ctypes.c_void_p(stream or None)))
+
+    def run_z_plain_device(self, z: float, delta_ptr: int, src_ptr: int, xhii_ptr: int, s: int = 0,
+                           src_kind: int = SF21_SRC_SFRD, stream: int = 0):
+        """Plain one-radius-per-launch form of set s (device pointers)."""
+        self._check(self._lib.sf21_hii_run_z_plain_device(self._h, z, src_kind, ctypes.c_void_p(delta_ptr),
+                                                          ctypes.c_void_p(src_ptr), s, ctypes.c_void_p(xhii_ptr),
+                                                          ctypes.c_void_p(stream or None)))
 
     def prologue(self, z: float, delta, src, s: int = 0, src_kind: int = SF21_SRC_SFRD):
         d = _f32(delta, self.n3)

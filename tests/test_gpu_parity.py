@@ -142,3 +142,22 @@ def test_halo_catalogue_branch(hii, oracle_lib):
     b = F.bands(rec0, rion, radii, sp.dx, sp.dk, tol=TOL_BAND)
     certain = b["ionised_lo"] == b["ionised_hi"]
     assert np.array_equal(x[0][certain].view(np.uint32), ref_x[certain].view(np.uint32))
+
+
+def test_plain_form_matches_reference(hii, oracle_lib):
+    """The plain one-radius-per-launch form (reference structure: FP32 FFT
+    convolution with the sphere, painting for R < 2 dx) through the C-ABI."""
+    import torch
+    g, sp = _case("hii_n64_sfr.npz")
+    fb = _bank(hii, sp)
+    z = float(g["zs"][0])
+    d = torch.from_numpy(g["delta_0"]).cuda()
+    s = torch.from_numpy(g["sfrd_0"]).cuda()
+    out = torch.empty_like(d)
+    fb.run_z_plain_device(z, d.data_ptr(), s.data_ptr(), out.data_ptr())
+    torch.cuda.synchronize()
+    x = out.cpu().numpy()
+    _, b, lo, hi = _bounds(oracle_lib, sp, z, g["delta_0"], g["sfrd_0"])
+    certain = b["ionised_lo"] == b["ionised_hi"]
+    assert np.array_equal(x[certain].view(np.uint32), g["xHII_0"][certain].view(np.uint32))
+    assert np.all((x == lo) | (x == hi))
