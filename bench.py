@@ -52,6 +52,9 @@ def workload(name: str):
         rng = np.random.default_rng(seed)
         zetas = np.exp(rng.uniform(np.log(10.0), np.log(100.0), 16))
         rmaxs = rng.uniform(5.0, 30.0, 16)
+    elif name == "single256":
+        N, L, z, seed = 256, 150.0, 7.0, 1236
+        zetas, rmaxs = np.array([30.0]), np.array([30.0])
     elif name == "plain128":
         N, L, z, seed = 128, 100.0, 8.0, 1234
         zetas, rmaxs = np.array([30.0]), np.array([50.0])
@@ -72,6 +75,7 @@ def describe(w):
     return {"batched512": "HII filter bank, batched: 512^3, L=300 Mpc/h, z=7, 64 sets "
                           "(zeta log-U[10,100], Rmax U[10,60] Mpc/h, factor 1.05)",
             "batched256": "HII filter bank, batched: 256^3, L=150 Mpc/h, z=7, 16 sets",
+            "single256": "HII filter bank: 256^3, L=150 Mpc/h, z=7, 1 set (zeta=30, Rmax=30 Mpc/h, factor 1.05)",
             "plain128": "HII filter bank: 128^3, L=100 Mpc/h, z=8, zeta=30, Rmax=50, factor 1.1"}[w["name"]]
 
 
@@ -194,7 +198,7 @@ def run_ours(args, w, rank, world):
     n3 = N ** 3
     nsets = len(w["sets"])
     delta, sfrd = synth.make_boxes(synth.Workload(N=N, L=w["L"], zs=[w["z"]], seed=w["seed"]), w["z"])
-    fb = hii.FilterBank(N, w["L"], w["hubble"], w["sets"], device=dev)
+    fb = hii.FilterBank(N, w["L"], w["hubble"], w["sets"], device=dev, kmax=args.kmax)
     R_total = sum(len(fb.radii(s)[0]) for s in range(nsets))
     units = float(n3) * R_total
     d_delta = torch.from_numpy(delta).cuda()
@@ -328,6 +332,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="batched512")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--kmax", type=int, default=0, help="radii per spectrum read (0 = library default)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
