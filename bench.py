@@ -198,7 +198,8 @@ def run_ours(args, w, rank, world):
     n3 = N ** 3
     nsets = len(w["sets"])
     delta, sfrd = synth.make_boxes(synth.Workload(N=N, L=w["L"], zs=[w["z"]], seed=w["seed"]), w["z"])
-    fb = hii.FilterBank(N, w["L"], w["hubble"], w["sets"], device=dev, kmax=args.kmax)
+    fb = hii.FilterBank(N, w["L"], w["hubble"], w["sets"], device=dev, kmax=args.kmax, path=args.path)
+    path, tune3, tunep = fb.path()
     R_total = sum(len(fb.radii(s)[0]) for s in range(nsets))
     units = float(n3) * R_total
     d_delta = torch.from_numpy(delta).cuda()
@@ -260,15 +261,18 @@ def run_ours(args, w, rank, world):
     dom_ms, dom_n = kinds[dom]
     per_launch_ms = dom_ms / dom_n
     # algorithmic bytes per launch (complex64 boxes: 8 B per voxel)
-    K_avg = R_total / (kinds.get("inv_rows_filter", (0, 1))[1] / steps)
+    nbatch = kinds.get("inv_cols_a_test", (0, 1))[1] / steps
+    K_avg = R_total / nbatch
     alg = {
         "inv_rows_filter": n3 * 8.0 * (1 + K_avg),      # spectrum read once, K boxes written
         "inv_cols_b": n3 * 16.0 * K_avg,                 # K boxes read + written
         "inv_cols_a_test": n3 * (8.0 * K_avg + 2.0),     # K boxes read, first-hit byte r/w
+        "inv_plane_filter": n3 * 8.0 * (1 + K_avg),      # spectrum read once, K boxes written
     }.get(dom, None)
     achieved = alg / (per_launch_ms / 1e3) / 1e9 if alg else None
     # whole radius pipeline against the 16 B per voxel*radius algorithmic traffic
-    pipe_ms = sum(kinds.get(k, (0, 0))[0] for k in ("inv_rows_filter", "inv_cols_b", "inv_cols_a_test"))
+    pipe_ms = sum(kinds.get(k, (0, 0))[0] for k in ("inv_rows_filter", "inv_cols_b", "inv_cols_a_test",
+                                                     "inv_plane_filter"))
     pipe_gbs = 16.0 * units * steps / (pipe_ms / 1e3) / 1e9 if pipe_ms else None
 
     # the plain one-radius-per-launch form on one parameter set (same box)
@@ -307,6 +311,8 @@ def run_ours(args, w, rank, world):
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded lognormal density + SFRD boxes)",
             "config": {"workload": describe(w), "N": N, "sets": nsets, "radii_total": R_total,
+                       "pipeline": {1: "three axis passes", 2: "cluster plane pass + kx pass"}[path],
+                       "tuned_batch_ms": {"three_pass": tune3, "plane": tunep},
                        "flush": "inputs larger than L2 (every box >= 537 MB)"},
             "e2e": {"value": e2e_val, "unit": "voxel*radii/s",
                     "h2d_bytes_per_step": 2 * 4 * n3, "d2h_bytes_per_step": nsets * 4 * n3},
@@ -333,6 +339,8 @@ def main():
     ap.add_argument("--workload", default="batched512")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--kmax", type=int, default=0, help="radii per spectrum read (0 = library default)")
+    ap.add_argument("--path", type=int, default=0,
+                    help="radius pipeline: 0 = tuned, 1 = three axis passes, 2 = cluster plane pass")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -58,6 +58,9 @@ typedef struct {
   int nsets;         /* parameter sets sharing each forward transform (>=1) */
   const sf21_hii_set *sets;
   int kmax;          /* radii per spectrum read (0 = automatic, <= 8)       */
+  int path;          /* radius pipeline: 0 = tuned at create (times one batch
+                        of each and keeps the faster), 1 = three axis passes,
+                        2 = plane passes on thread-block clusters (N 64..512) */
 } sf21_hii_config;
 
 typedef struct sf21_hii_ctx sf21_hii_ctx;
@@ -122,6 +125,10 @@ int sf21_hii_filtered(sf21_hii_ctx *ctx, double z, int src_kind, const float *de
  * the centre test of :339-348 / :437-438. */
 int sf21_hii_first_hit(sf21_hii_ctx *ctx, double z, int src_kind, const float *delta,
                        const float *src, int set, uint8_t *rc);
+
+/* Radius pipeline in use (1 or 2, see sf21_hii_config.path) and, when it was
+ * tuned at create, the measured ms of one batch of each (0 if not tuned). */
+int sf21_hii_path(const sf21_hii_ctx *ctx, double *ms_three_pass, double *ms_plane);
 
 /* Measurement hooks.  sf21_hii_profile(ctx, 1) starts recording CUDA events
  * around every kernel the context launches (on its launch stream) and clears

@@ -13,12 +13,18 @@
 // padded index n + n/16 to keep the strided stage stores at most 2-way
 // bank-conflicted).
 //
-// Twiddles come from a table tw[t] = exp(-2 pi i t / N) computed in double on
-// the host; the inverse transform uses the conjugates.  Transforms are
+// Twiddles come from a table computed in double on the host and rounded once,
+// laid out stage by stage so that the lanes of a warp read consecutive
+// entries (no shared-memory bank conflicts): for the radix-8 stage with
+// stride Ns the entry (r - 1) Ns + (j mod Ns) holds w^((j mod Ns) r N/(8 Ns)),
+// for the radix-4 tail (r - 1) N/4 + j4 holds w^(j4 r), for the radix-2 tail
+// j2 holds w^j2, with w = exp(-2 pi i / N) (twiddle_layout() below gives the
+// offsets); the inverse transform uses the conjugates.  Transforms are
 // unnormalised (forward sign -1, inverse +1), the FFTW convention the
 // reference relies on (get_HIIbubbles.c:110-183).
 #pragma once
 #include <cuda_runtime.h>
+#include <math.h>
 
 namespace sf21 {
 
@@ -84,6 +90,18 @@ __device__ __forceinline__ void dft8(float2 (&v)[8]) {
   v[7] = csub(e3, w3o);
 }
 
+// Offset of the twiddles of radix-8 stage st (st >= 1) in the table.
+__host__ __device__ constexpr int tw_stage_off(int st) {
+  int off = 0, ns = 8;
+  for (int s = 1; s < st; ++s) {
+    off += 7 * ns;
+    ns *= 8;
+  }
+  return off;
+}
+// Offset of the tail twiddles (after the Q radix-8 stages).
+__host__ __device__ constexpr int tw_tail_off(int N) { return tw_stage_off(ilog2c(N) / 3); }
+
 template <bool INV>
 __device__ __forceinline__ float2 twid(const float2* tw, int t) {
   float2 w = tw[t];
@@ -107,9 +125,9 @@ __device__ __forceinline__ void fft_line(float2 (&v)[8], float2* s, const float2
 #pragma unroll
       for (int r = 0; r < 8; ++r) v[r] = s[padx(j + r * N8)];
       const int jm = j & (Ns - 1);
-      const int step = N / (8 * Ns);
+      const float2* tws = tw + tw_stage_off(st);
 #pragma unroll
-      for (int r = 1; r < 8; ++r) v[r] = cmul(v[r], twid<INV>(tw, jm * r * step));
+      for (int r = 1; r < 8; ++r) v[r] = cmul(v[r], twid<INV>(tws, (r - 1) * Ns + jm));
     }
     dft8<INV>(v);
     const bool keep = (st == Q - 1) && (RB == 0);
@@ -128,7 +146,7 @@ __device__ __forceinline__ void fft_line(float2 (&v)[8], float2* s, const float2
     for (int m = 0; m < 4; ++m) {
       const int j2 = j + m * N8;
       float2 a = s[padx(j2)];
-      float2 b = cmul(s[padx(j2 + N / 2)], twid<INV>(tw, j2));
+      float2 b = cmul(s[padx(j2 + N / 2)], twid<INV>(tw + tw_tail_off(N), j2));
       v[m] = cadd(a, b);
       v[m + 4] = csub(a, b);
     }
@@ -137,16 +155,49 @@ __device__ __forceinline__ void fft_line(float2 (&v)[8], float2* s, const float2
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       const int j4 = j + h * N8;
+      const float2* twt = tw + tw_tail_off(N);
       float2 a0 = s[padx(j4)];
-      float2 a1 = cmul(s[padx(j4 + N / 4)], twid<INV>(tw, j4));
-      float2 a2 = cmul(s[padx(j4 + N / 2)], twid<INV>(tw, 2 * j4));
-      float2 a3 = cmul(s[padx(j4 + 3 * N / 4)], twid<INV>(tw, 3 * j4));
+      float2 a1 = cmul(s[padx(j4 + N / 4)], twid<INV>(twt, j4));
+      float2 a2 = cmul(s[padx(j4 + N / 2)], twid<INV>(twt, N / 4 + j4));
+      float2 a3 = cmul(s[padx(j4 + 3 * N / 4)], twid<INV>(twt, N / 2 + j4));
       dft4<INV>(a0, a1, a2, a3);
       // outputs j4 + r N/4 -> register j + (2r + h) N/8
       v[0 + h] = a0;
       v[2 + h] = a1;
       v[4 + h] = a2;
       v[6 + h] = a3;
+    }
+  }
+}
+
+// Host: the twiddle table of an N-point line in the layout above (N entries,
+// the unused tail is zero).  out[t] = (cos, sin) of the angle, in double.
+inline void twiddle_layout(int N, double* re, double* im) {
+  const double two_pi = 6.283185307179586476925286766559;
+  for (int t = 0; t < N; ++t) re[t] = im[t] = 0.0;
+  const int LOG = ilog2c(N), Q = LOG / 3, RB = LOG % 3;
+  int Ns = 8;
+  for (int st = 1; st < Q; ++st) {
+    const int off = tw_stage_off(st);
+    for (int r = 1; r < 8; ++r)
+      for (int jm = 0; jm < Ns; ++jm) {
+        const long e = (long)jm * r * (N / (8 * Ns));
+        re[off + (r - 1) * Ns + jm] = cos(-two_pi * (double)e / N);
+        im[off + (r - 1) * Ns + jm] = sin(-two_pi * (double)e / N);
+      }
+    Ns *= 8;
+  }
+  const int off = tw_tail_off(N);
+  if (RB == 2) {
+    for (int r = 1; r < 4; ++r)
+      for (int j4 = 0; j4 < N / 4; ++j4) {
+        re[off + (r - 1) * (N / 4) + j4] = cos(-two_pi * (double)(j4 * r) / N);
+        im[off + (r - 1) * (N / 4) + j4] = sin(-two_pi * (double)(j4 * r) / N);
+      }
+  } else if (RB == 1) {
+    for (int j2 = 0; j2 < N / 2; ++j2) {
+      re[off + j2] = cos(-two_pi * (double)j2 / N);
+      im[off + j2] = sin(-two_pi * (double)j2 / N);
     }
   }
 }

@@ -65,6 +65,8 @@ struct sf21_hii_ctx {
   long N = 0, N_halo = 0, n3 = 0;
   double L = 0, hubble = 0, dx = 0, dk = 0;
   int K = 8;
+  int path = 1;             // 1 = three axis passes, 2 = plane clusters + kx pass
+  double tune_ms[3] = {0, 0, 0};
   std::vector<SetInfo> sets;
   cudaStream_t stream = nullptr;
   float *d_delta = nullptr, *d_src = nullptr, *d_rec0 = nullptr, *d_fres = nullptr;
@@ -92,8 +94,9 @@ struct sf21_hii_ctx {
 // Kernel kinds reported by sf21_hii_profile_read, in this order.
 static const char* kKindNames[] = {"prologue", "alpha", "fwd_rows", "fwd_cols_b", "fwd_cols_a",
                                    "inv_rows_filter", "inv_cols_b", "inv_cols_a_test", "dt_rows",
-                                   "dt_b", "dt_a_finish"};
-enum { KD_PRO, KD_ALPHA, KD_FROWS, KD_FCB, KD_FCA, KD_IROWS, KD_ICB, KD_ICA, KD_DTR, KD_DTB, KD_DTA, KD_COUNT };
+                                   "dt_b", "dt_a_finish", "inv_plane_filter"};
+enum { KD_PRO, KD_ALPHA, KD_FROWS, KD_FCB, KD_FCA, KD_IROWS, KD_ICB, KD_ICA, KD_DTR, KD_DTB, KD_DTA, KD_PLANE,
+       KD_COUNT };
 
 // Records an event on st when timing is on; returns its index (or -1).
 static int mark(sf21_hii_ctx* c, cudaStream_t st) {
@@ -200,6 +203,8 @@ static int prologue_args(sf21_hii_ctx* c, double z, int kind, PrologueArgs* pa) 
   return SF21_OK;
 }
 
+static int enqueue_batch(sf21_hii_ctx* c, const Batch& bt, cudaStream_t st);
+
 extern "C" int sf21_hii_create(const sf21_hii_config* cfg, sf21_hii_ctx** out) {
   if (!out) return SF21_E_ARG;
   *out = nullptr;
@@ -275,15 +280,67 @@ extern "C" int sf21_hii_create(const sf21_hii_config* cfg, sf21_hii_ctx** out) {
   CREATE_CUDA(cudaMalloc(&c->d_alpha, sizeof(float)));
   // twiddles exp(-2 pi i t / N) in double, rounded once
   std::vector<float2> tw(N);
-  for (long t = 0; t < N; ++t) {
-    const double a = -2.0 * kPI * (double)t / (double)N;
-    tw[t] = make_float2((float)cos(a), (float)sin(a));
+  {
+    std::vector<double> tre(N), tim(N);
+    twiddle_layout((int)N, tre.data(), tim.data());
+    for (long t = 0; t < N; ++t) tw[t] = make_float2((float)tre[t], (float)tim[t]);
   }
   CREATE_CUDA(cudaMalloc(&c->d_tw, sizeof(float2) * N));
   CREATE_CUDA(cudaMemcpy(c->d_tw, tw.data(), sizeof(float2) * N, cudaMemcpyHostToDevice));
   for (SetInfo& s : c->sets) {
     CREATE_CUDA(cudaMalloc(&s.d_nmax, sizeof(int) * s.nmax.size()));
     CREATE_CUDA(cudaMemcpy(s.d_nmax, s.nmax.data(), sizeof(int) * s.nmax.size(), cudaMemcpyHostToDevice));
+  }
+  // path: explicit, or tuned by timing one K-radius batch of each variant
+  c->path = 1;
+  if (plane_supported((int)N)) {
+    CREATE_CUDA(plane_setup((int)N));
+    const int want = cfg->path;
+    const bool can = plane_max_active_clusters((int)N) > 0;
+    if (want == 2 && !can) {
+      g_create_err = "plane path requested but its clusters cannot be scheduled on this device";
+      free_ctx(c);
+      return SF21_E_UNSUPPORTED;
+    }
+    if (want == 2) c->path = 2;
+    if (want == 0 && can) {
+      CREATE_CUDA(cudaMemsetAsync(c->d_spec, 0, box_c, c->stream));
+      CREATE_CUDA(cudaMemsetAsync(c->d_alpha, 0, sizeof(float), c->stream));
+      Batch bt;
+      memset(&bt, 0, sizeof(bt));
+      bt.K = K;
+      bt.zmul = 1.0f;
+      for (int k = 0; k < K; ++k) {
+        bt.r[k].dkR = (float)(c->dk * c->dx * (2.0 + k));
+        bt.r[k].ridx = k;
+        bt.r[k].work = c->d_work[k];
+      }
+      cudaEvent_t t0, t1;
+      CREATE_CUDA(cudaEventCreate(&t0));
+      CREATE_CUDA(cudaEventCreate(&t1));
+      double best[3] = {0, 1e30, 1e30};
+      for (int p = 1; p <= 2; ++p) {
+        c->path = p;
+        for (int rep = 0; rep < 4; ++rep) {
+          CREATE_CUDA(cudaEventRecord(t0, c->stream));
+          if (enqueue_batch(c, bt, c->stream) != SF21_OK) {
+            g_create_err = c->err;
+            free_ctx(c);
+            return SF21_E_CUDA;
+          }
+          CREATE_CUDA(cudaEventRecord(t1, c->stream));
+          CREATE_CUDA(cudaEventSynchronize(t1));
+          float ms = 0.f;
+          CREATE_CUDA(cudaEventElapsedTime(&ms, t0, t1));
+          if (rep > 0 && ms < best[p]) best[p] = ms;  // first run warms up
+        }
+      }
+      cudaEventDestroy(t0);
+      cudaEventDestroy(t1);
+      c->tune_ms[1] = best[1];
+      c->tune_ms[2] = best[2];
+      c->path = best[2] < best[1] ? 2 : 1;
+    }
   }
 #undef CREATE_CUDA
   *out = c;
@@ -336,9 +393,35 @@ static int enqueue_front(sf21_hii_ctx* c, double z, int kind, const float* delta
   return SF21_OK;
 }
 
+// The radius pipeline of one batch: filter + inverse transform + centre test.
+static int enqueue_batch(sf21_hii_ctx* c, const Batch& bt, cudaStream_t st) {
+  const int N = (int)c->N;
+  if (c->path == 2) {
+    int e0 = mark(c, st);
+    CTX_CUDA(c, launch_plane_filter(N, c->d_spec, bt, c->d_tw, st));
+    int e1 = mark(c, st);
+    CTX_CUDA(c, launch_cols_a_test(N, bt, c->d_rc, c->d_alpha, c->d_tw, st));
+    int e2 = mark(c, st);
+    span(c, KD_PLANE, e0, e1);
+    span(c, KD_ICA, e1, e2);
+    return SF21_OK;
+  }
+  int e0 = mark(c, st);
+  CTX_CUDA(c, launch_inv_rows_filter(N, c->d_spec, bt, c->d_tw, st));
+  int e1 = mark(c, st);
+  CTX_CUDA(c, launch_cols(N, nullptr, bt, bt.K, 1, true, c->d_tw, st));
+  int e2 = mark(c, st);
+  CTX_CUDA(c, launch_cols_a_test(N, bt, c->d_rc, c->d_alpha, c->d_tw, st));
+  int e3 = mark(c, st);
+  span(c, KD_IROWS, e0, e1);
+  span(c, KD_ICB, e1, e2);
+  span(c, KD_ICA, e2, e3);
+  return SF21_OK;
+}
+
 static int enqueue_radii(sf21_hii_ctx* c, int set, cudaStream_t st) {
   const SetInfo& s = c->sets[set];
-  const int N = (int)c->N;
+  int rc;
   CTX_CUDA(c, cudaMemsetAsync(c->d_rc, RC_NONE, c->n3, st));
   const int nr = (int)s.R.size();
   for (int k0 = 0; k0 < nr; k0 += c->K) {
@@ -352,16 +435,7 @@ static int enqueue_radii(sf21_hii_ctx* c, int set, cudaStream_t st) {
       bt.r[k].ridx = k0 + k;
       bt.r[k].work = c->d_work[k];
     }
-    int e0 = mark(c, st);
-    CTX_CUDA(c, launch_inv_rows_filter(N, c->d_spec, bt, c->d_tw, st));
-    int e1 = mark(c, st);
-    CTX_CUDA(c, launch_cols(N, nullptr, bt, bt.K, 1, true, c->d_tw, st));
-    int e2 = mark(c, st);
-    CTX_CUDA(c, launch_cols_a_test(N, bt, c->d_rc, c->d_alpha, c->d_tw, st));
-    int e3 = mark(c, st);
-    span(c, KD_IROWS, e0, e1);
-    span(c, KD_ICB, e1, e2);
-    span(c, KD_ICA, e2, e3);
+    if ((rc = enqueue_batch(c, bt, st))) return rc;
   }
   return SF21_OK;
 }
@@ -600,4 +674,11 @@ extern "C" int sf21_hii_run_z_plain_device(sf21_hii_ctx* c, double z, int kind, 
   }
   CTX_CUDA(c, launch_plain_cap(n3, c->d_fres, xhii_dev, st));
   return SF21_OK;
+}
+
+extern "C" int sf21_hii_path(const sf21_hii_ctx* c, double* ms_three_pass, double* ms_plane) {
+  if (!c) return -SF21_E_ARG;
+  if (ms_three_pass) *ms_three_pass = c->tune_ms[1];
+  if (ms_plane) *ms_plane = c->tune_ms[2];
+  return c->path;
 }

@@ -53,6 +53,13 @@ cudaError_t launch_dt_a_finish(int N, const int* in, int vmax, uint64_t zeta, co
 cudaError_t launch_fill0(long n3, uint64_t zeta, const float* src, const float* rec0,
                          const PrologueArgs& pa, float* fill, cudaStream_t st);
 
+// Plane pass on thread-block clusters (kernels_plane.cu): filter + kz + ky of
+// whole kx planes for the batch's K radii, into the work boxes.
+bool plane_supported(int N);
+cudaError_t plane_setup(int N);
+int plane_max_active_clusters(int N);
+cudaError_t launch_plane_filter(int N, const float2* spec, const Batch& bt, const float2* tw, cudaStream_t st);
+
 // Plain form (kernels_plain.cu).
 cudaError_t launch_plain_centres(long n3, const float2* box, const float* alpha, float zmul, float* mask, int* flag,
                                  cudaStream_t st);

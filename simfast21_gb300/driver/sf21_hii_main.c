@@ -105,6 +105,7 @@ int main(int argc, char *argv[]) {
   cfg.device = 0;
   cfg.nsets = nsets;
   cfg.sets = sets;
+  cfg.path = 0; /* tuned */
   sf21_hii_ctx *ctx = NULL;
   int rc = sf21_hii_create(&cfg, &ctx);
   if (rc != SF21_OK) {

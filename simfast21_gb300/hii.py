@@ -27,7 +27,7 @@ _STATUS = {0: "SF21_OK", 1: "SF21_E_ARG", 2: "SF21_E_ALLOC", 3: "SF21_E_CUDA",
 EXPORTS = [
     "sf21_hii_create", "sf21_hii_destroy", "sf21_hii_last_error", "sf21_hii_run_z",
     "sf21_hii_run_z_device", "sf21_hii_radii", "sf21_hii_prologue", "sf21_hii_filtered",
-    "sf21_hii_first_hit", "sf21_hii_run_z_plain_device", "sf21_hii_profile", "sf21_hii_profile_read", "sf21_hii_profile_name",
+    "sf21_hii_first_hit", "sf21_hii_run_z_plain_device", "sf21_hii_path", "sf21_hii_profile", "sf21_hii_profile_read", "sf21_hii_profile_name",
 ]
 
 
@@ -44,7 +44,7 @@ class _Set(ctypes.Structure):
 class _Config(ctypes.Structure):
     _fields_ = [("N", ctypes.c_long), ("N_halo", ctypes.c_long), ("L", ctypes.c_double),
                 ("hubble", ctypes.c_double), ("device", ctypes.c_int), ("nsets", ctypes.c_int),
-                ("sets", ctypes.POINTER(_Set)), ("kmax", ctypes.c_int)]
+                ("sets", ctypes.POINTER(_Set)), ("kmax", ctypes.c_int), ("path", ctypes.c_int)]
 
 
 _lib = None
@@ -71,6 +71,7 @@ def load_library(path: str = LIB_PATH):
                                     ctypes.c_int, fp, fp]
     L.sf21_hii_first_hit.argtypes = [vp, ctypes.c_double, ctypes.c_int, fp, fp, ctypes.c_int, fp]
     L.sf21_hii_run_z_plain_device.argtypes = [vp, ctypes.c_double, ctypes.c_int, vp, vp, ctypes.c_int, vp, vp]
+    L.sf21_hii_path.argtypes = [vp, dp, dp]
     L.sf21_hii_profile.argtypes = [vp, ctypes.c_int]
     L.sf21_hii_profile_read.argtypes = [vp, dp, ctypes.POINTER(ctypes.c_long), ctypes.c_int]
     L.sf21_hii_profile_name.argtypes = [ctypes.c_int]
@@ -101,7 +102,7 @@ class FilterBank:
     """One GPU context for a box size and a list of parameter sets."""
 
     def __init__(self, N: int, L: float, hubble: float, sets, N_halo: int = 0, device: int = 0,
-                 kmax: int = 0):
+                 kmax: int = 0, path: int = 0):
         self._lib = load_library()
         self.N = int(N)
         self.n3 = self.N ** 3
@@ -109,7 +110,7 @@ class FilterBank:
         arr = (_Set * len(self.sets))(*[_Set(s.fesc, s.Rmax, s.Nbins) for s in self.sets])
         self._arr = arr
         cfg = _Config(N=self.N, N_halo=N_halo or self.N, L=L, hubble=hubble, device=device,
-                      nsets=len(self.sets), sets=arr, kmax=kmax)
+                      nsets=len(self.sets), sets=arr, kmax=kmax, path=path)
         h = ctypes.c_void_p()
         rc = self._lib.sf21_hii_create(ctypes.byref(cfg), ctypes.byref(h))
         if rc != 0:
@@ -130,6 +131,13 @@ class FilterBank:
     def _check(self, rc):
         if rc != 0:
             raise HIIError(rc, self._lib.sf21_hii_last_error(self._h).decode())
+
+    def path(self):
+        """(pipeline in use: 1 = three axis passes, 2 = plane clusters,
+        tuned ms of one batch for each or 0)."""
+        a, b = ctypes.c_double(0), ctypes.c_double(0)
+        p = self._lib.sf21_hii_path(self._h, ctypes.byref(a), ctypes.byref(b))
+        return p, a.value, b.value
 
     def radii(self, s: int = 0):
         buf = (ctypes.c_double * 512)()

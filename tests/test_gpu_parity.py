@@ -161,3 +161,20 @@ def test_plain_form_matches_reference(hii, oracle_lib):
     certain = b["ionised_lo"] == b["ionised_hi"]
     assert np.array_equal(x[certain].view(np.uint32), g["xHII_0"][certain].view(np.uint32))
     assert np.all((x == lo) | (x == hi))
+
+
+@pytest.mark.parametrize("N,L", [(64, 50.0), (128, 100.0)])
+def test_plane_and_three_pass_paths_agree(hii, N, L):
+    """The cluster plane pass (filter + kz + ky in distributed shared memory)
+    and the three axis passes run the same arithmetic: identical outputs."""
+    w = synth.Workload(N=N, L=L, zs=[8.0], zeta=40.0, Rmax=L / 2, factor=1.1, seed=21)
+    delta, sfrd = synth.make_boxes(w, 8.0)
+    sets = [(40.0, L / 2, w.Nbins), (15.0, L / 5, 20)]
+    a = hii.FilterBank(N, L, 0.71, sets, path=1)
+    b = hii.FilterBank(N, L, 0.71, sets, path=2)
+    assert a.path()[0] == 1 and b.path()[0] == 2
+    xa, na = a.run_z(8.0, delta, sfrd)
+    xb, nb = b.run_z(8.0, delta, sfrd)
+    assert np.array_equal(xa.view(np.uint32), xb.view(np.uint32))
+    for s in range(len(sets)):
+        assert np.array_equal(a.first_hit(8.0, delta, sfrd, s), b.first_hit(8.0, delta, sfrd, s))
