@@ -199,7 +199,7 @@ def run_ours(args, w, rank, world):
     nsets = len(w["sets"])
     delta, sfrd = synth.make_boxes(synth.Workload(N=N, L=w["L"], zs=[w["z"]], seed=w["seed"]), w["z"])
     fb = hii.FilterBank(N, w["L"], w["hubble"], w["sets"], device=dev, kmax=args.kmax, path=args.path)
-    path, tune3, tunep = fb.path()
+    path, tuned = fb.path()
     R_total = sum(len(fb.radii(s)[0]) for s in range(nsets))
     units = float(n3) * R_total
     d_delta = torch.from_numpy(delta).cuda()
@@ -311,8 +311,9 @@ def run_ours(args, w, rank, world):
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded lognormal density + SFRD boxes)",
             "config": {"workload": describe(w), "N": N, "sets": nsets, "radii_total": R_total,
-                       "pipeline": {1: "three axis passes", 2: "cluster plane pass + kx pass"}[path],
-                       "tuned_batch_ms": {"three_pass": tune3, "plane": tunep},
+                       "pipeline": {1: "three axis passes", 2: "cluster plane pass + kx pass",
+                                    3: "three axis passes, TMA-pipelined persistent strided passes"}[path],
+                       "tuned_batch_ms": {"three_pass": tuned[1], "plane": tuned[2], "tma_pipelined": tuned[3]},
                        "flush": "inputs larger than L2 (every box >= 537 MB)"},
             "e2e": {"value": e2e_val, "unit": "voxel*radii/s",
                     "h2d_bytes_per_step": 2 * 4 * n3, "d2h_bytes_per_step": nsets * 4 * n3},

@@ -59,8 +59,11 @@ typedef struct {
   const sf21_hii_set *sets;
   int kmax;          /* radii per spectrum read (0 = automatic, <= 8)       */
   int path;          /* radius pipeline: 0 = tuned at create (times one batch
-                        of each and keeps the faster), 1 = three axis passes,
-                        2 = plane passes on thread-block clusters (N 64..512) */
+                        of each available one and keeps the fastest),
+                        1 = three axis passes, 2 = plane passes on
+                        thread-block clusters (N 64..512), 3 = three axis
+                        passes with TMA-pipelined persistent strided passes
+                        (N 64..1024) */
 } sf21_hii_config;
 
 typedef struct sf21_hii_ctx sf21_hii_ctx;
@@ -126,9 +129,37 @@ int sf21_hii_filtered(sf21_hii_ctx *ctx, double z, int src_kind, const float *de
 int sf21_hii_first_hit(sf21_hii_ctx *ctx, double z, int src_kind, const float *delta,
                        const float *src, int set, uint8_t *rc);
 
-/* Radius pipeline in use (1 or 2, see sf21_hii_config.path) and, when it was
- * tuned at create, the measured ms of one batch of each (0 if not tuned). */
-int sf21_hii_path(const sf21_hii_ctx *ctx, double *ms_three_pass, double *ms_plane);
+/* Continuous ionisation criterion of set `set`: C(x) = max over the set's
+ * radii R with rec_R(x) > 0 of ion_R(x) / rec_R(x), the ratio the reference
+ * thresholds at 1 (get_HIIbubbles.c:339-348, 437-438), and the radius index
+ * of the maximum (argmax, 0xFF where no radius has rec_R > 0; C = 0 there).
+ * No reference counterpart: the reference only tests ratio >= 1.  The
+ * argmax stays in the context as the checkpoint of the next vjp call. */
+int sf21_hii_criterion(sf21_hii_ctx *ctx, double z, int src_kind, const float *delta,
+                       const float *src, int set, float *C, uint8_t *argmax);
+int sf21_hii_criterion_device(sf21_hii_ctx *ctx, double z, int src_kind, const float *delta_dev,
+                              const float *src_dev, int set, float *C_dev, uint8_t *argmax_dev,
+                              void *stream);
+
+/* Vector-Jacobian product of the criterion: given dC = dL/dC (N^3 floats),
+ * dL/d delta, dL/d src (N^3 each, NULL to skip) and dL/d fesc (one double,
+ * NULL to skip), for the same z, inputs and set as the preceding criterion
+ * call on ctx (its argmax index is the only checkpoint; the filtered fields
+ * are recomputed).  Away from argmax ties. No reference counterpart. */
+int sf21_hii_vjp(sf21_hii_ctx *ctx, double z, int src_kind, const float *delta, const float *src,
+                 int set, const float *dC, float *ddelta, float *dsrc, double *dfesc);
+int sf21_hii_vjp_device(sf21_hii_ctx *ctx, double z, int src_kind, const float *delta_dev,
+                        const float *src_dev, int set, const float *dC_dev, float *ddelta_dev,
+                        float *dsrc_dev, double *dfesc, void *stream);
+
+/* Radius pipeline in use (1..3, see sf21_hii_config.path); ms_tuned[p-1]
+ * receives the measured ms of one batch of pipeline p when it was tuned at
+ * create (0 if not timed), for p <= cap. */
+int sf21_hii_path(const sf21_hii_ctx *ctx, double *ms_tuned, int cap);
+
+/* Synchronises the context's stream and reports SF21_E_TIMEOUT if a bounded
+ * device wait (TMA copy completion) expired since the last check. */
+int sf21_hii_check(sf21_hii_ctx *ctx);
 
 /* Measurement hooks.  sf21_hii_profile(ctx, 1) starts recording CUDA events
  * around every kernel the context launches (on its launch stream) and clears

@@ -65,12 +65,25 @@ struct sf21_hii_ctx {
   long N = 0, N_halo = 0, n3 = 0;
   double L = 0, hubble = 0, dx = 0, dk = 0;
   int K = 8;
-  int path = 1;             // 1 = three axis passes, 2 = plane clusters + kx pass
-  double tune_ms[3] = {0, 0, 0};
+  int path = 1;             // 1 = three axis passes, 2 = plane clusters + kx pass,
+                            // 3 = three axis passes, strided ones TMA-pipelined
+  double tune_ms[4] = {0, 0, 0, 0};
+  float2* d_work_base = nullptr;  // K consecutive work boxes
+  PipeMaps pmaps;
+  int* d_err = nullptr;
+  int nsm = 0;
   std::vector<SetInfo> sets;
   cudaStream_t stream = nullptr;
   float *d_delta = nullptr, *d_src = nullptr, *d_rec0 = nullptr, *d_fres = nullptr;
   float *d_partials = nullptr, *d_alpha = nullptr, *d_xhii = nullptr;
+  // criterion / adjoint buffers (allocated on first use)
+  float* d_C = nullptr;
+  uint8_t* d_A = nullptr;
+  float2* d_acc = nullptr;
+  float* d_zpart = nullptr;
+  float *d_g = nullptr, *d_gd = nullptr, *d_gs = nullptr;
+  int crit_set = -1;
+  double crit_z = 0;
   // plain-form buffers (allocated on first use)
   float* d_mask = nullptr;
   int* d_flag = nullptr;
@@ -87,16 +100,17 @@ struct sf21_hii_ctx {
   size_t ev_used = 0;
   struct Span { int kind, a, b; };
   std::vector<Span> spans;
-  double prof_ms[16] = {0};
-  long prof_n[16] = {0};
+  double prof_ms[32] = {0};
+  long prof_n[32] = {0};
 };
 
 // Kernel kinds reported by sf21_hii_profile_read, in this order.
 static const char* kKindNames[] = {"prologue", "alpha", "fwd_rows", "fwd_cols_b", "fwd_cols_a",
                                    "inv_rows_filter", "inv_cols_b", "inv_cols_a_test", "dt_rows",
-                                   "dt_b", "dt_a_finish", "inv_plane_filter"};
+                                   "dt_b", "dt_a_finish", "inv_plane_filter", "crit_cols_a",
+                                   "adj_cols_a", "adj_cols_b_fwd", "adj_rows_acc", "adj_final"};
 enum { KD_PRO, KD_ALPHA, KD_FROWS, KD_FCB, KD_FCA, KD_IROWS, KD_ICB, KD_ICA, KD_DTR, KD_DTB, KD_DTA, KD_PLANE,
-       KD_COUNT };
+       KD_CRIT, KD_ADJA, KD_ADJB, KD_ADJR, KD_ADJF, KD_COUNT };
 
 // Records an event on st when timing is on; returns its index (or -1).
 static int mark(sf21_hii_ctx* c, cudaStream_t st) {
@@ -165,11 +179,12 @@ static void free_ctx(sf21_hii_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
   void* ptrs[] = {c->d_delta, c->d_src, c->d_rec0, c->d_fres, c->d_partials, c->d_alpha,
-                  c->d_xhii, c->d_spec, c->d_tw, c->d_rc, c->d_mask, c->d_flag, c->d_box2};
+                  c->d_xhii, c->d_spec, c->d_tw, c->d_rc, c->d_mask, c->d_flag, c->d_box2,
+                  c->d_C, c->d_A, c->d_acc, c->d_zpart, c->d_g, c->d_gd, c->d_gs};
   for (void* p : ptrs)
     if (p) cudaFree(p);
-  for (float2* w : c->d_work)
-    if (w) cudaFree(w);
+  if (c->d_work_base) cudaFree(c->d_work_base);
+  if (c->d_err) cudaFree(c->d_err);
   for (SetInfo& s : c->sets)
     if (s.d_nmax) cudaFree(s.d_nmax);
   for (cudaEvent_t e : c->ev) cudaEventDestroy(e);
@@ -204,6 +219,7 @@ static int prologue_args(sf21_hii_ctx* c, double z, int kind, PrologueArgs* pa) 
 }
 
 static int enqueue_batch(sf21_hii_ctx* c, const Batch& bt, cudaStream_t st);
+static int check_device_flag(sf21_hii_ctx* c);
 
 extern "C" int sf21_hii_create(const sf21_hii_config* cfg, sf21_hii_ctx** out) {
   if (!out) return SF21_E_ARG;
@@ -266,6 +282,7 @@ extern "C" int sf21_hii_create(const sf21_hii_config* cfg, sf21_hii_ctx** out) {
   CREATE_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
   CREATE_CUDA(fft_setup((int)N));
   CREATE_CUDA(dilate_setup((int)N));
+  CREATE_CUDA(adj_setup((int)N));
   CREATE_CUDA(cudaMalloc(&c->d_delta, box_f));
   CREATE_CUDA(cudaMalloc(&c->d_src, box_f));
   CREATE_CUDA(cudaMalloc(&c->d_rec0, box_f));
@@ -274,7 +291,11 @@ extern "C" int sf21_hii_create(const sf21_hii_config* cfg, sf21_hii_ctx** out) {
   CREATE_CUDA(cudaMalloc(&c->d_spec, box_c));
   CREATE_CUDA(cudaMalloc(&c->d_rc, c->n3));
   c->d_work.assign(K, nullptr);
-  for (int k = 0; k < K; ++k) CREATE_CUDA(cudaMalloc(&c->d_work[k], box_c));
+  CREATE_CUDA(cudaMalloc(&c->d_work_base, box_c * K));
+  for (int k = 0; k < K; ++k) c->d_work[k] = c->d_work_base + (size_t)k * c->n3;
+  CREATE_CUDA(cudaMalloc(&c->d_err, sizeof(int)));
+  CREATE_CUDA(cudaMemset(c->d_err, 0, sizeof(int)));
+  CREATE_CUDA(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, c->device));
   c->pro_blocks = prologue_blocks(c->n3);
   CREATE_CUDA(cudaMalloc(&c->d_partials, sizeof(float) * 2 * c->pro_blocks));
   CREATE_CUDA(cudaMalloc(&c->d_alpha, sizeof(float)));
@@ -292,55 +313,66 @@ extern "C" int sf21_hii_create(const sf21_hii_config* cfg, sf21_hii_ctx** out) {
     CREATE_CUDA(cudaMemcpy(s.d_nmax, s.nmax.data(), sizeof(int) * s.nmax.size(), cudaMemcpyHostToDevice));
   }
   // path: explicit, or tuned by timing one K-radius batch of each variant
-  c->path = 1;
-  if (plane_supported((int)N)) {
-    CREATE_CUDA(plane_setup((int)N));
-    const int want = cfg->path;
-    const bool can = plane_max_active_clusters((int)N) > 0;
-    if (want == 2 && !can) {
-      g_create_err = "plane path requested but its clusters cannot be scheduled on this device";
-      free_ctx(c);
-      return SF21_E_UNSUPPORTED;
+  const bool can_plane = plane_supported((int)N) && plane_setup((int)N) == cudaSuccess &&
+                         plane_max_active_clusters((int)N) > 0;
+  bool can_pipe = false;
+  if (pipe_supported((int)N) && pipe_setup((int)N) == cudaSuccess &&
+      pipe_make_maps((int)N, &c->pmaps, K, c->d_work_base) == cudaSuccess)
+    can_pipe = true;
+  cudaGetLastError();
+  const int want = cfg->path;
+  if ((want == 2 && !can_plane) || (want == 3 && !can_pipe) || want < 0 || want > 3) {
+    g_create_err = "requested radius pipeline not available for this box on this device";
+    free_ctx(c);
+    return SF21_E_UNSUPPORTED;
+  }
+  c->path = want ? want : 1;
+  if (want == 0 && (can_plane || can_pipe)) {
+    CREATE_CUDA(cudaMemsetAsync(c->d_spec, 0, box_c, c->stream));
+    CREATE_CUDA(cudaMemsetAsync(c->d_alpha, 0, sizeof(float), c->stream));
+    Batch bt;
+    memset(&bt, 0, sizeof(bt));
+    bt.K = K;
+    bt.zmul = 1.0f;
+    for (int k = 0; k < K; ++k) {
+      bt.r[k].dkR = (float)(c->dk * c->dx * (2.0 + k));
+      bt.r[k].ridx = k;
+      bt.r[k].work = c->d_work[k];
     }
-    if (want == 2) c->path = 2;
-    if (want == 0 && can) {
-      CREATE_CUDA(cudaMemsetAsync(c->d_spec, 0, box_c, c->stream));
-      CREATE_CUDA(cudaMemsetAsync(c->d_alpha, 0, sizeof(float), c->stream));
-      Batch bt;
-      memset(&bt, 0, sizeof(bt));
-      bt.K = K;
-      bt.zmul = 1.0f;
-      for (int k = 0; k < K; ++k) {
-        bt.r[k].dkR = (float)(c->dk * c->dx * (2.0 + k));
-        bt.r[k].ridx = k;
-        bt.r[k].work = c->d_work[k];
-      }
-      cudaEvent_t t0, t1;
-      CREATE_CUDA(cudaEventCreate(&t0));
-      CREATE_CUDA(cudaEventCreate(&t1));
-      double best[3] = {0, 1e30, 1e30};
-      for (int p = 1; p <= 2; ++p) {
-        c->path = p;
-        for (int rep = 0; rep < 4; ++rep) {
-          CREATE_CUDA(cudaEventRecord(t0, c->stream));
-          if (enqueue_batch(c, bt, c->stream) != SF21_OK) {
-            g_create_err = c->err;
-            free_ctx(c);
-            return SF21_E_CUDA;
-          }
-          CREATE_CUDA(cudaEventRecord(t1, c->stream));
-          CREATE_CUDA(cudaEventSynchronize(t1));
-          float ms = 0.f;
-          CREATE_CUDA(cudaEventElapsedTime(&ms, t0, t1));
-          if (rep > 0 && ms < best[p]) best[p] = ms;  // first run warms up
+    cudaEvent_t t0, t1;
+    CREATE_CUDA(cudaEventCreate(&t0));
+    CREATE_CUDA(cudaEventCreate(&t1));
+    double best[4] = {1e30, 1e30, 1e30, 1e30};
+    for (int p = 1; p <= 3; ++p) {
+      if ((p == 2 && !can_plane) || (p == 3 && !can_pipe)) continue;
+      c->path = p;
+      for (int rep = 0; rep < 4; ++rep) {
+        CREATE_CUDA(cudaEventRecord(t0, c->stream));
+        if (enqueue_batch(c, bt, c->stream) != SF21_OK) {
+          g_create_err = c->err;
+          free_ctx(c);
+          return SF21_E_CUDA;
         }
+        CREATE_CUDA(cudaEventRecord(t1, c->stream));
+        CREATE_CUDA(cudaEventSynchronize(t1));
+        float ms = 0.f;
+        CREATE_CUDA(cudaEventElapsedTime(&ms, t0, t1));
+        if (rep > 0 && ms < best[p]) best[p] = ms;  // the first run warms up
       }
-      cudaEventDestroy(t0);
-      cudaEventDestroy(t1);
-      c->tune_ms[1] = best[1];
-      c->tune_ms[2] = best[2];
-      c->path = best[2] < best[1] ? 2 : 1;
+      c->tune_ms[p] = best[p];
     }
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    int err_flag = 0;
+    CREATE_CUDA(cudaMemcpy(&err_flag, c->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err_flag) {
+      g_create_err = "a bounded device wait expired while tuning";
+      free_ctx(c);
+      return SF21_E_TIMEOUT;
+    }
+    c->path = 1;
+    for (int p = 2; p <= 3; ++p)
+      if (best[p] < best[c->path]) c->path = p;
   }
 #undef CREATE_CUDA
   *out = c;
@@ -404,6 +436,19 @@ static int enqueue_batch(sf21_hii_ctx* c, const Batch& bt, cudaStream_t st) {
     int e2 = mark(c, st);
     span(c, KD_PLANE, e0, e1);
     span(c, KD_ICA, e1, e2);
+    return SF21_OK;
+  }
+  if (c->path == 3) {
+    int e0 = mark(c, st);
+    CTX_CUDA(c, launch_inv_rows_filter(N, c->d_spec, bt, c->d_tw, st));
+    int e1 = mark(c, st);
+    CTX_CUDA(c, launch_pipe(N, 0, c->pmaps, bt, c->d_work_base, c->d_rc, c->d_alpha, c->d_tw, c->d_err, c->nsm, st));
+    int e2 = mark(c, st);
+    CTX_CUDA(c, launch_pipe(N, 1, c->pmaps, bt, c->d_work_base, c->d_rc, c->d_alpha, c->d_tw, c->d_err, c->nsm, st));
+    int e3 = mark(c, st);
+    span(c, KD_IROWS, e0, e1);
+    span(c, KD_ICB, e1, e2);
+    span(c, KD_ICA, e2, e3);
     return SF21_OK;
   }
   int e0 = mark(c, st);
@@ -515,6 +560,7 @@ extern "C" int sf21_hii_run_z(sf21_hii_ctx* c, double z, int kind, const float* 
     }
   }
   for (std::thread& t : sums) t.join();
+  if (status == SF21_OK) status = check_device_flag(c);
   return status;
 }
 
@@ -676,9 +722,197 @@ extern "C" int sf21_hii_run_z_plain_device(sf21_hii_ctx* c, double z, int kind, 
   return SF21_OK;
 }
 
-extern "C" int sf21_hii_path(const sf21_hii_ctx* c, double* ms_three_pass, double* ms_plane) {
+extern "C" int sf21_hii_path(const sf21_hii_ctx* c, double* ms_tuned, int cap) {
   if (!c) return -SF21_E_ARG;
-  if (ms_three_pass) *ms_three_pass = c->tune_ms[1];
-  if (ms_plane) *ms_plane = c->tune_ms[2];
+  for (int p = 1; p <= 3 && p <= cap; ++p) ms_tuned[p - 1] = c->tune_ms[p] < 1e29 ? c->tune_ms[p] : 0.0;
   return c->path;
+}
+
+// Status of the bounded device waits: SF21_E_TIMEOUT if one expired since the
+// last check (the flag is cleared), else SF21_OK.
+static int check_device_flag(sf21_hii_ctx* c) {
+  int f = 0;
+  CTX_CUDA(c, cudaMemcpy(&f, c->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (f) {
+    CTX_CUDA(c, cudaMemset(c->d_err, 0, sizeof(int)));
+    CTX_FAIL(c, SF21_E_TIMEOUT, "a bounded device wait expired (TMA copy did not complete)");
+  }
+  return SF21_OK;
+}
+
+extern "C" int sf21_hii_check(sf21_hii_ctx* c) {
+  if (!c) return SF21_E_ARG;
+  CTX_CUDA(c, cudaSetDevice(c->device));
+  CTX_CUDA(c, cudaStreamSynchronize(c->stream));
+  return check_device_flag(c);
+}
+
+// ---- criterion C(x) = max_R ion_R / rec_R and its vector-Jacobian product ----
+static int ensure_adj_buffers(sf21_hii_ctx* c) {
+  const long n3 = c->n3;
+  if (!c->d_C) CTX_CUDA(c, cudaMalloc(&c->d_C, sizeof(float) * n3));
+  if (!c->d_A) CTX_CUDA(c, cudaMalloc(&c->d_A, n3));
+  return SF21_OK;
+}
+
+// recompute the filtered fields of a batch up to (not including) the kx pass
+static int enqueue_recompute(sf21_hii_ctx* c, const Batch& bt, cudaStream_t st) {
+  const int N = (int)c->N;
+  if (c->path == 2) {
+    int e0 = mark(c, st);
+    CTX_CUDA(c, launch_plane_filter(N, c->d_spec, bt, c->d_tw, st));
+    span(c, KD_PLANE, e0, mark(c, st));
+  } else {
+    int e0 = mark(c, st);
+    CTX_CUDA(c, launch_inv_rows_filter(N, c->d_spec, bt, c->d_tw, st));
+    int e1 = mark(c, st);
+    CTX_CUDA(c, launch_cols(N, nullptr, bt, bt.K, 1, true, c->d_tw, st));
+    span(c, KD_IROWS, e0, e1);
+    span(c, KD_ICB, e1, mark(c, st));
+  }
+  return SF21_OK;
+}
+
+static Batch make_batch(const sf21_hii_ctx* c, int set, int k0) {
+  const SetInfo& s = c->sets[set];
+  const int nr = (int)s.R.size();
+  Batch bt;
+  memset(&bt, 0, sizeof(bt));
+  bt.K = nr - k0 < c->K ? nr - k0 : c->K;
+  bt.set = set;
+  bt.zmul = (float)s.fesc;
+  for (int k = 0; k < bt.K; ++k) {
+    bt.r[k].dkR = (float)(c->dk * s.R[k0 + k]);
+    bt.r[k].ridx = k0 + k;
+    bt.r[k].work = c->d_work[k];
+  }
+  return bt;
+}
+
+extern "C" int sf21_hii_criterion_device(sf21_hii_ctx* c, double z, int kind, const float* delta_dev,
+                                         const float* src_dev, int set, float* C_dev, uint8_t* argmax_dev,
+                                         void* stream) {
+  int rc = check_run_args(c, kind, delta_dev, src_dev, C_dev);
+  if (rc) return rc;
+  if (set < 0 || set >= (int)c->sets.size()) CTX_FAIL(c, SF21_E_ARG, "bad set index %d", set);
+  CTX_CUDA(c, cudaSetDevice(c->device));
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+  if ((rc = ensure_adj_buffers(c))) return rc;
+  if ((rc = enqueue_front(c, z, kind, delta_dev, src_dev, st))) return rc;
+  const int N = (int)c->N;
+  CTX_CUDA(c, launch_crit_init(c->n3, c->d_C, c->d_A, st));
+  const int nr = (int)c->sets[set].R.size();
+  for (int k0 = 0; k0 < nr; k0 += c->K) {
+    Batch bt = make_batch(c, set, k0);
+    if ((rc = enqueue_recompute(c, bt, st))) return rc;
+    int e0 = mark(c, st);
+    CTX_CUDA(c, launch_cols_a_crit(N, bt, c->d_C, c->d_A, c->d_alpha, c->d_tw, st));
+    span(c, KD_CRIT, e0, mark(c, st));
+  }
+  CTX_CUDA(c, launch_crit_finalize(c->n3, c->d_C, c->d_A, st));
+  if (C_dev != c->d_C)
+    CTX_CUDA(c, cudaMemcpyAsync(C_dev, c->d_C, sizeof(float) * c->n3, cudaMemcpyDeviceToDevice, st));
+  if (argmax_dev && argmax_dev != c->d_A)
+    CTX_CUDA(c, cudaMemcpyAsync(argmax_dev, c->d_A, c->n3, cudaMemcpyDeviceToDevice, st));
+  c->crit_set = set;
+  c->crit_z = z;
+  return SF21_OK;
+}
+
+extern "C" int sf21_hii_vjp_device(sf21_hii_ctx* c, double z, int kind, const float* delta_dev,
+                                   const float* src_dev, int set, const float* dC_dev, float* ddelta_dev,
+                                   float* dsrc_dev, double* dzeta, void* stream) {
+  int rc = check_run_args(c, kind, delta_dev, src_dev, dC_dev);
+  if (rc) return rc;
+  if (set != c->crit_set || z != c->crit_z || !c->d_A)
+    CTX_FAIL(c, SF21_E_ARG, "vjp needs the argmax checkpoint of a criterion call for the same set and z");
+  CTX_CUDA(c, cudaSetDevice(c->device));
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+  const int N = (int)c->N;
+  const long n3 = c->n3;
+  const int nzp = adj_zpart_blocks(N);
+  if (!c->d_acc) CTX_CUDA(c, cudaMalloc(&c->d_acc, sizeof(float2) * n3));
+  if (!c->d_zpart) CTX_CUDA(c, cudaMalloc(&c->d_zpart, sizeof(float) * nzp));
+  // recompute the spectrum (the checkpoint holds only the argmax index)
+  if ((rc = enqueue_front(c, z, kind, delta_dev, src_dev, st))) return rc;
+  CTX_CUDA(c, cudaMemsetAsync(c->d_acc, 0, sizeof(float2) * n3, st));
+  CTX_CUDA(c, cudaMemsetAsync(c->d_zpart, 0, sizeof(float) * nzp, st));
+  Batch none;
+  memset(&none, 0, sizeof(none));
+  const int nr = (int)c->sets[set].R.size();
+  for (int k0 = 0; k0 < nr; k0 += c->K) {
+    Batch bt = make_batch(c, set, k0);
+    if ((rc = enqueue_recompute(c, bt, st))) return rc;
+    int e0 = mark(c, st);
+    CTX_CUDA(c, launch_cols_a_adj(N, bt, dC_dev, c->d_A, c->d_alpha, c->d_zpart, c->d_tw, st));
+    int e1 = mark(c, st);
+    CTX_CUDA(c, launch_cols(N, nullptr, bt, bt.K, 1, false, c->d_tw, st));
+    int e2 = mark(c, st);
+    CTX_CUDA(c, launch_rows_adj_acc(N, bt, c->d_acc, c->d_tw, st));
+    int e3 = mark(c, st);
+    span(c, KD_ADJA, e0, e1);
+    span(c, KD_ADJB, e1, e2);
+    span(c, KD_ADJR, e2, e3);
+  }
+  // back to real space: sum_R B_R (cotangents)
+  int f0 = mark(c, st);
+  CTX_CUDA(c, launch_inv_rows_plain(N, c->d_acc, c->d_tw, st));
+  CTX_CUDA(c, launch_cols(N, c->d_acc, none, 1, 1, true, c->d_tw, st));
+  CTX_CUDA(c, launch_cols(N, c->d_acc, none, 1, 0, true, c->d_tw, st));
+  double mul = 1.0;
+  for (int m = 0; m < c->pa.n_src_mul; ++m) {
+    double v;
+    memcpy(&v, &c->pa.src_mul[m], 8);
+    mul *= v;
+  }
+  CTX_CUDA(c, launch_grad_finish(n3, c->d_acc, c->d_alpha, delta_dev, c->d_rec0, 1.76105133f, 0.81722878f,
+                                 (float)mul, ddelta_dev, dsrc_dev, st));
+  span(c, KD_ADJF, f0, mark(c, st));
+  if (dzeta) {
+    std::vector<float> zp(nzp);
+    CTX_CUDA(c, cudaMemcpyAsync(zp.data(), c->d_zpart, sizeof(float) * nzp, cudaMemcpyDeviceToHost, st));
+    CTX_CUDA(c, cudaStreamSynchronize(st));
+    double s = 0.0;
+    for (float v : zp) s += v;
+    *dzeta = s;
+  }
+  return SF21_OK;
+}
+
+extern "C" int sf21_hii_criterion(sf21_hii_ctx* c, double z, int kind, const float* delta, const float* src,
+                                  int set, float* C, uint8_t* argmax) {
+  int rc = check_run_args(c, kind, delta, src, C);
+  if (rc) return rc;
+  CTX_CUDA(c, cudaSetDevice(c->device));
+  const size_t bf = sizeof(float) * c->n3;
+  CTX_CUDA(c, cudaMemcpyAsync(c->d_delta, delta, bf, cudaMemcpyHostToDevice, c->stream));
+  CTX_CUDA(c, cudaMemcpyAsync(c->d_src, src, bf, cudaMemcpyHostToDevice, c->stream));
+  if ((rc = ensure_adj_buffers(c))) return rc;
+  if ((rc = sf21_hii_criterion_device(c, z, kind, c->d_delta, c->d_src, set, c->d_C, c->d_A, c->stream)))
+    return rc;
+  CTX_CUDA(c, cudaMemcpyAsync(C, c->d_C, bf, cudaMemcpyDeviceToHost, c->stream));
+  if (argmax) CTX_CUDA(c, cudaMemcpyAsync(argmax, c->d_A, c->n3, cudaMemcpyDeviceToHost, c->stream));
+  CTX_CUDA(c, cudaStreamSynchronize(c->stream));
+  return SF21_OK;
+}
+
+extern "C" int sf21_hii_vjp(sf21_hii_ctx* c, double z, int kind, const float* delta, const float* src, int set,
+                            const float* dC, float* ddelta, float* dsrc, double* dzeta) {
+  int rc = check_run_args(c, kind, delta, src, dC);
+  if (rc) return rc;
+  CTX_CUDA(c, cudaSetDevice(c->device));
+  const size_t bf = sizeof(float) * c->n3;
+  if (!c->d_g) CTX_CUDA(c, cudaMalloc(&c->d_g, bf));
+  if (ddelta && !c->d_gd) CTX_CUDA(c, cudaMalloc(&c->d_gd, bf));
+  if (dsrc && !c->d_gs) CTX_CUDA(c, cudaMalloc(&c->d_gs, bf));
+  CTX_CUDA(c, cudaMemcpyAsync(c->d_delta, delta, bf, cudaMemcpyHostToDevice, c->stream));
+  CTX_CUDA(c, cudaMemcpyAsync(c->d_src, src, bf, cudaMemcpyHostToDevice, c->stream));
+  CTX_CUDA(c, cudaMemcpyAsync(c->d_g, dC, bf, cudaMemcpyHostToDevice, c->stream));
+  if ((rc = sf21_hii_vjp_device(c, z, kind, c->d_delta, c->d_src, set, c->d_g, ddelta ? c->d_gd : nullptr,
+                                dsrc ? c->d_gs : nullptr, dzeta, c->stream)))
+    return rc;
+  if (ddelta) CTX_CUDA(c, cudaMemcpyAsync(ddelta, c->d_gd, bf, cudaMemcpyDeviceToHost, c->stream));
+  if (dsrc) CTX_CUDA(c, cudaMemcpyAsync(dsrc, c->d_gs, bf, cudaMemcpyDeviceToHost, c->stream));
+  CTX_CUDA(c, cudaStreamSynchronize(c->stream));
+  return SF21_OK;
 }

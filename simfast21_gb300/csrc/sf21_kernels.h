@@ -1,5 +1,6 @@
 // Internal launch API between the C-ABI layer (hii_api.cu) and the kernels.
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -59,6 +60,33 @@ bool plane_supported(int N);
 cudaError_t plane_setup(int N);
 int plane_max_active_clusters(int N);
 cudaError_t launch_plane_filter(int N, const float2* spec, const Batch& bt, const float2* tw, cudaStream_t st);
+
+// TMA-pipelined persistent strided passes (kernels_pipe.cu).  The K work
+// boxes must be consecutive N^3 slices of one allocation starting at work0.
+struct PipeMaps {
+  CUtensorMap b_rows;  // tiles of rows along b (ky pass)
+  CUtensorMap a_rows;  // tiles of rows along a (kx pass)
+};
+bool pipe_supported(int N);
+cudaError_t pipe_setup(int N);
+cudaError_t pipe_make_maps(int N, PipeMaps* pm, int K, void* work_base);
+// mode 0: ky inverse pass in place over the batch's boxes; mode 1: kx inverse
+// pass + centre test + first-hit update.  nsm = persistent CTAs.
+cudaError_t launch_pipe(int N, int mode, const PipeMaps& pm, const Batch& bt, float2* work0, uint8_t* rc,
+                        const float* alpha, const float2* tw, int* err, int nsm, cudaStream_t st);
+
+// Criterion and adjoint (kernels_adj.cu).
+cudaError_t adj_setup(int N);
+int adj_zpart_blocks(int N);
+cudaError_t launch_cols_a_crit(int N, const Batch& bt, float* C, uint8_t* A, const float* alpha, const float2* tw,
+                               cudaStream_t st);
+cudaError_t launch_cols_a_adj(int N, const Batch& bt, const float* g, const uint8_t* A, const float* alpha,
+                              float* zpart, const float2* tw, cudaStream_t st);
+cudaError_t launch_rows_adj_acc(int N, const Batch& bt, float2* acc, const float2* tw, cudaStream_t st);
+cudaError_t launch_grad_finish(long n3, const float2* G, const float* alpha, const float* delta, const float* rec0,
+                               float r2, float r3, float src_mul, float* gdelta, float* gsrc, cudaStream_t st);
+cudaError_t launch_crit_init(long n3, float* C, uint8_t* A, cudaStream_t st);
+cudaError_t launch_crit_finalize(long n3, float* C, const uint8_t* A, cudaStream_t st);
 
 // Plain form (kernels_plain.cu).
 cudaError_t launch_plain_centres(long n3, const float2* box, const float* alpha, float zmul, float* mask, int* flag,

@@ -27,7 +27,8 @@ _STATUS = {0: "SF21_OK", 1: "SF21_E_ARG", 2: "SF21_E_ALLOC", 3: "SF21_E_CUDA",
 EXPORTS = [
     "sf21_hii_create", "sf21_hii_destroy", "sf21_hii_last_error", "sf21_hii_run_z",
     "sf21_hii_run_z_device", "sf21_hii_radii", "sf21_hii_prologue", "sf21_hii_filtered",
-    "sf21_hii_first_hit", "sf21_hii_run_z_plain_device", "sf21_hii_path", "sf21_hii_profile", "sf21_hii_profile_read", "sf21_hii_profile_name",
+    "sf21_hii_first_hit", "sf21_hii_run_z_plain_device", "sf21_hii_criterion", "sf21_hii_criterion_device",
+    "sf21_hii_vjp", "sf21_hii_vjp_device", "sf21_hii_path", "sf21_hii_check", "sf21_hii_profile", "sf21_hii_profile_read", "sf21_hii_profile_name",
 ]
 
 
@@ -71,7 +72,12 @@ def load_library(path: str = LIB_PATH):
                                     ctypes.c_int, fp, fp]
     L.sf21_hii_first_hit.argtypes = [vp, ctypes.c_double, ctypes.c_int, fp, fp, ctypes.c_int, fp]
     L.sf21_hii_run_z_plain_device.argtypes = [vp, ctypes.c_double, ctypes.c_int, vp, vp, ctypes.c_int, vp, vp]
-    L.sf21_hii_path.argtypes = [vp, dp, dp]
+    L.sf21_hii_criterion.argtypes = [vp, ctypes.c_double, ctypes.c_int, fp, fp, ctypes.c_int, fp, fp]
+    L.sf21_hii_criterion_device.argtypes = [vp, ctypes.c_double, ctypes.c_int, vp, vp, ctypes.c_int, vp, vp, vp]
+    L.sf21_hii_vjp.argtypes = [vp, ctypes.c_double, ctypes.c_int, fp, fp, ctypes.c_int, fp, fp, fp, dp]
+    L.sf21_hii_vjp_device.argtypes = [vp, ctypes.c_double, ctypes.c_int, vp, vp, ctypes.c_int, vp, vp, vp, dp, vp]
+    L.sf21_hii_path.argtypes = [vp, dp, ctypes.c_int]
+    L.sf21_hii_check.argtypes = [vp]
     L.sf21_hii_profile.argtypes = [vp, ctypes.c_int]
     L.sf21_hii_profile_read.argtypes = [vp, dp, ctypes.POINTER(ctypes.c_long), ctypes.c_int]
     L.sf21_hii_profile_name.argtypes = [ctypes.c_int]
@@ -134,10 +140,14 @@ class FilterBank:
 
     def path(self):
         """(pipeline in use: 1 = three axis passes, 2 = plane clusters,
-        tuned ms of one batch for each or 0)."""
-        a, b = ctypes.c_double(0), ctypes.c_double(0)
-        p = self._lib.sf21_hii_path(self._h, ctypes.byref(a), ctypes.byref(b))
-        return p, a.value, b.value
+        3 = TMA-pipelined three passes; {pipeline: tuned ms of one batch})."""
+        ms = (ctypes.c_double * 3)()
+        p = self._lib.sf21_hii_path(self._h, ms, 3)
+        return p, {i + 1: ms[i] for i in range(3)}
+
+    def check(self):
+        """Raise if a bounded device wait expired since the last check."""
+        self._check(self._lib.sf21_hii_check(self._h))
 
     def radii(self, s: int = 0):
         buf = (ctypes.c_double * 512)()
@@ -170,6 +180,42 @@ class FilterBank:
         self._check(self._lib.sf21_hii_run_z_plain_device(self._h, z, src_kind, ctypes.c_void_p(delta_ptr),
                                                           ctypes.c_void_p(src_ptr), s, ctypes.c_void_p(xhii_ptr),
                                                           ctypes.c_void_p(stream or None)))
+
+    # ---- differentiable criterion -------------------------------------------
+    def criterion(self, z: float, delta, src, s: int = 0, src_kind: int = SF21_SRC_SFRD):
+        """(C, argmax) boxes of set s; the argmax is kept as the vjp checkpoint."""
+        d = _f32(delta, self.n3)
+        sr = _f32(src, self.n3)
+        C = np.empty((self.N,) * 3, np.float32)
+        A = np.empty((self.N,) * 3, np.uint8)
+        self._check(self._lib.sf21_hii_criterion(self._h, z, src_kind, _ptr(d), _ptr(sr), s, _ptr(C), _ptr(A)))
+        return C, A
+
+    def vjp(self, z: float, delta, src, dC, s: int = 0, src_kind: int = SF21_SRC_SFRD):
+        """(dL/d delta, dL/d src, dL/d fesc) for the cotangent dC = dL/dC."""
+        d = _f32(delta, self.n3)
+        sr = _f32(src, self.n3)
+        g = _f32(dC, self.n3)
+        gd = np.empty((self.N,) * 3, np.float32)
+        gs = np.empty((self.N,) * 3, np.float32)
+        gz = ctypes.c_double(0.0)
+        self._check(self._lib.sf21_hii_vjp(self._h, z, src_kind, _ptr(d), _ptr(sr), s, _ptr(g), _ptr(gd),
+                                           _ptr(gs), ctypes.byref(gz)))
+        return gd, gs, gz.value
+
+    def criterion_device(self, z, delta_ptr, src_ptr, C_ptr, A_ptr, s=0, src_kind=SF21_SRC_SFRD, stream=0):
+        self._check(self._lib.sf21_hii_criterion_device(
+            self._h, z, src_kind, ctypes.c_void_p(delta_ptr), ctypes.c_void_p(src_ptr), s,
+            ctypes.c_void_p(C_ptr), ctypes.c_void_p(A_ptr), ctypes.c_void_p(stream or None)))
+
+    def vjp_device(self, z, delta_ptr, src_ptr, dC_ptr, gd_ptr, gs_ptr, s=0, src_kind=SF21_SRC_SFRD, stream=0,
+                   want_zeta=True):
+        gz = ctypes.c_double(0.0)
+        self._check(self._lib.sf21_hii_vjp_device(
+            self._h, z, src_kind, ctypes.c_void_p(delta_ptr), ctypes.c_void_p(src_ptr), s,
+            ctypes.c_void_p(dC_ptr), ctypes.c_void_p(gd_ptr or None), ctypes.c_void_p(gs_ptr or None),
+            ctypes.byref(gz) if want_zeta else None, ctypes.c_void_p(stream or None)))
+        return gz.value
 
     def prologue(self, z: float, delta, src, s: int = 0, src_kind: int = SF21_SRC_SFRD):
         d = _f32(delta, self.n3)

@@ -164,17 +164,19 @@ def test_plain_form_matches_reference(hii, oracle_lib):
 
 
 @pytest.mark.parametrize("N,L", [(64, 50.0), (128, 100.0)])
-def test_plane_and_three_pass_paths_agree(hii, N, L):
-    """The cluster plane pass (filter + kz + ky in distributed shared memory)
-    and the three axis passes run the same arithmetic: identical outputs."""
+def test_radius_pipelines_agree(hii, N, L):
+    """The three radius pipelines -- three axis passes, the cluster plane pass
+    (filter + kz + ky in distributed shared memory) and the TMA-pipelined
+    persistent strided passes -- run the same arithmetic: identical outputs."""
     w = synth.Workload(N=N, L=L, zs=[8.0], zeta=40.0, Rmax=L / 2, factor=1.1, seed=21)
     delta, sfrd = synth.make_boxes(w, 8.0)
     sets = [(40.0, L / 2, w.Nbins), (15.0, L / 5, 20)]
-    a = hii.FilterBank(N, L, 0.71, sets, path=1)
-    b = hii.FilterBank(N, L, 0.71, sets, path=2)
-    assert a.path()[0] == 1 and b.path()[0] == 2
-    xa, na = a.run_z(8.0, delta, sfrd)
-    xb, nb = b.run_z(8.0, delta, sfrd)
-    assert np.array_equal(xa.view(np.uint32), xb.view(np.uint32))
-    for s in range(len(sets)):
-        assert np.array_equal(a.first_hit(8.0, delta, sfrd, s), b.first_hit(8.0, delta, sfrd, s))
+    banks = {p: hii.FilterBank(N, L, 0.71, sets, path=p) for p in (1, 2, 3)}
+    ref_x, ref_n = banks[1].run_z(8.0, delta, sfrd)
+    for p in (2, 3):
+        assert banks[p].path()[0] == p
+        x, n = banks[p].run_z(8.0, delta, sfrd)
+        assert np.array_equal(ref_x.view(np.uint32), x.view(np.uint32)), p
+        for s in range(len(sets)):
+            assert np.array_equal(banks[1].first_hit(8.0, delta, sfrd, s), banks[p].first_hit(8.0, delta, sfrd, s))
+    banks[3].check()
