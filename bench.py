@@ -52,6 +52,9 @@ def workload(name: str):
         rng = np.random.default_rng(seed)
         zetas = np.exp(rng.uniform(np.log(10.0), np.log(100.0), 16))
         rmaxs = rng.uniform(5.0, 30.0, 16)
+    elif name == "single512":
+        N, L, z, seed = 512, 300.0, 7.0, 1236
+        zetas, rmaxs = np.array([30.0]), np.array([35.0])
     elif name == "single256":
         N, L, z, seed = 256, 150.0, 7.0, 1236
         zetas, rmaxs = np.array([30.0]), np.array([30.0])
@@ -76,6 +79,7 @@ def describe(w):
                           "(zeta log-U[10,100], Rmax U[10,60] Mpc/h, factor 1.05)",
             "batched256": "HII filter bank, batched: 256^3, L=150 Mpc/h, z=7, 16 sets",
             "single256": "HII filter bank: 256^3, L=150 Mpc/h, z=7, 1 set (zeta=30, Rmax=30 Mpc/h, factor 1.05)",
+            "single512": "HII filter bank: 512^3, L=300 Mpc/h, z=7, 1 set (zeta=30, Rmax=35 Mpc/h, factor 1.05)",
             "plain128": "HII filter bank: 128^3, L=100 Mpc/h, z=8, zeta=30, Rmax=50, factor 1.1"}[w["name"]]
 
 
@@ -312,8 +316,10 @@ def run_ours(args, w, rank, world):
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded lognormal density + SFRD boxes)",
             "config": {"workload": describe(w), "N": N, "sets": nsets, "radii_total": R_total,
                        "pipeline": {1: "three axis passes", 2: "cluster plane pass + kx pass",
-                                    3: "three axis passes, TMA-pipelined persistent strided passes"}[path],
-                       "tuned_batch_ms": {"three_pass": tuned[1], "plane": tuned[2], "tma_pipelined": tuned[3]},
+                                    3: "three axis passes, ky pass TMA-pipelined",
+                                    4: "three axis passes, ky and kx passes TMA-pipelined"}[path],
+                       "tuned_batch_ms": {"three_pass": tuned[1], "plane": tuned[2], "tma_ky": tuned[3],
+                                          "tma_ky_kx": tuned[4]},
                        "flush": "inputs larger than L2 (every box >= 537 MB)"},
             "e2e": {"value": e2e_val, "unit": "voxel*radii/s",
                     "h2d_bytes_per_step": 2 * 4 * n3, "d2h_bytes_per_step": nsets * 4 * n3},

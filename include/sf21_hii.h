@@ -62,8 +62,13 @@ typedef struct {
                         of each available one and keeps the fastest),
                         1 = three axis passes, 2 = plane passes on
                         thread-block clusters (N 64..512), 3 = three axis
-                        passes with TMA-pipelined persistent strided passes
-                        (N 64..1024) */
+                        passes with the ky pass TMA-pipelined and
+                        persistent, 4 = ky and kx passes TMA-pipelined
+                        (3 and 4: N 64..1024) */
+  int graph;         /* 0 = sf21_hii_run_z_device captures its per-redshift
+                        schedule as a CUDA graph and replays it while z, the
+                        kind, the buffers and the stream stay the same;
+                        -1 = launch kernel by kernel */
 } sf21_hii_config;
 
 typedef struct sf21_hii_ctx sf21_hii_ctx;
@@ -107,6 +112,19 @@ int sf21_hii_run_z_device(sf21_hii_ctx *ctx, double z, int src_kind, const float
 int sf21_hii_run_z_plain_device(sf21_hii_ctx *ctx, double z, int src_kind, const float *delta_dev,
                                 const float *src_dev, int set, float *xhii_dev, void *stream);
 
+/* Halo-catalogue source (use_SFR = F): from the catalogue records
+ * {float Mass, x, y, z} (Halo_t, auxiliary.h:13-17; positions in N_halo cell
+ * units) builds on the GPU the box the reference holds in halo_map after
+ * get_HIIbubbles.c:249-253 -- cloud-in-cell of Rion(M, z) on the N_halo^3 grid
+ * in catalogue order and the block average to N_smoothed^3 -- bit-identical,
+ * i.e. the SF21_SRC_RION input.  Replaces the serial loop :233-253. */
+int sf21_hii_halo_source(sf21_hii_ctx *ctx, double z, long nhalos, const void *halos, float *rion_box);
+
+/* One redshift of the halo branch end to end (source box + :215-477); the
+ * source box stays on the GPU.  Same outputs as sf21_hii_run_z. */
+int sf21_hii_run_z_halos(sf21_hii_ctx *ctx, double z, const float *delta, long nhalos, const void *halos,
+                         float *xhii, double *neutral);
+
 /* Radius list of a set exactly as the reference iterates it (:192, 298-461):
  * writes up to cap radii (Mpc/h, descending), returns the count (or <0 on
  * error); *n_fft receives how many take the FFT branch (R >= 2 dx). */
@@ -130,7 +148,9 @@ int sf21_hii_first_hit(sf21_hii_ctx *ctx, double z, int src_kind, const float *d
                        const float *src, int set, uint8_t *rc);
 
 /* Continuous ionisation criterion of set `set`: C(x) = max over the set's
- * radii R with rec_R(x) > 0 of ion_R(x) / rec_R(x), the ratio the reference
+ * FFT-branch radii (R >= 2 dx, :299) with rec_R(x) > 0 of ion_R(x) / rec_R(x)
+ * (below 2 dx the top-hat's ringing takes rec_R through zero and the ratio is
+ * ill-conditioned), the ratio the reference
  * thresholds at 1 (get_HIIbubbles.c:339-348, 437-438), and the radius index
  * of the maximum (argmax, 0xFF where no radius has rec_R > 0; C = 0 there).
  * No reference counterpart: the reference only tests ratio >= 1.  The
@@ -152,7 +172,7 @@ int sf21_hii_vjp_device(sf21_hii_ctx *ctx, double z, int src_kind, const float *
                         const float *src_dev, int set, const float *dC_dev, float *ddelta_dev,
                         float *dsrc_dev, double *dfesc, void *stream);
 
-/* Radius pipeline in use (1..3, see sf21_hii_config.path); ms_tuned[p-1]
+/* Radius pipeline in use (1..4, see sf21_hii_config.path); ms_tuned[p-1]
  * receives the measured ms of one batch of pipeline p when it was tuned at
  * create (0 if not timed), for p <= cap. */
 int sf21_hii_path(const sf21_hii_ctx *ctx, double *ms_tuned, int cap);

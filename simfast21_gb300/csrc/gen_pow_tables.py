@@ -27,6 +27,7 @@ for k in range(11):
     ifact.append(rnd(Decimal(2) ** 124 / f))
 exp2t = [rnd(Decimal(2) ** 124 * (LN2 * Decimal(j) / 128).exp()) for j in range(128)]
 inv_ln2 = rnd(Decimal(2) ** 124 / LN2)
+log2e_q96 = rnd(Decimal(2) ** 96 / LN2)
 ln2 = rnd(Decimal(2) ** 124 * LN2)
 
 M64 = (1 << 64) - 1
@@ -57,6 +58,8 @@ out.append(arr("SD_POW_EXP2T_HI", [v >> 64 for v in exp2t]))
 out.append(arr("SD_POW_EXP2T_LO", [v & M64 for v in exp2t]))
 out.append(f"#define SD_POW_INV_LN2_HI (0x{inv_ln2 >> 64:016x}ULL)")
 out.append(f"#define SD_POW_INV_LN2_LO (0x{inv_ln2 & M64:016x}ULL)")
+out.append(f"#define SD_EXP_LOG2E_HI (0x{log2e_q96 >> 64:016x}ULL)")
+out.append(f"#define SD_EXP_LOG2E_LO (0x{log2e_q96 & M64:016x}ULL)")
 out.append(f"#define SD_POW_LN2_HI (0x{ln2 >> 64:016x}ULL)")
 out.append(f"#define SD_POW_LN2_LO (0x{ln2 & M64:016x}ULL)")
 print("\n".join(out))

@@ -66,9 +66,20 @@ struct sf21_hii_ctx {
   double L = 0, hubble = 0, dx = 0, dk = 0;
   int K = 8;
   int path = 1;             // 1 = three axis passes, 2 = plane clusters + kx pass,
-                            // 3 = three axis passes, strided ones TMA-pipelined
-  double tune_ms[4] = {0, 0, 0, 0};
+                            // 3 = three axis passes, ky pass TMA-pipelined,
+                            // 4 = three axis passes, ky and kx passes TMA-pipelined
+  double tune_ms[5] = {0, 0, 0, 0, 0};
   float2* d_work_base = nullptr;  // K consecutive work boxes
+  // CUDA graph of the per-redshift schedule of run_z_device (replayed while
+  // z, the source kind, the buffers and the stream stay the same)
+  bool use_graph = true;
+  cudaGraphExec_t gexec = nullptr;
+  struct GraphKey {
+    double z;
+    int kind;
+    const void *delta, *src, *xhii;
+    cudaStream_t st;
+  } gkey = {0, -1, nullptr, nullptr, nullptr, nullptr};
   PipeMaps pmaps;
   int* d_err = nullptr;
   int nsm = 0;
@@ -84,6 +95,12 @@ struct sf21_hii_ctx {
   float *d_g = nullptr, *d_gd = nullptr, *d_gs = nullptr;
   int crit_set = -1;
   double crit_z = 0;
+  // halo-catalogue source buffers (allocated / grown on use)
+  void* d_halos = nullptr;
+  long halo_cap = 0;
+  float* d_fine = nullptr;
+  void* d_hscratch = nullptr;
+  size_t hscratch_bytes = 0;
   // plain-form buffers (allocated on first use)
   float* d_mask = nullptr;
   int* d_flag = nullptr;
@@ -180,7 +197,8 @@ static void free_ctx(sf21_hii_ctx* c) {
   cudaSetDevice(c->device);
   void* ptrs[] = {c->d_delta, c->d_src, c->d_rec0, c->d_fres, c->d_partials, c->d_alpha,
                   c->d_xhii, c->d_spec, c->d_tw, c->d_rc, c->d_mask, c->d_flag, c->d_box2,
-                  c->d_C, c->d_A, c->d_acc, c->d_zpart, c->d_g, c->d_gd, c->d_gs};
+                  c->d_C, c->d_A, c->d_acc, c->d_zpart, c->d_g, c->d_gd, c->d_gs, c->d_halos, c->d_fine,
+                  c->d_hscratch};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->d_work_base) cudaFree(c->d_work_base);
@@ -188,6 +206,7 @@ static void free_ctx(sf21_hii_ctx* c) {
   for (SetInfo& s : c->sets)
     if (s.d_nmax) cudaFree(s.d_nmax);
   for (cudaEvent_t e : c->ev) cudaEventDestroy(e);
+  if (c->gexec) cudaGraphExecDestroy(c->gexec);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -269,6 +288,7 @@ extern "C" int sf21_hii_create(const sf21_hii_config* cfg, sf21_hii_ctx** out) {
   int K = cfg->kmax > 0 ? cfg->kmax : KMAX;
   if (K > KMAX) K = KMAX;
   c->K = K;
+  c->use_graph = cfg->graph >= 0;
 #define CREATE_CUDA(call)                                                                   \
   do {                                                                                      \
     cudaError_t _e = (call);                                                                \
@@ -321,7 +341,7 @@ extern "C" int sf21_hii_create(const sf21_hii_config* cfg, sf21_hii_ctx** out) {
     can_pipe = true;
   cudaGetLastError();
   const int want = cfg->path;
-  if ((want == 2 && !can_plane) || (want == 3 && !can_pipe) || want < 0 || want > 3) {
+  if ((want == 2 && !can_plane) || (want >= 3 && !can_pipe) || want < 0 || want > 4) {
     g_create_err = "requested radius pipeline not available for this box on this device";
     free_ctx(c);
     return SF21_E_UNSUPPORTED;
@@ -342,9 +362,9 @@ extern "C" int sf21_hii_create(const sf21_hii_config* cfg, sf21_hii_ctx** out) {
     cudaEvent_t t0, t1;
     CREATE_CUDA(cudaEventCreate(&t0));
     CREATE_CUDA(cudaEventCreate(&t1));
-    double best[4] = {1e30, 1e30, 1e30, 1e30};
-    for (int p = 1; p <= 3; ++p) {
-      if ((p == 2 && !can_plane) || (p == 3 && !can_pipe)) continue;
+    double best[5] = {1e30, 1e30, 1e30, 1e30, 1e30};
+    for (int p = 1; p <= 4; ++p) {
+      if ((p == 2 && !can_plane) || (p >= 3 && !can_pipe)) continue;
       c->path = p;
       for (int rep = 0; rep < 4; ++rep) {
         CREATE_CUDA(cudaEventRecord(t0, c->stream));
@@ -371,7 +391,7 @@ extern "C" int sf21_hii_create(const sf21_hii_config* cfg, sf21_hii_ctx** out) {
       return SF21_E_TIMEOUT;
     }
     c->path = 1;
-    for (int p = 2; p <= 3; ++p)
+    for (int p = 2; p <= 4; ++p)
       if (best[p] < best[c->path]) c->path = p;
   }
 #undef CREATE_CUDA
@@ -438,13 +458,16 @@ static int enqueue_batch(sf21_hii_ctx* c, const Batch& bt, cudaStream_t st) {
     span(c, KD_ICA, e1, e2);
     return SF21_OK;
   }
-  if (c->path == 3) {
+  if (c->path == 3 || c->path == 4) {
     int e0 = mark(c, st);
     CTX_CUDA(c, launch_inv_rows_filter(N, c->d_spec, bt, c->d_tw, st));
     int e1 = mark(c, st);
     CTX_CUDA(c, launch_pipe(N, 0, c->pmaps, bt, c->d_work_base, c->d_rc, c->d_alpha, c->d_tw, c->d_err, c->nsm, st));
     int e2 = mark(c, st);
-    CTX_CUDA(c, launch_pipe(N, 1, c->pmaps, bt, c->d_work_base, c->d_rc, c->d_alpha, c->d_tw, c->d_err, c->nsm, st));
+    if (c->path == 4)
+      CTX_CUDA(c, launch_pipe(N, 1, c->pmaps, bt, c->d_work_base, c->d_rc, c->d_alpha, c->d_tw, c->d_err, c->nsm, st));
+    else
+      CTX_CUDA(c, launch_cols_a_test(N, bt, c->d_rc, c->d_alpha, c->d_tw, st));
     int e3 = mark(c, st);
     span(c, KD_IROWS, e0, e1);
     span(c, KD_ICB, e1, e2);
@@ -510,17 +533,61 @@ static int check_run_args(sf21_hii_ctx* c, int kind, const void* delta, const vo
   return SF21_OK;
 }
 
+static int enqueue_run(sf21_hii_ctx* c, double z, int kind, const float* delta_dev, const float* src_dev,
+                       float* xhii_dev, cudaStream_t st) {
+  int rc;
+  if ((rc = enqueue_front(c, z, kind, delta_dev, src_dev, st))) return rc;
+  for (int s = 0; s < (int)c->sets.size(); ++s) {
+    if ((rc = enqueue_radii(c, s, st))) return rc;
+    if ((rc = enqueue_finish(c, s, src_dev, xhii_dev + (size_t)s * c->n3, st))) return rc;
+  }
+  return SF21_OK;
+}
+
 extern "C" int sf21_hii_run_z_device(sf21_hii_ctx* c, double z, int kind, const float* delta_dev,
                                      const float* src_dev, float* xhii_dev, void* stream) {
   int rc = check_run_args(c, kind, delta_dev, src_dev, xhii_dev);
   if (rc) return rc;
   CTX_CUDA(c, cudaSetDevice(c->device));
   cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
-  if ((rc = enqueue_front(c, z, kind, delta_dev, src_dev, st))) return rc;
-  for (int s = 0; s < (int)c->sets.size(); ++s) {
-    if ((rc = enqueue_radii(c, s, st))) return rc;
-    if ((rc = enqueue_finish(c, s, src_dev, xhii_dev + (size_t)s * c->n3, st))) return rc;
+  if (!c->use_graph || c->prof) return enqueue_run(c, z, kind, delta_dev, src_dev, xhii_dev, st);
+  // replay the captured schedule if nothing it depends on changed
+  sf21_hii_ctx::GraphKey key = {z, kind, delta_dev, src_dev, xhii_dev, st};
+  const bool same = c->gexec && key.z == c->gkey.z && key.kind == c->gkey.kind && key.delta == c->gkey.delta &&
+                    key.src == c->gkey.src && key.xhii == c->gkey.xhii && key.st == c->gkey.st;
+  if (!same) {
+    cudaGraph_t g = nullptr;
+    CTX_CUDA(c, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    rc = enqueue_run(c, z, kind, delta_dev, src_dev, xhii_dev, st);
+    cudaError_t ce = cudaStreamEndCapture(st, &g);
+    if (rc) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (ce != cudaSuccess) CTX_FAIL(c, SF21_E_CUDA, "graph capture failed: %s", cudaGetErrorString(ce));
+    bool updated = false;
+    if (c->gexec) {
+      cudaGraphExecUpdateResultInfo info;
+      if (cudaGraphExecUpdate(c->gexec, g, &info) == cudaSuccess) {
+        updated = true;
+      } else {
+        cudaGetLastError();
+        cudaGraphExecDestroy(c->gexec);
+        c->gexec = nullptr;
+      }
+    }
+    if (!updated) {
+      ce = cudaGraphInstantiate(&c->gexec, g, 0);
+      if (ce != cudaSuccess) {
+        cudaGraphDestroy(g);
+        c->gexec = nullptr;
+        CTX_FAIL(c, SF21_E_CUDA, "graph instantiate failed: %s", cudaGetErrorString(ce));
+      }
+    }
+    cudaGraphDestroy(g);
+    c->gkey = key;
   }
+  CTX_CUDA(c, cudaGraphLaunch(c->gexec, st));
   return SF21_OK;
 }
 
@@ -724,7 +791,7 @@ extern "C" int sf21_hii_run_z_plain_device(sf21_hii_ctx* c, double z, int kind, 
 
 extern "C" int sf21_hii_path(const sf21_hii_ctx* c, double* ms_tuned, int cap) {
   if (!c) return -SF21_E_ARG;
-  for (int p = 1; p <= 3 && p <= cap; ++p) ms_tuned[p - 1] = c->tune_ms[p] < 1e29 ? c->tune_ms[p] : 0.0;
+  for (int p = 1; p <= 4 && p <= cap; ++p) ms_tuned[p - 1] = c->tune_ms[p] < 1e29 ? c->tune_ms[p] : 0.0;
   return c->path;
 }
 
@@ -773,9 +840,8 @@ static int enqueue_recompute(sf21_hii_ctx* c, const Batch& bt, cudaStream_t st) 
   return SF21_OK;
 }
 
-static Batch make_batch(const sf21_hii_ctx* c, int set, int k0) {
+static Batch make_batch(const sf21_hii_ctx* c, int set, int k0, int nr) {
   const SetInfo& s = c->sets[set];
-  const int nr = (int)s.R.size();
   Batch bt;
   memset(&bt, 0, sizeof(bt));
   bt.K = nr - k0 < c->K ? nr - k0 : c->K;
@@ -801,9 +867,9 @@ extern "C" int sf21_hii_criterion_device(sf21_hii_ctx* c, double z, int kind, co
   if ((rc = enqueue_front(c, z, kind, delta_dev, src_dev, st))) return rc;
   const int N = (int)c->N;
   CTX_CUDA(c, launch_crit_init(c->n3, c->d_C, c->d_A, st));
-  const int nr = (int)c->sets[set].R.size();
+  const int nr = c->sets[set].n_fft;  // radii of the FFT branch (R >= 2 dx)
   for (int k0 = 0; k0 < nr; k0 += c->K) {
-    Batch bt = make_batch(c, set, k0);
+    Batch bt = make_batch(c, set, k0, nr);
     if ((rc = enqueue_recompute(c, bt, st))) return rc;
     int e0 = mark(c, st);
     CTX_CUDA(c, launch_cols_a_crit(N, bt, c->d_C, c->d_A, c->d_alpha, c->d_tw, st));
@@ -839,9 +905,9 @@ extern "C" int sf21_hii_vjp_device(sf21_hii_ctx* c, double z, int kind, const fl
   CTX_CUDA(c, cudaMemsetAsync(c->d_zpart, 0, sizeof(float) * nzp, st));
   Batch none;
   memset(&none, 0, sizeof(none));
-  const int nr = (int)c->sets[set].R.size();
+  const int nr = c->sets[set].n_fft;
   for (int k0 = 0; k0 < nr; k0 += c->K) {
-    Batch bt = make_batch(c, set, k0);
+    Batch bt = make_batch(c, set, k0, nr);
     if ((rc = enqueue_recompute(c, bt, st))) return rc;
     int e0 = mark(c, st);
     CTX_CUDA(c, launch_cols_a_adj(N, bt, dC_dev, c->d_A, c->d_alpha, c->d_zpart, c->d_tw, st));
@@ -915,4 +981,79 @@ extern "C" int sf21_hii_vjp(sf21_hii_ctx* c, double z, int kind, const float* de
   if (dsrc) CTX_CUDA(c, cudaMemcpyAsync(dsrc, c->d_gs, bf, cudaMemcpyDeviceToHost, c->stream));
   CTX_CUDA(c, cudaStreamSynchronize(c->stream));
   return SF21_OK;
+}
+
+// ---- halo-catalogue source box on the GPU ---------------------------------------
+static int enqueue_halo_source(sf21_hii_ctx* c, double z, long nhalos, const void* halos, float* out_dev,
+                               cudaStream_t st) {
+  if (nhalos < 0 || (nhalos > 0 && !halos)) CTX_FAIL(c, SF21_E_ARG, "bad halo catalogue");
+  if (c->N_halo < c->N) CTX_FAIL(c, SF21_E_ARG, "N_halo < N_smoothed (smooth_box, auxiliary.c:651-654)");
+  if (nhalos > (1L << 28)) CTX_FAIL(c, SF21_E_UNSUPPORTED, "more than 2^28 halos");
+  const long nh3 = c->N_halo * c->N_halo * c->N_halo;
+  if (!c->d_fine) CTX_CUDA(c, cudaMalloc(&c->d_fine, sizeof(float) * nh3));
+  if (nhalos > c->halo_cap) {
+    if (c->d_halos) cudaFree(c->d_halos);
+    if (c->d_hscratch) cudaFree(c->d_hscratch);
+    c->d_halos = nullptr;
+    c->d_hscratch = nullptr;
+    c->halo_cap = 0;
+    const long cap = nhalos + nhalos / 4 + 1024;
+    CTX_CUDA(c, cudaMalloc(&c->d_halos, (size_t)cap * 16));
+    c->hscratch_bytes = halo_scratch_bytes(cap);
+    CTX_CUDA(c, cudaMalloc(&c->d_hscratch, c->hscratch_bytes));
+    c->halo_cap = cap;
+  }
+  if (nhalos > 0)
+    CTX_CUDA(c, cudaMemcpyAsync(c->d_halos, halos, (size_t)nhalos * 16, cudaMemcpyHostToDevice, st));
+  CTX_CUDA(c, launch_halo_source(nhalos, c->d_halos, z, c->N_halo, c->N, c->d_fine, out_dev, c->d_hscratch,
+                                 c->hscratch_bytes, st));
+  return SF21_OK;
+}
+
+extern "C" int sf21_hii_halo_source(sf21_hii_ctx* c, double z, long nhalos, const void* halos, float* rion) {
+  if (!c || !rion) return SF21_E_ARG;
+  CTX_CUDA(c, cudaSetDevice(c->device));
+  int rc = enqueue_halo_source(c, z, nhalos, halos, c->d_src, c->stream);
+  if (rc) return rc;
+  CTX_CUDA(c, cudaMemcpyAsync(rion, c->d_src, sizeof(float) * c->n3, cudaMemcpyDeviceToHost, c->stream));
+  CTX_CUDA(c, cudaStreamSynchronize(c->stream));
+  return SF21_OK;
+}
+
+extern "C" int sf21_hii_run_z_halos(sf21_hii_ctx* c, double z, const float* delta, long nhalos, const void* halos,
+                                    float* xhii, double* neutral) {
+  if (!c || !delta || !xhii) return SF21_E_ARG;
+  CTX_CUDA(c, cudaSetDevice(c->device));
+  cudaStream_t st = c->stream;
+  const size_t bf = sizeof(float) * c->n3;
+  int rc = enqueue_halo_source(c, z, nhalos, halos, c->d_src, st);
+  if (rc) return rc;
+  CTX_CUDA(c, cudaMemcpyAsync(c->d_delta, delta, bf, cudaMemcpyHostToDevice, st));
+  if ((rc = enqueue_front(c, z, SF21_SRC_RION, c->d_delta, c->d_src, st))) return rc;
+  std::vector<std::thread> sums;
+  int status = SF21_OK;
+  for (int s = 0; s < (int)c->sets.size() && status == SF21_OK; ++s) {
+    if ((status = enqueue_radii(c, s, st))) break;
+    if ((status = enqueue_finish(c, s, c->d_src, c->d_xhii, st))) break;
+    float* dst = xhii + (size_t)s * c->n3;
+    cudaError_t e = cudaMemcpyAsync(dst, c->d_xhii, bf, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+      c->err = std::string("xHII download failed: ") + cudaGetErrorString(e);
+      status = SF21_E_CUDA;
+      break;
+    }
+    if (neutral) {
+      const long n3 = c->n3;
+      double* out = neutral + s;
+      sums.emplace_back([dst, n3, out]() {
+        double acc = 0.;
+        for (long i = 0; i < n3; ++i) acc += 1.0 - dst[i];
+        *out = acc / n3;
+      });
+    }
+  }
+  for (std::thread& t : sums) t.join();
+  if (status == SF21_OK) status = check_device_flag(c);
+  return status;
 }

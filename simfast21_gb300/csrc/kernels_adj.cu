@@ -4,9 +4,12 @@
 // ion_R = zeta * B_R ion1, rec_R = B_R rec0 with B_R = IFFT(W_R FFT(.)) the
 // (unnormalised, real, symmetric) top-hat filter of radius R, rec0 the
 // recombination-rate box (get_HIIbubbles.c:222) and ion1 the zeta-free
-// ionisation-rate box (:273).  Radii with rec_R(x) <= 0 do not compete (the
-// reference's test treats them as automatic centres, :340-347, so they carry
-// no ratio).  The forward keeps the running max and its radius index A(x)
+// ionisation-rate box (:273).  The maximum runs over the radii of the FFT
+// branch (R >= 2 dx, :299): below that the sharp k-space top-hat rings and
+// the filtered recombination rate passes through zero, where the ratio is
+// ill-conditioned (the small-R branch, :402-458, tests single cells).  Radii
+// with rec_R(x) <= 0 do not compete (the reference's test treats them as
+// automatic centres, :340-347, so they carry no ratio).  The forward keeps the running max and its radius index A(x)
 // (uint8): the index is the only checkpoint; the backward recomputes the
 // filtered fields radius by radius.
 //

@@ -88,6 +88,13 @@ cudaError_t launch_grad_finish(long n3, const float2* G, const float* alpha, con
 cudaError_t launch_crit_init(long n3, float* C, uint8_t* A, cudaStream_t st);
 cudaError_t launch_crit_finalize(long n3, float* C, const uint8_t* A, cudaStream_t st);
 
+// Halo-catalogue source box (kernels_halo.cu): CIC of Rion + block average,
+// bit-identical with the reference's serial loop.  halos_dev: nh records
+// {float Mass, x, y, z}; fine: N_halo^3 floats; out: N_smooth^3 floats.
+size_t halo_scratch_bytes(long nh);
+cudaError_t launch_halo_source(long nh, const void* halos_dev, double z, long N_halo, long N_smooth, float* fine,
+                               float* out, void* scratch, size_t scratch_bytes, cudaStream_t st);
+
 // Plain form (kernels_plain.cu).
 cudaError_t launch_plain_centres(long n3, const float2* box, const float* alpha, float zmul, float* mask, int* flag,
                                  cudaStream_t st);

@@ -316,13 +316,9 @@ SD_HD sd_i128 sd_mulq124(sd_i128 a, sd_i128 b) {
 // and 2^w = 2^n 2^(j2/128) e^u with u = r ln 2 < 2^-7.5 and e^u to u^10.
 // Every constant is a Q.124 (or Q.96) fixed-point number, so the relative
 // error of the result before the final rounding is far below 2^-80.
-SD_HD sd_t sd_pow(sd_t x, sd_t y) {
-  if (sd_is_zero(y)) return 0x3FF0000000000000ULL;
-  if (sd_is_zero(x)) return (y >> 63) ? 0x7FF0000000000000ULL : 0;
-  if (x >> 63) return SD_QNAN;
+// log2(x) in Q.96 for a positive normal x with binary exponent in [-60, 60].
+SD_HD sd_i128 sd_log2_q96(sd_t x) {
   const int ex = (int)((x >> 52) & 0x7FF) - 1023;
-  const int ey = (int)((y >> 52) & 0x7FF) - 1023;
-  if (ex < -60 || ex > 60 || ey > 5 || ey < -60) return SD_QNAN;
   const uint64_t M = (x & 0xFFFFFFFFFFFFFULL) | (1ULL << 52);
   const int j = (int)((M >> 45) & 127);
   // m/c_j = M * INV[j] / 2^114 (exact); t in Q.124
@@ -332,10 +328,16 @@ SD_HD sd_t sd_pow(sd_t x, sd_t y) {
   for (int k = 8; k >= 1; --k)
     acc = SD_Q124(SD_POW_RCP_HI[k], SD_POW_RCP_LO[k]) - sd_mulq124(T, acc);
   const sd_i128 lnp = sd_mulq124(T, acc);  // ln(1 + t), Q.124, |lnp| < 2^117
-  // log2(x) in Q.96
   sd_i128 l2 = sd_mulq124(lnp, SD_Q124(SD_POW_INV_LN2_HI, SD_POW_INV_LN2_LO)) >> 28;
   l2 += (sd_i128)(((sd_u128)SD_POW_L2C_HI[j] << 64) | SD_POW_L2C_LO[j]);
   l2 += ((sd_i128)ex) << 96;  // |l2| < 2^103
+  return l2;
+}
+
+// 2^(y * l2) for a double y with binary exponent in [-60, 10] and l2 in Q.96
+// (|l2| < 2^103), rounded once to double; 0 / inf outside the range.
+SD_HD sd_t sd_exp2_mul(sd_t y, sd_i128 l2) {
+  const int ey = (int)((y >> 52) & 0x7FF) - 1023;
   // w = y * l2 in Q.96, y = my * 2^(ey - 52)
   const uint64_t my = (y & 0xFFFFFFFFFFFFFULL) | (1ULL << 52);
   const bool wneg = ((y >> 63) != 0) != (l2 < 0);
@@ -343,7 +345,7 @@ SD_HD sd_t sd_pow(sd_t x, sd_t y) {
   const uint64_t u0 = (uint64_t)ul2, u1 = (uint64_t)(ul2 >> 64);  // u1 < 2^39
   const sd_u128 q0 = (sd_u128)u0 * my;  // weight 1
   const sd_u128 q1 = (sd_u128)u1 * my;  // weight 2^64, < 2^92
-  const int s = 52 - ey;                // >= 47
+  const int s = 52 - ey;                // >= 42
   sd_u128 w;                            // |w| in Q.96
   if (s <= 64)
     w = (q1 << (64 - s)) + (q0 >> s);
@@ -359,7 +361,8 @@ SD_HD sd_t sd_pow(sd_t x, sd_t y) {
       n = -n;
     }
   }
-  if (n > 1000 || n < -1000) return SD_QNAN;
+  if (n > 1023) return 0x7FF0000000000000ULL;
+  if (n < -1022) return 0;  // below the normal range (not met by the prologue)
   const int j2 = (int)(f >> 89);
   const sd_i128 r = (sd_i128)((f & ((((sd_u128)1) << 89) - 1)) << 28);  // Q.124, < 2^-7
   const sd_i128 u = sd_mulq124(r, SD_Q124(SD_POW_LN2_HI, SD_POW_LN2_LO));
@@ -373,4 +376,26 @@ SD_HD sd_t sd_pow(sd_t x, sd_t y) {
   const int sh = lead - 62;
   const uint64_t m = (uint64_t)(mm >> sh) | ((mm & ((((sd_u128)1) << sh) - 1)) != 0);
   return sd_round_pack(0, (int)n + (lead - 124), m);
+}
+
+SD_HD sd_t sd_pow(sd_t x, sd_t y) {
+  if (sd_is_zero(y)) return 0x3FF0000000000000ULL;
+  if (sd_is_zero(x)) return (y >> 63) ? 0x7FF0000000000000ULL : 0;
+  if (x >> 63) return SD_QNAN;
+  const int ex = (int)((x >> 52) & 0x7FF) - 1023;
+  const int ey = (int)((y >> 52) & 0x7FF) - 1023;
+  if (ex < -60 || ex > 60 || ey > 5 || ey < -60) return SD_QNAN;
+  return sd_exp2_mul(y, sd_log2_q96(x));
+}
+
+// exp(x) = 2^(x log2 e), correctly rounded for |x| < 2048 with a normal
+// result; results below the double normal range return 0 (they round to 0 in
+// float, which is all the stage keeps).
+SD_HD sd_t sd_exp(sd_t x) {
+  if (sd_is_zero(x)) return 0x3FF0000000000000ULL;
+  const int ex = (int)((x >> 52) & 0x7FF) - 1023;
+  if (ex < -60) return 0x3FF0000000000000ULL;  // |x| < 2^-60: exp(x) rounds to 1
+  if (ex > 10) return (x >> 63) ? 0 : 0x7FF0000000000000ULL;
+  const sd_i128 log2e = (sd_i128)(((sd_u128)SD_EXP_LOG2E_HI << 64) | SD_EXP_LOG2E_LO);  // Q.96
+  return sd_exp2_mul(x, log2e);
 }

@@ -140,19 +140,22 @@ int main(int argc, char *argv[]) {
     fflush(stdout);
     snprintf(fname, sizeof fname, "%s/delta/deltanl_z%.3f_N%ld_L%.1f.dat", base, redshift, N, Lmpc);
     if (sf21_read_box(fname, delta, N3) != 0) die("\nError reading deltanl file... Check path or if the file exists...");
-    int kind;
     if (sp.use_SFR) {
       snprintf(fname, sizeof fname, "%s/SFR/sfrd_z%.3f_N%ld_L%.1f.dat", base, redshift, N, Lmpc);
       if (sf21_read_box(fname, src, N3) != 0) die("\nError reading SFR file... Check path or if the file exists...");
-      kind = SF21_SRC_SFRD;
+      rc = sf21_hii_run_z(ctx, redshift, SF21_SRC_SFRD, delta, src, xhii, neutral);
     } else {
+      /* halo branch: cloud-in-cell of Rion and smooth_box on the GPU (:229-259) */
       snprintf(fname, sizeof fname, "%s/Halos/halonl_z%.3f_N%ld_L%.1f.dat.catalog", base, redshift, sp.N_halo,
                Lmpc);
-      if (sf21_halo_rion_box(fname, redshift, &sp, src) != 0)
+      long nh = 0;
+      void *halos = NULL;
+      if (sf21_read_halos(fname, &nh, &halos) != 0)
         die("\nError reading halo catalogue... Check path or if the file exists...");
-      kind = SF21_SRC_RION;
+      printf("Reading %ld halos...\n", nh);
+      rc = sf21_hii_run_z_halos(ctx, redshift, delta, nh, halos, xhii, neutral);
+      free(halos);
     }
-    rc = sf21_hii_run_z(ctx, redshift, kind, delta, src, xhii, neutral);
     if (rc != SF21_OK) {
       printf("sf21_hii_run_z failed (%d): %s\n", rc, sf21_hii_last_error(ctx));
       return 1;

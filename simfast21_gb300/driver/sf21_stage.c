@@ -69,74 +69,16 @@ int sf21_write_box(const char *path, const float *buf, long n) {
   return put == (size_t)n ? 0 : 2;
 }
 
-/* Rion(M, z), user_functions.c:40-47 */
-static double rion_of(float m, double z) {
-  const double c1 = 1.575e39, c2 = 9.367608e+07, c3 = 0.44, c4 = 2.27044695e+00;
-  double t1 = c1 * m * pow((1.0 + z), c4);
-  double t2 = pow((m / c2), c3);
-  double t3 = exp(-pow((c2 / m), 3.0));
-  return t1 * t2 * t3 / 1.e+45;
-}
-
-static long wrap(long x, long n) {
-  x = x % n;
-  if (x < 0) x += n;
-  return x;
-}
-
-/* cloud-in-cell of one value, the reference's corner order (auxiliary.c:761-808) */
-static void cic(float x1, float y1, float z1, float v, float *map, long N) {
-  long x = (long)x1, y = (long)y1, z = (long)z1;
-  x1 -= x;
-  y1 -= y;
-  z1 -= z;
-  for (long a = 0; a < 2; a++)
-    for (long b = 0; b < 2; b++)
-      for (long c = 0; c < 2; c++) {
-        x += a; y += b; z += c;
-        if (x1 < 0.0) { x = x - 1; x1 = fabsf(x1); }
-        if (y1 < 0.0) { y = y - 1; y1 = fabsf(y1); }
-        if (z1 < 0.0) { z = z - 1; z1 = fabsf(z1); }
-        x = wrap(x, N); y = wrap(y, N); z = wrap(z, N);
-        if (a == 1) x1 = 1.0 - x1;
-        if (b == 1) y1 = 1.0 - y1;
-        if (c == 1) z1 = 1.0 - z1;
-        map[x * N * N + y * N + z] += (1.0 - x1) * (1.0 - y1) * (1.0 - z1) * v;
-        x -= a; y -= b; z -= c;
-        if (a == 1) x1 = 1.0 - x1;
-        if (b == 1) y1 = 1.0 - y1;
-        if (c == 1) z1 = 1.0 - z1;
-      }
-}
-
-int sf21_halo_rion_box(const char *path, double z, const sf21_stage_params *p, float *out) {
-  typedef struct { float Mass, x, y, z; } halo_t; /* auxiliary.h:13-17 */
+int sf21_read_halos(const char *path, long *nhalos, void **records) {
   FILE *f = fopen(path, "rb");
   if (!f) return 1;
   long nh = 0;
   if (fread(&nh, sizeof(long), 1, f) != 1 || nh < 0) { fclose(f); return 2; }
-  halo_t *h = malloc(sizeof(halo_t) * (size_t)(nh ? nh : 1));
+  void *h = malloc((size_t)16 * (size_t)(nh ? nh : 1));
   if (!h) { fclose(f); return 3; }
-  if (fread(h, sizeof(halo_t), (size_t)nh, f) != (size_t)nh) { free(h); fclose(f); return 2; }
+  if (fread(h, 16, (size_t)nh, f) != (size_t)nh) { free(h); fclose(f); return 2; }
   fclose(f);
-  const long Nh = p->N_halo, Ns = p->N_smooth;
-  if (Ns > Nh) { free(h); return 4; } /* auxiliary.c:651-654 */
-  float *fine = calloc((size_t)(Nh * Nh * Nh), sizeof(float));
-  if (!fine) { free(h); return 3; }
-  for (long i = 0; i < nh; i++) cic(h[i].x, h[i].y, h[i].z, (float)rion_of(h[i].Mass, z), fine, Nh);
-  free(h);
-  long sm = (long)roundf((1.0 * Nh) / Ns);
-  if (Ns * sm > Nh) sm = sm - 1;
-  const double sm3 = 1.0 * sm * sm * sm;
-  for (long i = 0; i < Ns; i++)
-    for (long j = 0; j < Ns; j++)
-      for (long q = 0; q < Ns; q++) {
-        double av = 0.0;
-        for (long a = 0; a < sm; a++)
-          for (long b = 0; b < sm; b++)
-            for (long c = 0; c < sm; c++) av += fine[(i * sm + a) * Nh * Nh + (j * sm + b) * Nh + (q * sm + c)];
-        out[i * Ns * Ns + j * Ns + q] = (float)(av / sm3);
-      }
-  free(fine);
+  *nhalos = nh;
+  *records = h;
   return 0;
 }

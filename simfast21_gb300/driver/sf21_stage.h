@@ -27,11 +27,10 @@ int sf21_read_params(const char *basedir, sf21_stage_params *p);
 int sf21_read_box(const char *path, float *buf, long n);
 int sf21_write_box(const char *path, const float *buf, long n);
 
-/* Halo branch source (get_HIIbubbles.c:229-253): reads the catalogue
- * (long nhalos, then {float Mass,x,y,z} per halo), deposits Rion(M, z) by
- * cloud-in-cell on the N_halo^3 grid in catalogue order (auxiliary.c:761-808)
- * and block-averages to N_smooth^3 (auxiliary.c:643-684).  The result is the
- * box before the *(dx_s/dx_h)^3*fesc of :258, i.e. SF21_SRC_RION input. */
-int sf21_halo_rion_box(const char *path, double z, const sf21_stage_params *p, float *out);
+/* Halo catalogue (Halos/halonl_z*.dat.catalog, output_files.txt:33-41):
+ * long nhalos, then nhalos records {float Mass, x, y, z} (Halo_t,
+ * auxiliary.h:13-17).  *records is malloc'ed (16 B per halo).  The source
+ * box itself is built on the GPU by sf21_hii_run_z_halos. */
+int sf21_read_halos(const char *path, long *nhalos, void **records);
 
 #endif

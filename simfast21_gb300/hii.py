@@ -28,7 +28,8 @@ EXPORTS = [
     "sf21_hii_create", "sf21_hii_destroy", "sf21_hii_last_error", "sf21_hii_run_z",
     "sf21_hii_run_z_device", "sf21_hii_radii", "sf21_hii_prologue", "sf21_hii_filtered",
     "sf21_hii_first_hit", "sf21_hii_run_z_plain_device", "sf21_hii_criterion", "sf21_hii_criterion_device",
-    "sf21_hii_vjp", "sf21_hii_vjp_device", "sf21_hii_path", "sf21_hii_check", "sf21_hii_profile", "sf21_hii_profile_read", "sf21_hii_profile_name",
+    "sf21_hii_vjp", "sf21_hii_vjp_device", "sf21_hii_path", "sf21_hii_check", "sf21_hii_halo_source",
+    "sf21_hii_run_z_halos", "sf21_hii_profile", "sf21_hii_profile_read", "sf21_hii_profile_name",
 ]
 
 
@@ -45,7 +46,8 @@ class _Set(ctypes.Structure):
 class _Config(ctypes.Structure):
     _fields_ = [("N", ctypes.c_long), ("N_halo", ctypes.c_long), ("L", ctypes.c_double),
                 ("hubble", ctypes.c_double), ("device", ctypes.c_int), ("nsets", ctypes.c_int),
-                ("sets", ctypes.POINTER(_Set)), ("kmax", ctypes.c_int), ("path", ctypes.c_int)]
+                ("sets", ctypes.POINTER(_Set)), ("kmax", ctypes.c_int), ("path", ctypes.c_int),
+                ("graph", ctypes.c_int)]
 
 
 _lib = None
@@ -77,6 +79,8 @@ def load_library(path: str = LIB_PATH):
     L.sf21_hii_vjp.argtypes = [vp, ctypes.c_double, ctypes.c_int, fp, fp, ctypes.c_int, fp, fp, fp, dp]
     L.sf21_hii_vjp_device.argtypes = [vp, ctypes.c_double, ctypes.c_int, vp, vp, ctypes.c_int, vp, vp, vp, dp, vp]
     L.sf21_hii_path.argtypes = [vp, dp, ctypes.c_int]
+    L.sf21_hii_halo_source.argtypes = [vp, ctypes.c_double, ctypes.c_long, vp, fp]
+    L.sf21_hii_run_z_halos.argtypes = [vp, ctypes.c_double, fp, ctypes.c_long, vp, fp, dp]
     L.sf21_hii_check.argtypes = [vp]
     L.sf21_hii_profile.argtypes = [vp, ctypes.c_int]
     L.sf21_hii_profile_read.argtypes = [vp, dp, ctypes.POINTER(ctypes.c_long), ctypes.c_int]
@@ -108,7 +112,7 @@ class FilterBank:
     """One GPU context for a box size and a list of parameter sets."""
 
     def __init__(self, N: int, L: float, hubble: float, sets, N_halo: int = 0, device: int = 0,
-                 kmax: int = 0, path: int = 0):
+                 kmax: int = 0, path: int = 0, graph: bool = True):
         self._lib = load_library()
         self.N = int(N)
         self.n3 = self.N ** 3
@@ -116,7 +120,7 @@ class FilterBank:
         arr = (_Set * len(self.sets))(*[_Set(s.fesc, s.Rmax, s.Nbins) for s in self.sets])
         self._arr = arr
         cfg = _Config(N=self.N, N_halo=N_halo or self.N, L=L, hubble=hubble, device=device,
-                      nsets=len(self.sets), sets=arr, kmax=kmax, path=path)
+                      nsets=len(self.sets), sets=arr, kmax=kmax, path=path, graph=0 if graph else -1)
         h = ctypes.c_void_p()
         rc = self._lib.sf21_hii_create(ctypes.byref(cfg), ctypes.byref(h))
         if rc != 0:
@@ -140,10 +144,11 @@ class FilterBank:
 
     def path(self):
         """(pipeline in use: 1 = three axis passes, 2 = plane clusters,
-        3 = TMA-pipelined three passes; {pipeline: tuned ms of one batch})."""
-        ms = (ctypes.c_double * 3)()
-        p = self._lib.sf21_hii_path(self._h, ms, 3)
-        return p, {i + 1: ms[i] for i in range(3)}
+        3 = TMA-pipelined ky pass, 4 = TMA-pipelined ky and kx passes;
+        {pipeline: tuned ms of one batch})."""
+        ms = (ctypes.c_double * 4)()
+        p = self._lib.sf21_hii_path(self._h, ms, 4)
+        return p, {i + 1: ms[i] for i in range(4)}
 
     def check(self):
         """Raise if a bounded device wait expired since the last check."""
@@ -180,6 +185,27 @@ class FilterBank:
         self._check(self._lib.sf21_hii_run_z_plain_device(self._h, z, src_kind, ctypes.c_void_p(delta_ptr),
                                                           ctypes.c_void_p(src_ptr), s, ctypes.c_void_p(xhii_ptr),
                                                           ctypes.c_void_p(stream or None)))
+
+    # ---- halo-catalogue source (use_SFR = F) ---------------------------------
+    def halo_source(self, z: float, catalogue: np.ndarray) -> np.ndarray:
+        """Rion box (CIC + smooth_box, before *(dx_s/dx_h)^3*fesc) from records
+        with fields Mass, x, y, z (float32)."""
+        cat = np.ascontiguousarray(catalogue)
+        assert cat.dtype.itemsize == 16
+        out = np.empty((self.N,) * 3, np.float32)
+        self._check(self._lib.sf21_hii_halo_source(self._h, z, len(cat), cat.ctypes.data_as(ctypes.c_void_p),
+                                                   _ptr(out)))
+        return out
+
+    def run_z_halos(self, z: float, delta, catalogue: np.ndarray):
+        """xHII boxes and neutral fractions from a density box and a halo catalogue."""
+        d = _f32(delta, self.n3)
+        cat = np.ascontiguousarray(catalogue)
+        out = np.empty((len(self.sets), self.N, self.N, self.N), np.float32)
+        neutral = (ctypes.c_double * len(self.sets))()
+        self._check(self._lib.sf21_hii_run_z_halos(self._h, z, _ptr(d), len(cat),
+                                                   cat.ctypes.data_as(ctypes.c_void_p), _ptr(out), neutral))
+        return out, np.array(neutral[:], dtype=np.float64)
 
     # ---- differentiable criterion -------------------------------------------
     def criterion(self, z: float, delta, src, s: int = 0, src_kind: int = SF21_SRC_SFRD):

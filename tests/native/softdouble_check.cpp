@@ -40,7 +40,7 @@ int main(int argc, char** argv) {
   long n = argc > 1 ? atol(argv[1]) : 1000000;
   rng_state = argc > 2 ? strtoull(argv[2], 0, 10) : 88172645463325252ULL;
   Stat sa{"add"}, ss{"sub"}, sm{"mul"}, sdv{"div"}, sq{"sqrt"}, sf{"to_float"},
-      sff{"from_float"}, sp{"pow"}, sp4{"pow4"}, spf{"pow_then_float"};
+      sff{"from_float"}, sp{"pow"}, sp4{"pow4"}, spf{"pow_then_float"}, se{"exp"}, sp3{"pow3"};
   for (long i = 0; i < n; i++) {
     double a = rnd_double(-40, 40, true), b = rnd_double(-40, 40, true);
     if (i % 4 == 1) b = rnd_double(-2, 2, true) + a;  // near-cancellation cases
@@ -62,10 +62,14 @@ int main(int argc, char** argv) {
     acc(sp, sd_pow(d2bits(x), d2bits(y)), d2bits(std::pow(x, y)));
     double x4 = rnd_double(-12, 0, false);
     acc(sp4, sd_pow(d2bits(x4), d2bits(4.0)), d2bits(std::pow(x4, 4.0)));
+    double xe = -rnd_double(-20, 9, false) * 0.68;  // exp over (-696, 0): normal results
+    acc(se, sd_exp(d2bits(xe)), d2bits(std::exp(xe)));
+    double x3 = rnd_double(-8, 8, false);
+    acc(sp3, sd_pow(d2bits(x3), d2bits(3.0)), d2bits(std::pow(x3, 3.0)));
     spf.n++;
     if (f2bits(sd_to_float(sd_pow(d2bits(x), d2bits(y)))) != f2bits((float)std::pow(x, y))) spf.bad++;
   }
-  Stat* all[] = {&sa, &ss, &sm, &sdv, &sq, &sf, &sff, &sp, &sp4, &spf};
+  Stat* all[] = {&sa, &ss, &sm, &sdv, &sq, &sf, &sff, &sp, &sp4, &spf, &se, &sp3};
   for (Stat* s : all) printf("%s %ld %ld %ld\n", s->name, s->n, s->bad, s->maxulp);
   return 0;
 }

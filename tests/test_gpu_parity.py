@@ -171,12 +171,47 @@ def test_radius_pipelines_agree(hii, N, L):
     w = synth.Workload(N=N, L=L, zs=[8.0], zeta=40.0, Rmax=L / 2, factor=1.1, seed=21)
     delta, sfrd = synth.make_boxes(w, 8.0)
     sets = [(40.0, L / 2, w.Nbins), (15.0, L / 5, 20)]
-    banks = {p: hii.FilterBank(N, L, 0.71, sets, path=p) for p in (1, 2, 3)}
+    banks = {p: hii.FilterBank(N, L, 0.71, sets, path=p) for p in (1, 2, 3, 4)}
     ref_x, ref_n = banks[1].run_z(8.0, delta, sfrd)
-    for p in (2, 3):
+    for p in (2, 3, 4):
         assert banks[p].path()[0] == p
         x, n = banks[p].run_z(8.0, delta, sfrd)
         assert np.array_equal(ref_x.view(np.uint32), x.view(np.uint32)), p
         for s in range(len(sets)):
             assert np.array_equal(banks[1].first_hit(8.0, delta, sfrd, s), banks[p].first_hit(8.0, delta, sfrd, s))
     banks[3].check()
+    banks[4].check()
+
+
+def test_halo_source_on_gpu_bit_exact(hii, oracle_lib):
+    """CIC of Rion + smooth_box on the GPU equals the reference's serial loop
+    (get_HIIbubbles.c:233-253) bit for bit; the end-to-end halo branch matches
+    the reference's xHII outside the band."""
+    g, sp = _case("hii_n32_halo.npz")
+    p = oracle_params(oracle_lib, sp)
+    z = float(g["zs"][0])
+    fb = _bank(hii, sp)
+    got = fb.halo_source(z, g["catalogue"])
+    want = oracle_lib.halo_smoothed(p, z, g["catalogue"])
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    x, neutral = fb.run_z_halos(z, g["delta_0"], g["catalogue"])
+    rion = oracle_lib.halo_source(p, z, g["catalogue"])
+    rec0, _, _ = fb.prologue(z, g["delta_0"], want, src_kind=hii.SF21_SRC_RION)
+    radii, _ = P.radii(sp.Rmax, sp.dx, sp.Nbins)
+    b = F.bands(rec0, rion, radii, sp.dx, sp.dk, tol=TOL_BAND)
+    certain = b["ionised_lo"] == b["ionised_hi"]
+    assert np.array_equal(x[0][certain].view(np.uint32), g["xHII_0"][certain].view(np.uint32))
+
+
+def test_halo_source_larger_catalogue(hii, oracle_lib):
+    """64^3 box from a 128^3 CIC grid (smoothing factor 2), many halos per cell."""
+    N, Nh, L = 64, 128, 50.0
+    w = synth.Workload(N=N, L=L, zs=[7.5], zeta=0.5, Rmax=L / 2, factor=1.1, seed=55)
+    g = synth.gaussian_field(N, 55)
+    delta = synth.lognormal_delta(g, 0.8)
+    cat = synth.halo_catalogue(delta, 56, occupancy=0.05, n_halo=Nh)
+    p = oracle_lib.params(N, L, 0.71, L / 2, w.Nbins, 0.5, N_halo=Nh)
+    fb = hii.FilterBank(N, L, 0.71, [(0.5, L / 2, w.Nbins)], N_halo=Nh)
+    got = fb.halo_source(7.5, cat)
+    want = oracle_lib.halo_smoothed(p, 7.5, cat)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))

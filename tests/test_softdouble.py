@@ -30,7 +30,7 @@ def test_basic_ops_bit_exact(checker):
         assert n > 0 and bad == 0, (op, stats[op])
     # pow is correctly rounded; libm pow may misround near ties by 1 ulp,
     # never more, and the float rounding of the prologue hides it.
-    for op in ("pow", "pow4"):
+    for op in ("pow", "pow4", "pow3", "exp"):
         n, bad, maxulp = stats[op]
         assert maxulp <= 1 and bad < n * 0.005, (op, stats[op])
     assert stats["pow_then_float"][1] == 0
