@@ -120,6 +120,23 @@ int sf21_hii_run_z_plain_device(sf21_hii_ctx *ctx, double z, int src_kind, const
  * i.e. the SF21_SRC_RION input.  Replaces the serial loop :233-253. */
 int sf21_hii_halo_source(sf21_hii_ctx *ctx, double z, long nhalos, const void *halos, float *rion_box);
 
+/* Allocation-free form of sf21_hii_halo_source, for callers that may not
+ * allocate device memory when they need the box (a fixed device-memory
+ * budget after start-up, a host pool callback).  No reference counterpart:
+ * the reference builds this box with its serial loop (:233-253).  No context;
+ * device pointers: halos_dev holds nhalos records {float Mass, x, y, z},
+ * rion_box_dev receives N_smoothed^3 floats, bit-identical with
+ * sf21_hii_halo_source.  Its scratch is a fixed 16 MiB array in the
+ * library's device image, so N_halo <= 128 and nhalos <= 16384; larger
+ * requests return SF21_E_UNSUPPORTED before any GPU work (message in
+ * sf21_hii_last_error(NULL)).  The first call on each device (that device
+ * current) looks the array up (cudaGetSymbolAddress); make that first call
+ * before any stream capture.  Calls that overlap on one device share the
+ * array and race: serialise them.  Enqueues on stream (a cudaStream_t, NULL
+ * = legacy default stream) and returns. */
+int sf21_hii_halo_source_noalloc(double z, long N_halo, long N_smoothed, long nhalos, const void *halos_dev,
+                                 float *rion_box_dev, void *stream);
+
 /* One redshift of the halo branch end to end (source box + :215-477); the
  * source box stays on the GPU.  Same outputs as sf21_hii_run_z. */
 int sf21_hii_run_z_halos(sf21_hii_ctx *ctx, double z, const float *delta, long nhalos, const void *halos,

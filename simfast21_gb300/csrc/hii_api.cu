@@ -404,6 +404,11 @@ extern "C" int sf21_hii_destroy(sf21_hii_ctx* ctx) {
   return SF21_OK;
 }
 
+namespace sf21 {
+// Error text of the context-free entry points, read with sf21_hii_last_error(NULL).
+void set_global_error(const char* msg) { g_create_err = msg; }
+}  // namespace sf21
+
 extern "C" const char* sf21_hii_last_error(const sf21_hii_ctx* ctx) {
   return ctx ? ctx->err.c_str() : g_create_err.c_str();
 }

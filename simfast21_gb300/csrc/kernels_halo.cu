@@ -16,7 +16,12 @@
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
+#include <stdio.h>
 #include <string.h>
+
+#include <mutex>
+
+#include "../../include/sf21_hii.h"
 
 #include "sf21_kernels.h"
 #include "softdouble.h"
@@ -190,4 +195,136 @@ cudaError_t launch_halo_source(long nh, const void* halos_dev, double z, long N_
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free variant (sf21_hii_halo_source_noalloc).  Some callers cannot
+// call cudaMalloc at the point where they need the source box: a host
+// application that owns a fixed device-memory budget and forbids allocations
+// after start-up, a caller running between CUDA graph launches that must not
+// change the device heap, or one that calls from inside a memory pool's
+// callbacks.  For them the fine grid, the sort keys/values and CUB's temporary
+// storage live in this fixed file-scope array instead of cudaMalloc'd scratch,
+// which caps the sizes (kNoAllocMaxNHalo, kNoAllocMaxHalos).  One array per
+// device: calls that overlap on the same device (two streams, two threads)
+// share it and race; the caller serialises them.
+constexpr size_t kNoAllocScratchBytes = (size_t)16 << 20;  // 16 MiB
+constexpr long kNoAllocMaxNHalo = 128;                     // fine grid <= 8 MiB
+constexpr long kNoAllocMaxHalos = 16384;                   // 131072 CIC entries, 4 MiB
+constexpr int kNoAllocMaxDevices = 64;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+static std::mutex g_noalloc_mu;
+static void* g_noalloc_ptr[kNoAllocMaxDevices];
+
+// Set-up, once per device with that device current: the device address of
+// the array.  Nothing is allocated (the array belongs to the loaded module).
+static cudaError_t noalloc_scratch(void** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return cudaSuccess;
+}
+
+static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+int halo_source_noalloc(double z, long N_halo, long N_smooth, long nh, const void* halos_dev, float* out,
+                        cudaStream_t st, char* err, size_t errlen) {
+  if (nh < 0 || (nh > 0 && !halos_dev) || !out || N_smooth < 1 || N_halo < 1) {
+    snprintf(err, errlen, "bad arguments");
+    return SF21_E_ARG;
+  }
+  if (N_halo < N_smooth) {
+    snprintf(err, errlen, "N_halo < N_smoothed (smooth_box, auxiliary.c:651-654)");
+    return SF21_E_ARG;
+  }
+  if (N_halo > kNoAllocMaxNHalo || nh > kNoAllocMaxHalos) {
+    snprintf(err, errlen, "no-alloc halo source limited to N_halo <= %ld and <= %ld halos (got N_halo %ld, %ld halos)",
+             kNoAllocMaxNHalo, kNoAllocMaxHalos, N_halo, nh);
+    return SF21_E_UNSUPPORTED;
+  }
+  const long ne = 8 * nh;
+  const long Nh3 = N_halo * N_halo * N_halo;
+  size_t sort_tmp = 0;
+  if (ne > 0)
+    cub::DeviceRadixSort::SortPairs(nullptr, sort_tmp, (unsigned long long*)nullptr, (unsigned long long*)nullptr,
+                                    (uint32_t*)nullptr, (uint32_t*)nullptr, (int)ne);
+  // layout: fine | k0 | k1 | s0 | s1 | vals | CUB temp, each 256-byte aligned
+  const size_t o_k0 = align256(sizeof(float) * Nh3);
+  const size_t o_k1 = o_k0 + align256(ne * sizeof(unsigned long long));
+  const size_t o_s0 = o_k1 + align256(ne * sizeof(unsigned long long));
+  const size_t o_s1 = o_s0 + align256(ne * sizeof(uint32_t));
+  const size_t o_v = o_s1 + align256(ne * sizeof(uint32_t));
+  const size_t o_t = o_v + align256(ne * sizeof(sd_t));
+  if (o_t + sort_tmp > kNoAllocScratchBytes) {
+    snprintf(err, errlen, "no-alloc halo source needs %zu scratch bytes, has %zu", o_t + sort_tmp,
+             kNoAllocScratchBytes);
+    return SF21_E_UNSUPPORTED;
+  }
+  void* base = nullptr;
+  cudaError_t e = noalloc_scratch(&base);
+  if (e != cudaSuccess) {
+    snprintf(err, errlen, "scratch set-up failed: %s", cudaGetErrorString(e));
+    return SF21_E_CUDA;
+  }
+  unsigned char* p = (unsigned char*)base;
+  float* fine = (float*)p;
+  RionConst rk;
+  rk.c1 = bits_of(1.575e39);
+  rk.c2 = bits_of(9.367608e+07);
+  rk.c3 = bits_of(0.44);
+  rk.three = bits_of(3.0);
+  rk.vnorm = bits_of(1.e+45);
+  rk.p1 = bits_of(pow((1.0 + z), 2.27044695e+00));
+  // The fine grid is the only part that must start at zero (the CIC chains
+  // write each touched cell once, untouched cells stay 0); keys, sequence
+  // numbers and values are written in full before they are read, and CUB
+  // initialises its own temporary storage.
+  if ((e = cudaMemsetAsync(fine, 0, sizeof(float) * Nh3, st)) == cudaSuccess && nh > 0) {
+    unsigned long long* k0 = (unsigned long long*)(p + o_k0);
+    unsigned long long* k1 = (unsigned long long*)(p + o_k1);
+    uint32_t* s0 = (uint32_t*)(p + o_s0);
+    uint32_t* s1 = (uint32_t*)(p + o_s1);
+    sd_t* vals = (sd_t*)(p + o_v);
+    k_halo_contrib<<<grid_for(nh), 256, 0, st>>>(nh, (const HaloRec*)halos_dev, rk, N_halo, k0, s0, vals);
+    e = cudaGetLastError();
+    int end_bit = 1;
+    while (end_bit < 64 && ((unsigned long long)1 << end_bit) < (unsigned long long)Nh3) ++end_bit;
+    if (e == cudaSuccess) e = cub::DeviceRadixSort::SortPairs(p + o_t, sort_tmp, k0, k1, s0, s1, (int)ne, 0, end_bit, st);
+    if (e == cudaSuccess) {
+      k_halo_accumulate<<<grid_for(ne), 256, 0, st>>>(ne, k1, s1, vals, fine);
+      e = cudaGetLastError();
+    }
+  }
+  if (e == cudaSuccess) {
+    long sm = (long)roundf((float)((1.0 * N_halo) / N_smooth));
+    if (N_smooth * sm > N_halo) sm = sm - 1;
+    k_smooth_box<<<grid_for(N_smooth * N_smooth * N_smooth), 256, 0, st>>>(fine, out, N_halo, N_smooth, sm,
+                                                                           bits_of(1.0 * sm * sm * sm));
+    e = cudaGetLastError();
+  }
+  if (e != cudaSuccess) {
+    snprintf(err, errlen, "no-alloc halo source: %s", cudaGetErrorString(e));
+    return SF21_E_CUDA;
+  }
+  return SF21_OK;
+}
+
 }  // namespace sf21
+
+// Context-free, allocation-free halo source box (declared in sf21_hii.h).
+extern "C" int sf21_hii_halo_source_noalloc(double z, long N_halo, long N_smoothed, long nhalos,
+                                            const void* halos_dev, float* rion_box_dev, void* stream) {
+  char err[256] = {0};
+  const int rc = sf21::halo_source_noalloc(z, N_halo, N_smoothed, nhalos, halos_dev, rion_box_dev,
+                                           (cudaStream_t)stream, err, sizeof err);
+  if (rc != SF21_OK) sf21::set_global_error(err);
+  return rc;
+}

@@ -94,6 +94,12 @@ cudaError_t launch_crit_finalize(long n3, float* C, const uint8_t* A, cudaStream
 size_t halo_scratch_bytes(long nh);
 cudaError_t launch_halo_source(long nh, const void* halos_dev, double z, long N_halo, long N_smooth, float* fine,
                                float* out, void* scratch, size_t scratch_bytes, cudaStream_t st);
+// The same with its scratch in a fixed static device array (no allocation);
+// returns an SF21_* status and writes a message into err on failure.
+int halo_source_noalloc(double z, long N_halo, long N_smooth, long nh, const void* halos_dev, float* out,
+                        cudaStream_t st, char* err, size_t errlen);
+// Error text of the context-free entry points (hii_api.cu).
+void set_global_error(const char* msg);
 
 // Plain form (kernels_plain.cu).
 cudaError_t launch_plain_centres(long n3, const float2* box, const float* alpha, float zmul, float* mask, int* flag,

@@ -30,6 +30,7 @@ EXPORTS = [
     "sf21_hii_first_hit", "sf21_hii_run_z_plain_device", "sf21_hii_criterion", "sf21_hii_criterion_device",
     "sf21_hii_vjp", "sf21_hii_vjp_device", "sf21_hii_path", "sf21_hii_check", "sf21_hii_halo_source",
     "sf21_hii_run_z_halos", "sf21_hii_profile", "sf21_hii_profile_read", "sf21_hii_profile_name",
+    "sf21_hii_halo_source_noalloc",
 ]
 
 
@@ -81,6 +82,8 @@ def load_library(path: str = LIB_PATH):
     L.sf21_hii_path.argtypes = [vp, dp, ctypes.c_int]
     L.sf21_hii_halo_source.argtypes = [vp, ctypes.c_double, ctypes.c_long, vp, fp]
     L.sf21_hii_run_z_halos.argtypes = [vp, ctypes.c_double, fp, ctypes.c_long, vp, fp, dp]
+    L.sf21_hii_halo_source_noalloc.argtypes = [ctypes.c_double, ctypes.c_long, ctypes.c_long, ctypes.c_long,
+                                               vp, vp, vp]
     L.sf21_hii_check.argtypes = [vp]
     L.sf21_hii_profile.argtypes = [vp, ctypes.c_int]
     L.sf21_hii_profile_read.argtypes = [vp, dp, ctypes.POINTER(ctypes.c_long), ctypes.c_int]
@@ -99,6 +102,17 @@ def _f32(a, n3):
     if a.size != n3:
         raise ValueError(f"box has {a.size} elements, expected {n3}")
     return a
+
+
+def halo_source_noalloc(z: float, N_halo: int, N_smoothed: int, nhalos: int, halos_ptr: int, out_ptr: int,
+                        stream: int = 0) -> None:
+    """Halo source box with no device allocation (device pointers; enqueues on
+    stream).  Limited to N_halo <= 128 and nhalos <= 16384."""
+    L = load_library()
+    rc = L.sf21_hii_halo_source_noalloc(z, N_halo, N_smoothed, nhalos, ctypes.c_void_p(halos_ptr or None),
+                                        ctypes.c_void_p(out_ptr or None), ctypes.c_void_p(stream or None))
+    if rc != 0:
+        raise HIIError(rc, L.sf21_hii_last_error(None).decode())
 
 
 @dataclass
