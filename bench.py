@@ -189,7 +189,68 @@ def run_reference(args, w, rank):
     }))
 
 
+# radius pipelines of the library (FilterBank.path): short and long names
+PIPELINES = {
+    1: ("three_pass", "three axis passes"),
+    2: ("plane", "cluster plane pass + kx pass"),
+    3: ("tma_ky", "three axis passes, ky pass TMA-pipelined"),
+    4: ("tma_ky_kx", "three axis passes, ky and kx passes TMA-pipelined"),
+    5: ("cb_three_pass", "column-block-major work boxes, three axis passes"),
+    6: ("cb_tma_ky", "column-block-major work boxes, ky pass TMA-pipelined"),
+    7: ("cb_tma_ky_kx", "column-block-major work boxes, ky and kx passes TMA-pipelined"),
+}
+
+
 # ---------------------------------------------------------------------------
+def grad_metrics(N, L, z, zeta, rmax, factor, seed, stream, dev, kmax=0):
+    """Forward criterion and VJP times (CUDA events on the launch stream) and
+    device memory held by the context during them."""
+    import torch
+    from simfast21_gb300 import hii
+    free0, _ = torch.cuda.mem_get_info()
+    delta, sfrd = synth.make_boxes_torch(N, L, z, seed, device="cuda")
+    nb = max(1, int(round(math.log(rmax / (L / N)) / math.log(factor))))
+    fb = hii.FilterBank(N, L, 0.71, [(zeta, rmax, nb)], device=dev, kmax=kmax)
+    C = torch.empty_like(delta)
+    A = torch.empty(delta.shape, dtype=torch.uint8, device="cuda")
+    g = torch.rand(delta.shape, device="cuda", dtype=torch.float32)
+    gd = torch.empty_like(delta)
+    gs = torch.empty_like(delta)
+    sptr = stream.cuda_stream
+
+    def fwd():
+        fb.criterion_device(z, delta.data_ptr(), sfrd.data_ptr(), C.data_ptr(), A.data_ptr(), stream=sptr)
+
+    def bwd():
+        fb.vjp_device(z, delta.data_ptr(), sfrd.data_ptr(), g.data_ptr(), gd.data_ptr(), gs.data_ptr(),
+                      stream=sptr, want_zeta=False)
+
+    fwd()
+    bwd()
+    torch.cuda.synchronize()
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    reps = 2
+    e[0].record(stream)
+    for _ in range(reps):
+        fwd()
+    e[1].record(stream)
+    for _ in range(reps):
+        bwd()
+    e[2].record(stream)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    fms = e[0].elapsed_time(e[1]) / reps
+    bms = e[1].elapsed_time(e[2]) / reps
+    nr = len(fb.radii(0)[0])
+    nf = fb.radii(0)[1]
+    fb.close()
+    del delta, sfrd, C, A, g, gd, gs
+    torch.cuda.empty_cache()
+    return {"N": N, "radii_fft_branch": nf, "radii": nr, "fwd_ms": fms, "bwd_ms": bms, "bwd_over_fwd": bms / fms,
+            "device_bytes_in_use": int(free0 - free1),
+            "checkpoint": "uint8 argmax radius per voxel; filtered fields recomputed"}
+
+
 def run_ours(args, w, rank, world):
     import torch
     from simfast21_gb300 import build as B
@@ -296,6 +357,17 @@ def run_ours(args, w, rank, world):
              "batched_per_set_speedup": (value / world) / (plain_units / (plain_ms / 1e3))}
     del d_plain
 
+    # differentiation: criterion forward and hand-written VJP (bwd/fwd),
+    # 256^3 (L=200, z=8, zeta=30, Rmax=60, factor 1.05) and, with --grad-large,
+    # 1024^3 (L=500, z=7, Rmax=80, factor 1.12) with peak HBM
+    grad = None
+    if not args.no_grad:
+        del d_x
+        torch.cuda.synchronize()
+        grad = {"box256": grad_metrics(256, 200.0, 8.0, 30.0, 60.0, 1.05, 4321, stream, dev)}
+        if args.grad_large:
+            grad["box1024"] = grad_metrics(1024, 500.0, 7.0, 30.0, 80.0, 1.12, 5555, stream, dev, kmax=4)
+
     # CPU baseline (rank 0 only)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -315,11 +387,8 @@ def run_ours(args, w, rank, world):
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded lognormal density + SFRD boxes)",
             "config": {"workload": describe(w), "N": N, "sets": nsets, "radii_total": R_total,
-                       "pipeline": {1: "three axis passes", 2: "cluster plane pass + kx pass",
-                                    3: "three axis passes, ky pass TMA-pipelined",
-                                    4: "three axis passes, ky and kx passes TMA-pipelined"}[path],
-                       "tuned_batch_ms": {"three_pass": tuned[1], "plane": tuned[2], "tma_ky": tuned[3],
-                                          "tma_ky_kx": tuned[4]},
+                       "pipeline": PIPELINES[path][1],
+                       "tuned_batch_ms": {PIPELINES[p][0]: tuned[p] for p in PIPELINES},
                        "flush": "inputs larger than L2 (every box >= 537 MB)"},
             "e2e": {"value": e2e_val, "unit": "voxel*radii/s",
                     "h2d_bytes_per_step": 2 * 4 * n3, "d2h_bytes_per_step": nsets * 4 * n3},
@@ -332,6 +401,7 @@ def run_ours(args, w, rank, world):
             "kernels_ms_per_step": {k: round(v[0] / steps, 3) for k, v in kinds.items()},
             "clocks": clk.summary(),
             "plain_gpu": plain,
+            "differentiation": grad,
             "cpu_baseline": cpu,
         }
         print(json.dumps(out))
@@ -346,8 +416,10 @@ def main():
     ap.add_argument("--workload", default="batched512")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--kmax", type=int, default=0, help="radii per spectrum read (0 = library default)")
+    ap.add_argument("--no-grad", action="store_true", help="skip the bwd/fwd measurement")
+    ap.add_argument("--grad-large", action="store_true", help="also time fwd+bwd at 1024^3 (peak HBM)")
     ap.add_argument("--path", type=int, default=0,
-                    help="radius pipeline: 0 = tuned, 1 = three axis passes, 2 = cluster plane pass")
+                    help="radius pipeline: 0 = tuned, else one of PIPELINES")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -20,7 +20,7 @@ LIB = os.path.join(HERE, "libsf21hii.so")
 DRIVER = os.path.join(HERE, "sf21_hii")
 DRIVER_SRC = [os.path.join(HERE, "driver", f) for f in ("sf21_hii_main.c", "sf21_stage.c")]
 SOURCES = ["kernels_fft.cu", "kernels_plane.cu", "kernels_pipe.cu", "kernels_adj.cu", "kernels_elem.cu",
-           "kernels_plain.cu", "kernels_halo.cu", "hii_api.cu"]
+           "kernels_plain.cu", "kernels_halo.cu", "kernels_cb.cu", "kernels_dt.cu", "hii_api.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3"]
 

@@ -60,6 +60,11 @@ struct SetInfo {
 
 }  // namespace
 
+// Radius pipelines: 1 three axis passes, 2 plane clusters + kx pass,
+// 3 TMA ky + kx pass, 4 TMA ky + TMA kx, and over column-block-major work
+// boxes: 5 three axis passes, 6 TMA ky + kx pass, 7 TMA ky + TMA kx.
+constexpr int NPATH = 7;
+
 struct sf21_hii_ctx {
   int device = 0;
   long N = 0, N_halo = 0, n3 = 0;
@@ -68,7 +73,7 @@ struct sf21_hii_ctx {
   int path = 1;             // 1 = three axis passes, 2 = plane clusters + kx pass,
                             // 3 = three axis passes, ky pass TMA-pipelined,
                             // 4 = three axis passes, ky and kx passes TMA-pipelined
-  double tune_ms[5] = {0, 0, 0, 0, 0};
+  double tune_ms[NPATH + 1] = {};
   float2* d_work_base = nullptr;  // K consecutive work boxes
   // CUDA graph of the per-redshift schedule of run_z_device (replayed while
   // z, the source kind, the buffers and the stream stay the same)
@@ -86,6 +91,8 @@ struct sf21_hii_ctx {
   std::vector<SetInfo> sets;
   cudaStream_t stream = nullptr;
   float *d_delta = nullptr, *d_src = nullptr, *d_rec0 = nullptr, *d_fres = nullptr;
+  uint64_t* d_chain = nullptr;  // source chain before zeta (double bits), per redshift
+  float2* d_om = nullptr;       // 1 - fresid rounded down / to nearest, per redshift
   float *d_partials = nullptr, *d_alpha = nullptr, *d_xhii = nullptr;
   // criterion / adjoint buffers (allocated on first use)
   float* d_C = nullptr;
@@ -123,11 +130,12 @@ struct sf21_hii_ctx {
 
 // Kernel kinds reported by sf21_hii_profile_read, in this order.
 static const char* kKindNames[] = {"prologue", "alpha", "fwd_rows", "fwd_cols_b", "fwd_cols_a",
-                                   "inv_rows_filter", "inv_cols_b", "inv_cols_a_test", "dt_rows",
-                                   "dt_b", "dt_a_finish", "inv_plane_filter", "crit_cols_a",
-                                   "adj_cols_a", "adj_cols_b_fwd", "adj_rows_acc", "adj_final"};
+                                   "inv_rows_filter", "inv_cols_b", "inv_cols_a_test", "dt_a",
+                                   "dt_b", "dt_c_finish", "inv_plane_filter", "crit_cols_a",
+                                   "adj_cols_a", "adj_cols_b_fwd", "adj_rows_acc", "adj_final",
+                                   "finish_prep"};
 enum { KD_PRO, KD_ALPHA, KD_FROWS, KD_FCB, KD_FCA, KD_IROWS, KD_ICB, KD_ICA, KD_DTR, KD_DTB, KD_DTA, KD_PLANE,
-       KD_CRIT, KD_ADJA, KD_ADJB, KD_ADJR, KD_ADJF, KD_COUNT };
+       KD_CRIT, KD_ADJA, KD_ADJB, KD_ADJR, KD_ADJF, KD_PREP, KD_COUNT };
 
 // Records an event on st when timing is on; returns its index (or -1).
 static int mark(sf21_hii_ctx* c, cudaStream_t st) {
@@ -198,7 +206,7 @@ static void free_ctx(sf21_hii_ctx* c) {
   void* ptrs[] = {c->d_delta, c->d_src, c->d_rec0, c->d_fres, c->d_partials, c->d_alpha,
                   c->d_xhii, c->d_spec, c->d_tw, c->d_rc, c->d_mask, c->d_flag, c->d_box2,
                   c->d_C, c->d_A, c->d_acc, c->d_zpart, c->d_g, c->d_gd, c->d_gs, c->d_halos, c->d_fine,
-                  c->d_hscratch};
+                  c->d_hscratch, c->d_chain, c->d_om};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->d_work_base) cudaFree(c->d_work_base);
@@ -301,12 +309,15 @@ extern "C" int sf21_hii_create(const sf21_hii_config* cfg, sf21_hii_ctx** out) {
   CREATE_CUDA(cudaSetDevice(c->device));
   CREATE_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
   CREATE_CUDA(fft_setup((int)N));
-  CREATE_CUDA(dilate_setup((int)N));
+  CREATE_CUDA(dt_setup((int)N));
+  CREATE_CUDA(cb_setup((int)N));
   CREATE_CUDA(adj_setup((int)N));
   CREATE_CUDA(cudaMalloc(&c->d_delta, box_f));
   CREATE_CUDA(cudaMalloc(&c->d_src, box_f));
   CREATE_CUDA(cudaMalloc(&c->d_rec0, box_f));
   CREATE_CUDA(cudaMalloc(&c->d_fres, box_f));
+  CREATE_CUDA(cudaMalloc(&c->d_chain, sizeof(uint64_t) * c->n3));
+  CREATE_CUDA(cudaMalloc(&c->d_om, sizeof(float2) * c->n3));
   CREATE_CUDA(cudaMalloc(&c->d_xhii, box_f));
   CREATE_CUDA(cudaMalloc(&c->d_spec, box_c));
   CREATE_CUDA(cudaMalloc(&c->d_rc, c->n3));
@@ -341,7 +352,8 @@ extern "C" int sf21_hii_create(const sf21_hii_config* cfg, sf21_hii_ctx** out) {
     can_pipe = true;
   cudaGetLastError();
   const int want = cfg->path;
-  if ((want == 2 && !can_plane) || (want >= 3 && !can_pipe) || want < 0 || want > 4) {
+  if ((want == 2 && !can_plane) || ((want == 3 || want == 4 || want == 6 || want == 7) && !can_pipe) ||
+      want < 0 || want > NPATH) {
     g_create_err = "requested radius pipeline not available for this box on this device";
     free_ctx(c);
     return SF21_E_UNSUPPORTED;
@@ -362,9 +374,10 @@ extern "C" int sf21_hii_create(const sf21_hii_config* cfg, sf21_hii_ctx** out) {
     cudaEvent_t t0, t1;
     CREATE_CUDA(cudaEventCreate(&t0));
     CREATE_CUDA(cudaEventCreate(&t1));
-    double best[5] = {1e30, 1e30, 1e30, 1e30, 1e30};
-    for (int p = 1; p <= 4; ++p) {
-      if ((p == 2 && !can_plane) || (p >= 3 && !can_pipe)) continue;
+    double best[NPATH + 1];
+    for (int p = 0; p <= NPATH; ++p) best[p] = 1e30;
+    for (int p = 1; p <= NPATH; ++p) {
+      if ((p == 2 && !can_plane) || ((p == 3 || p == 4 || p == 6 || p == 7) && !can_pipe)) continue;
       c->path = p;
       for (int rep = 0; rep < 4; ++rep) {
         CREATE_CUDA(cudaEventRecord(t0, c->stream));
@@ -391,7 +404,7 @@ extern "C" int sf21_hii_create(const sf21_hii_config* cfg, sf21_hii_ctx** out) {
       return SF21_E_TIMEOUT;
     }
     c->path = 1;
-    for (int p = 2; p <= 4; ++p)
+    for (int p = 2; p <= NPATH; ++p)
       if (best[p] < best[c->path]) c->path = p;
   }
 #undef CREATE_CUDA
@@ -442,6 +455,9 @@ static int enqueue_front(sf21_hii_ctx* c, double z, int kind, const float* delta
   int e4 = mark(c, st);
   CTX_CUDA(c, launch_cols(N, c->d_spec, none, 1, 0, false, c->d_tw, st));
   int e5 = mark(c, st);
+  CTX_CUDA(c, launch_finish_prep(c->n3, src, c->d_fres, c->pa, c->d_chain, c->d_om, st));
+  int e6 = mark(c, st);
+  span(c, KD_PREP, e5, e6);
   span(c, KD_PRO, e0, e1);
   span(c, KD_ALPHA, e1, e2);
   span(c, KD_FROWS, e2, e3);
@@ -463,14 +479,37 @@ static int enqueue_batch(sf21_hii_ctx* c, const Batch& bt, cudaStream_t st) {
     span(c, KD_ICA, e1, e2);
     return SF21_OK;
   }
+  if (c->path >= 5) {  // column-block-major work boxes
+    int e0 = mark(c, st);
+    CTX_CUDA(c, launch_rows_filter_cb(N, c->d_spec, bt, c->d_tw, st));
+    int e1 = mark(c, st);
+    if (c->path == 5)
+      CTX_CUDA(c, launch_cols_b_cb(N, bt, c->d_tw, st));
+    else
+      CTX_CUDA(c, launch_pipe(N, 0, 1, c->pmaps, bt, c->d_work_base, c->d_rc, c->d_alpha, c->d_tw, c->d_err,
+                              c->nsm, st));
+    int e2 = mark(c, st);
+    if (c->path == 7)
+      CTX_CUDA(c, launch_pipe(N, 1, 1, c->pmaps, bt, c->d_work_base, c->d_rc, c->d_alpha, c->d_tw, c->d_err,
+                              c->nsm, st));
+    else
+      CTX_CUDA(c, launch_cols_a_test_cb(N, bt, c->d_rc, c->d_alpha, c->d_tw, st));
+    int e3 = mark(c, st);
+    span(c, KD_IROWS, e0, e1);
+    span(c, KD_ICB, e1, e2);
+    span(c, KD_ICA, e2, e3);
+    return SF21_OK;
+  }
   if (c->path == 3 || c->path == 4) {
     int e0 = mark(c, st);
     CTX_CUDA(c, launch_inv_rows_filter(N, c->d_spec, bt, c->d_tw, st));
     int e1 = mark(c, st);
-    CTX_CUDA(c, launch_pipe(N, 0, c->pmaps, bt, c->d_work_base, c->d_rc, c->d_alpha, c->d_tw, c->d_err, c->nsm, st));
+    CTX_CUDA(c, launch_pipe(N, 0, 0, c->pmaps, bt, c->d_work_base, c->d_rc, c->d_alpha, c->d_tw, c->d_err, c->nsm,
+                            st));
     int e2 = mark(c, st);
     if (c->path == 4)
-      CTX_CUDA(c, launch_pipe(N, 1, c->pmaps, bt, c->d_work_base, c->d_rc, c->d_alpha, c->d_tw, c->d_err, c->nsm, st));
+      CTX_CUDA(c, launch_pipe(N, 1, 0, c->pmaps, bt, c->d_work_base, c->d_rc, c->d_alpha, c->d_tw, c->d_err,
+                              c->nsm, st));
     else
       CTX_CUDA(c, launch_cols_a_test(N, bt, c->d_rc, c->d_alpha, c->d_tw, st));
     int e3 = mark(c, st);
@@ -513,17 +552,19 @@ static int enqueue_radii(sf21_hii_ctx* c, int set, cudaStream_t st) {
   return SF21_OK;
 }
 
-static int enqueue_finish(sf21_hii_ctx* c, int set, const float* src, float* xhii, cudaStream_t st) {
+// Dilation + finish of one set; the per-voxel inputs (rec0, chain, om) are
+// those of the last enqueue_front.
+static int enqueue_finish(sf21_hii_ctx* c, int set, float* xhii, cudaStream_t st) {
   const SetInfo& s = c->sets[set];
   const int N = (int)c->N;
   int* dt0 = reinterpret_cast<int*>(c->d_work[0]);
   int* dt1 = dt0 + c->n3;
   int e0 = mark(c, st);
-  CTX_CUDA(c, launch_dt_rows(N, c->d_rc, s.d_nmax, s.vmax, dt0, st));
+  CTX_CUDA(c, launch_dt_pa(N, c->d_rc, s.d_nmax, dt0, st));
   int e1 = mark(c, st);
-  CTX_CUDA(c, launch_dt_b(N, dt0, s.vmax, dt1, st));
+  CTX_CUDA(c, launch_dt_pb(N, dt0, dt1, st));
   int e2 = mark(c, st);
-  CTX_CUDA(c, launch_dt_a_finish(N, dt1, s.vmax, dbits(s.fesc), src, c->d_rec0, c->d_fres, c->pa, xhii, st));
+  CTX_CUDA(c, launch_dt_pc_finish(N, dt1, dbits(s.fesc), c->d_chain, c->d_rec0, c->d_om, xhii, st));
   int e3 = mark(c, st);
   span(c, KD_DTR, e0, e1);
   span(c, KD_DTB, e1, e2);
@@ -544,7 +585,7 @@ static int enqueue_run(sf21_hii_ctx* c, double z, int kind, const float* delta_d
   if ((rc = enqueue_front(c, z, kind, delta_dev, src_dev, st))) return rc;
   for (int s = 0; s < (int)c->sets.size(); ++s) {
     if ((rc = enqueue_radii(c, s, st))) return rc;
-    if ((rc = enqueue_finish(c, s, src_dev, xhii_dev + (size_t)s * c->n3, st))) return rc;
+    if ((rc = enqueue_finish(c, s, xhii_dev + (size_t)s * c->n3, st))) return rc;
   }
   return SF21_OK;
 }
@@ -612,7 +653,7 @@ extern "C" int sf21_hii_run_z(sf21_hii_ctx* c, double z, int kind, const float* 
   int status = SF21_OK;
   for (int s = 0; s < (int)c->sets.size() && status == SF21_OK; ++s) {
     if ((status = enqueue_radii(c, s, st))) break;
-    if ((status = enqueue_finish(c, s, c->d_src, c->d_xhii, st))) break;
+    if ((status = enqueue_finish(c, s, c->d_xhii, st))) break;
     float* dst = xhii + (size_t)s * c->n3;
     cudaError_t e = cudaMemcpyAsync(dst, c->d_xhii, bf, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -796,7 +837,7 @@ extern "C" int sf21_hii_run_z_plain_device(sf21_hii_ctx* c, double z, int kind, 
 
 extern "C" int sf21_hii_path(const sf21_hii_ctx* c, double* ms_tuned, int cap) {
   if (!c) return -SF21_E_ARG;
-  for (int p = 1; p <= 4 && p <= cap; ++p) ms_tuned[p - 1] = c->tune_ms[p] < 1e29 ? c->tune_ms[p] : 0.0;
+  for (int p = 1; p <= NPATH && p <= cap; ++p) ms_tuned[p - 1] = c->tune_ms[p] < 1e29 ? c->tune_ms[p] : 0.0;
   return c->path;
 }
 
@@ -1039,7 +1080,7 @@ extern "C" int sf21_hii_run_z_halos(sf21_hii_ctx* c, double z, const float* delt
   int status = SF21_OK;
   for (int s = 0; s < (int)c->sets.size() && status == SF21_OK; ++s) {
     if ((status = enqueue_radii(c, s, st))) break;
-    if ((status = enqueue_finish(c, s, c->d_src, c->d_xhii, st))) break;
+    if ((status = enqueue_finish(c, s, c->d_xhii, st))) break;
     float* dst = xhii + (size_t)s * c->n3;
     cudaError_t e = cudaMemcpyAsync(dst, c->d_xhii, bf, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);

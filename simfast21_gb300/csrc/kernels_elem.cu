@@ -1,9 +1,9 @@
-// Element-wise and stencil kernels of the HII stage: the prologue
+// Element-wise kernels of the HII stage: the prologue
 // (get_HIIbubbles.c:216-225, 272-274), the norm balance of the packed
-// transform, and the per-set finish: dilation of the bubble centres, the
-// single-cell fill (:281-288) and the cap by the residual neutral fraction
-// (:469-471).  All per-voxel double arithmetic of the reference is
-// reproduced bit for bit with the integer soft-double routines.
+// transform and the single-cell fill check hook (:281-288).  All per-voxel
+// double arithmetic of the reference is reproduced bit for bit with the
+// integer soft-double routines.  The dilation and the per-set finish are in
+// kernels_dt.cu.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -135,122 +135,6 @@ cudaError_t launch_alpha(const float* partials, int nblocks, float* alpha, cudaS
   return cudaGetLastError();
 }
 
-// ---------------------------------------------------------------------------
-// Dilation.  A voxel y is ionised by the radius loops iff some centre x with
-// first-hit radius R_c(x) lies within the discrete ball of that radius:
-// n(x, y) <= nmax(R_c(x)), n = squared per-axis minimum-image lattice
-// distance (the sphere window of get_HIIbubbles.c:366 and the painting of
-// :440-448).  Balls of smaller radii nest, so only the first (largest) hit
-// matters.  With v(x) = nmax(R_c(x)) (-1 for no centre) the test is
-//   max_x [v(x) - n(x, y)] >= 0,
-// separable into three 1D max-plus passes with the kernel -d^2.  Values below
-// zero can never come back to >= 0, so they are clamped to -1.
-constexpr int DT_ROW_THREADS = 256;
-
-__device__ __forceinline__ int dt_window(int vmax, int N) {
-  int w = (int)sqrtf((float)vmax);
-  while ((w + 1) * (w + 1) <= vmax) ++w;
-  while (w * w > vmax) --w;
-  return w < N / 2 ? w : N / 2;
-}
-
-// pass along c (contiguous): one row per CTA iteration, input from rc.
-__global__ void __launch_bounds__(DT_ROW_THREADS)
-k_dt_rows(int N, const uint8_t* __restrict__ rc, const int* __restrict__ nmax, int vmax,
-          int* __restrict__ out) {
-  extern __shared__ int srow[];
-  const long row = blockIdx.x;
-  const uint8_t* in = rc + row * N;
-  for (int c = threadIdx.x; c < N; c += blockDim.x) {
-    const uint8_t h = in[c];
-    srow[c] = (h == RC_NONE) ? -1 : nmax[h];
-  }
-  __syncthreads();
-  const int W = dt_window(vmax, N);
-  for (int y = threadIdx.x; y < N; y += blockDim.x) {
-    int best = srow[y];
-    for (int d = 1; d <= W; ++d) {
-      const int dd = d * d;
-      int u = srow[(y + d) & (N - 1)] - dd;
-      int w = srow[(y - d) & (N - 1)] - dd;
-      best = max(best, max(u, w));
-    }
-    out[row * N + y] = best < -1 ? -1 : best;
-  }
-}
-
-// pass along b (stride N): tile N x CW for fixed a.
-constexpr int DT_CW = 16;
-__global__ void k_dt_b(int N, const int* __restrict__ in, int vmax, int* __restrict__ out) {
-  extern __shared__ int stile[];  // [N][DT_CW]
-  const int nblk = N / DT_CW;
-  const long a = blockIdx.x / nblk;
-  const int c0 = (blockIdx.x % nblk) * DT_CW;
-  const long base = a * N * N + c0;
-  for (int t = threadIdx.x; t < N * DT_CW; t += blockDim.x) {
-    const int b = t / DT_CW, c = t % DT_CW;
-    stile[t] = in[base + (long)b * N + c];
-  }
-  __syncthreads();
-  const int W = dt_window(vmax, N);
-  for (int t = threadIdx.x; t < N * DT_CW; t += blockDim.x) {
-    const int b = t / DT_CW, c = t % DT_CW;
-    int best = stile[t];
-    for (int d = 1; d <= W; ++d) {
-      const int dd = d * d;
-      best = max(best, max(stile[((b + d) & (N - 1)) * DT_CW + c] - dd,
-                           stile[((b - d) & (N - 1)) * DT_CW + c] - dd));
-    }
-    out[base + (long)b * N + c] = best < -1 ? -1 : best;
-  }
-}
-
-// pass along a (stride N^2) fused with the finish of the xHII box.
-__global__ void k_dt_a_finish(int N, const int* __restrict__ in, int vmax, sd_t zeta,
-                              const float* __restrict__ src, const float* __restrict__ rec0,
-                              const float* __restrict__ fres, const PrologueArgs pa,
-                              float* __restrict__ xhii) {
-  extern __shared__ int stile[];  // [N][DT_CW]
-  const int nblk = N / DT_CW;
-  const long b = blockIdx.x / nblk;
-  const int c0 = (blockIdx.x % nblk) * DT_CW;
-  const long base = b * N + c0;
-  const long stride = (long)N * N;
-  for (int t = threadIdx.x; t < N * DT_CW; t += blockDim.x) {
-    const int a = t / DT_CW, c = t % DT_CW;
-    stile[t] = in[base + (long)a * stride + c];
-  }
-  __syncthreads();
-  const int W = dt_window(vmax, N);
-  for (int t = threadIdx.x; t < N * DT_CW; t += blockDim.x) {
-    const int a = t / DT_CW, c = t % DT_CW;
-    int best = stile[t];
-    for (int d = 1; d <= W && best < 0; ++d) {
-      const int dd = d * d;
-      best = max(best, max(stile[((a + d) & (N - 1)) * DT_CW + c] - dd,
-                           stile[((a - d) & (N - 1)) * DT_CW + c] - dd));
-    }
-    const long i = base + (long)a * stride + c;
-    // single-cell fill (:281-288) with h = (float)(chain(src) * zeta)
-    const float h = sd_to_float(sd_mul(src_chain(src[i], pa), zeta));
-    const float dd0 = rec0[i];
-    float f;
-    if (h > 0.0f) {
-      if (dd0 > 0.0f)
-        f = (h >= dd0) ? 1.0f : __fdiv_rn(h, dd0);
-      else
-        f = 1.0f;
-    } else {
-      f = 0.0f;
-    }
-    if (best >= 0) f = 1.0f;  // inside a bubble (:392, :448)
-    // cap: if (bubblef > 1.0 - fresid) bubblef = 1.0 - fresid   (:470)
-    const sd_t om = sd_sub(SD_ONE, sd_from_float(fres[i]));
-    if (sd_gt(sd_from_float(f), om)) f = sd_to_float(om);
-    xhii[i] = f;
-  }
-}
-
 // Single-cell fill alone (check hook): :281-288 without dilation and cap.
 __global__ void k_fill0(long n3, sd_t zeta, const float* __restrict__ src, const float* __restrict__ rec0,
                         const PrologueArgs pa, float* __restrict__ fill) {
@@ -269,34 +153,6 @@ __global__ void k_fill0(long n3, sd_t zeta, const float* __restrict__ src, const
 cudaError_t launch_fill0(long n3, uint64_t zeta, const float* src, const float* rec0,
                          const PrologueArgs& pa, float* fill, cudaStream_t st) {
   k_fill0<<<prologue_blocks(n3), PRO_THREADS, 0, st>>>(n3, zeta, src, rec0, pa, fill);
-  return cudaGetLastError();
-}
-
-cudaError_t dilate_setup(int N) {
-  cudaError_t e;
-  const int tile = N * DT_CW * (int)sizeof(int);
-  if ((e = cudaFuncSetAttribute(k_dt_b, cudaFuncAttributeMaxDynamicSharedMemorySize, tile))) return e;
-  if ((e = cudaFuncSetAttribute(k_dt_a_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, tile))) return e;
-  return cudaSuccess;
-}
-
-cudaError_t launch_dt_rows(int N, const uint8_t* rc, const int* nmax, int vmax, int* out, cudaStream_t st) {
-  k_dt_rows<<<(unsigned)((long)N * N), DT_ROW_THREADS, N * sizeof(int), st>>>(N, rc, nmax, vmax, out);
-  return cudaGetLastError();
-}
-
-static unsigned dt_grid(int N) { return (unsigned)((long)N * (N / DT_CW)); }
-static int dt_threads(int N) { return N * DT_CW < 512 ? N * DT_CW : 512; }
-
-cudaError_t launch_dt_b(int N, const int* in, int vmax, int* out, cudaStream_t st) {
-  k_dt_b<<<dt_grid(N), dt_threads(N), (size_t)N * DT_CW * sizeof(int), st>>>(N, in, vmax, out);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_dt_a_finish(int N, const int* in, int vmax, uint64_t zeta, const float* src, const float* rec0,
-                               const float* fres, const PrologueArgs& pa, float* xhii, cudaStream_t st) {
-  k_dt_a_finish<<<dt_grid(N), dt_threads(N), (size_t)N * DT_CW * sizeof(int), st>>>(N, in, vmax, zeta, src, rec0,
-                                                                                  fres, pa, xhii);
   return cudaGetLastError();
 }
 

@@ -75,7 +75,11 @@ struct PipeGeom {
 
 // MODE 0: ky inverse pass, in place, over the K work boxes of the batch.
 // MODE 1: kx inverse pass + centre test + first-hit update (K boxes per tile).
-template <int N, int MODE>
+// LAYOUT 0: work boxes in the natural layout (a N^2 + b N + c);
+// LAYOUT 1: column-block major (((c / CW) N + a) N + b) CW + c mod CW
+// (kernels_cb.cu): a ky tile is one contiguous run, a kx tile stays inside
+// one N^2 CW slab.  rc is in the natural layout either way.
+template <int N, int MODE, int LAYOUT>
 __global__ void __launch_bounds__(PipeGeom<N>::THREADS, 1)
 k_pipe(const __grid_constant__ CUtensorMap tmap, Batch bt, float2* __restrict__ work0, long box_stride,
        uint8_t* __restrict__ rc, const float* __restrict__ alpha_ptr, const float2* __restrict__ gtw,
@@ -113,7 +117,18 @@ k_pipe(const __grid_constant__ CUtensorMap tmap, Batch bt, float2* __restrict__ 
   auto decode = [&](long li, int& k, int& outer, int& cb) {
     const long ti = li / per_tile;
     const long tile = blockIdx.x + ti * gridDim.x;
-    if (MODE == 0) {
+    if (LAYOUT == 1) {  // consecutive tiles are adjacent in memory
+      if (MODE == 0) {
+        k = (int)(tile / ((long)N * nblk));
+        const long rem = tile % ((long)N * nblk);
+        cb = (int)(rem / N);
+        outer = (int)(rem % N);
+      } else {
+        k = (int)(li % per_tile);
+        cb = (int)(tile / N);
+        outer = (int)(tile % N);
+      }
+    } else if (MODE == 0) {
       k = (int)(tile / ((long)N * nblk));
       const long rem = tile % ((long)N * nblk);
       outer = (int)(rem / nblk);
@@ -132,7 +147,12 @@ k_pipe(const __grid_constant__ CUtensorMap tmap, Batch bt, float2* __restrict__ 
     mbar_expect_tx(bar, (uint32_t)G::STAGE);
     const int wk = (int)((bt.r[k].work - work0) / box_stride);
     for (int q = 0; q < G::NBOX; ++q) {
-      if (MODE == 0)  // rows b, fixed a = outer
+      if (LAYOUT == 1) {  // map dims (2 CW floats, b, a, column block + nblk * box)
+        if (MODE == 0)
+          tma_load_4d(dst + (size_t)q * G::BOX * G::CW, &tmap, bar, 0, q * G::BOX, outer, wk * nblk + cb);
+        else
+          tma_load_4d(dst + (size_t)q * G::BOX * G::CW, &tmap, bar, 0, outer, q * G::BOX, wk * nblk + cb);
+      } else if (MODE == 0)  // rows b, fixed a = outer
         tma_load_4d(dst + (size_t)q * G::BOX * G::CW, &tmap, bar, 2 * cb * G::CW, q * G::BOX, outer, wk);
       else            // rows a, fixed b = outer
         tma_load_4d(dst + (size_t)q * G::BOX * G::CW, &tmap, bar, 2 * cb * G::CW, outer, q * G::BOX, wk);
@@ -162,7 +182,11 @@ k_pipe(const __grid_constant__ CUtensorMap tmap, Batch bt, float2* __restrict__ 
     __syncthreads();  // stage free for the copy issued next iteration
     fft_line<N, true>(v, xch + col * G::LS, stw, j);
     const int c = cb * G::CW + col;
-    if (MODE == 0) {
+    if (MODE == 0 && LAYOUT == 1) {
+      float2* box = bt.r[k].work + ((long)cb * N + outer) * N * G::CW + col;
+#pragma unroll
+      for (int r = 0; r < 8; ++r) box[(j + r * (N / 8)) * G::CW] = v[r];
+    } else if (MODE == 0) {
       float2* box = bt.r[k].work + (long)outer * N * N + c;
 #pragma unroll
       for (int r = 0; r < 8; ++r) box[(long)(j + r * (N / 8)) * N] = v[r];
@@ -218,14 +242,23 @@ static PFN_encodeTiled encode_fn() {
   return fn;
 }
 
-// Tensor map over K contiguous N^3 complex boxes viewed as float32
-// (2N, N, N, K); box (2 CW, rows, 1, 1) for the ky pass (rows along b) or
-// (2 CW, 1, rows, 1) for the kx pass (rows along a).
-static cudaError_t make_map(CUtensorMap* m, int N, int K, void* base, int cw, int box_rows, bool rows_along_a) {
+// Tensor map over K contiguous N^3 complex boxes viewed as float32:
+// natural layout (2N, N, N, K), column-block-major layout
+// (2 CW, N, N, K N / CW); box (2 CW, rows, 1, 1) for the ky pass (rows along
+// b) or (2 CW, 1, rows, 1) for the kx pass (rows along a).
+static cudaError_t make_map(CUtensorMap* m, int N, int K, void* base, int cw, int box_rows, bool rows_along_a,
+                            int layout = 0) {
   PFN_encodeTiled enc = encode_fn();
   if (!enc) return cudaErrorNotSupported;
   cuuint64_t dims[4] = {(cuuint64_t)2 * N, (cuuint64_t)N, (cuuint64_t)N, (cuuint64_t)K};
   cuuint64_t strides[3] = {(cuuint64_t)2 * N * 4, (cuuint64_t)2 * N * N * 4, (cuuint64_t)2 * N * N * N * 4};
+  if (layout == 1) {
+    dims[0] = (cuuint64_t)2 * cw;
+    dims[3] = (cuuint64_t)K * (N / cw);
+    strides[0] = (cuuint64_t)2 * cw * 4;
+    strides[1] = (cuuint64_t)2 * cw * N * 4;
+    strides[2] = (cuuint64_t)2 * cw * N * N * 4;
+  }
   cuuint32_t box[4] = {(cuuint32_t)(2 * cw), rows_along_a ? 1u : (cuuint32_t)box_rows,
                        rows_along_a ? (cuuint32_t)box_rows : 1u, 1u};
   cuuint32_t estr[4] = {1, 1, 1, 1};
@@ -240,21 +273,32 @@ struct PipeLaunch {
   using G = PipeGeom<N>;
   static cudaError_t setup() {
     cudaError_t e;
-    if ((e = cudaFuncSetAttribute(k_pipe<N, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::SMEM))) return e;
-    return cudaFuncSetAttribute(k_pipe<N, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::SMEM);
+    if ((e = cudaFuncSetAttribute(k_pipe<N, 0, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::SMEM)))
+      return e;
+    if ((e = cudaFuncSetAttribute(k_pipe<N, 1, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::SMEM)))
+      return e;
+    if ((e = cudaFuncSetAttribute(k_pipe<N, 0, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::SMEM)))
+      return e;
+    return cudaFuncSetAttribute(k_pipe<N, 1, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::SMEM);
   }
   static cudaError_t maps(PipeMaps* pm, int K, void* base) {
     cudaError_t e;
     if ((e = make_map(&pm->b_rows, N, K, base, G::CW, G::BOX, false))) return e;
-    return make_map(&pm->a_rows, N, K, base, G::CW, G::BOX, true);
+    if ((e = make_map(&pm->a_rows, N, K, base, G::CW, G::BOX, true))) return e;
+    if ((e = make_map(&pm->b_rows_cb, N, K, base, G::CW, G::BOX, false, 1))) return e;
+    return make_map(&pm->a_rows_cb, N, K, base, G::CW, G::BOX, true, 1);
   }
-  static cudaError_t launch(int mode, const PipeMaps& pm, const Batch& bt, float2* work0, uint8_t* rc,
+  static cudaError_t launch(int mode, int layout, const PipeMaps& pm, const Batch& bt, float2* work0, uint8_t* rc,
                             const float* alpha, const float2* tw, int* err, int nsm, cudaStream_t st) {
     const long box_stride = (long)N * N * N;
-    if (mode == 0)
-      k_pipe<N, 0><<<nsm, G::THREADS, G::SMEM, st>>>(pm.b_rows, bt, work0, box_stride, rc, alpha, tw, err);
+    if (mode == 0 && layout == 0)
+      k_pipe<N, 0, 0><<<nsm, G::THREADS, G::SMEM, st>>>(pm.b_rows, bt, work0, box_stride, rc, alpha, tw, err);
+    else if (mode == 1 && layout == 0)
+      k_pipe<N, 1, 0><<<nsm, G::THREADS, G::SMEM, st>>>(pm.a_rows, bt, work0, box_stride, rc, alpha, tw, err);
+    else if (mode == 0)
+      k_pipe<N, 0, 1><<<nsm, G::THREADS, G::SMEM, st>>>(pm.b_rows_cb, bt, work0, box_stride, rc, alpha, tw, err);
     else
-      k_pipe<N, 1><<<nsm, G::THREADS, G::SMEM, st>>>(pm.a_rows, bt, work0, box_stride, rc, alpha, tw, err);
+      k_pipe<N, 1, 1><<<nsm, G::THREADS, G::SMEM, st>>>(pm.a_rows_cb, bt, work0, box_stride, rc, alpha, tw, err);
     return cudaGetLastError();
   }
 };
@@ -283,14 +327,14 @@ cudaError_t pipe_make_maps(int N, PipeMaps* pm, int K, void* work_base) {
   }
 }
 
-cudaError_t launch_pipe(int N, int mode, const PipeMaps& pm, const Batch& bt, float2* work0, uint8_t* rc,
-                        const float* alpha, const float2* tw, int* err, int nsm, cudaStream_t st) {
+cudaError_t launch_pipe(int N, int mode, int layout, const PipeMaps& pm, const Batch& bt, float2* work0,
+                        uint8_t* rc, const float* alpha, const float2* tw, int* err, int nsm, cudaStream_t st) {
   switch (N) {
-    case 64: return PipeLaunch<64>::launch(mode, pm, bt, work0, rc, alpha, tw, err, nsm, st);
-    case 128: return PipeLaunch<128>::launch(mode, pm, bt, work0, rc, alpha, tw, err, nsm, st);
-    case 256: return PipeLaunch<256>::launch(mode, pm, bt, work0, rc, alpha, tw, err, nsm, st);
-    case 512: return PipeLaunch<512>::launch(mode, pm, bt, work0, rc, alpha, tw, err, nsm, st);
-    case 1024: return PipeLaunch<1024>::launch(mode, pm, bt, work0, rc, alpha, tw, err, nsm, st);
+    case 64: return PipeLaunch<64>::launch(mode, layout, pm, bt, work0, rc, alpha, tw, err, nsm, st);
+    case 128: return PipeLaunch<128>::launch(mode, layout, pm, bt, work0, rc, alpha, tw, err, nsm, st);
+    case 256: return PipeLaunch<256>::launch(mode, layout, pm, bt, work0, rc, alpha, tw, err, nsm, st);
+    case 512: return PipeLaunch<512>::launch(mode, layout, pm, bt, work0, rc, alpha, tw, err, nsm, st);
+    case 1024: return PipeLaunch<1024>::launch(mode, layout, pm, bt, work0, rc, alpha, tw, err, nsm, st);
     default: return cudaErrorInvalidValue;
   }
 }

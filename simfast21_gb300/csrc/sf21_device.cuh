@@ -31,9 +31,10 @@ struct Batch {
 // truncation < 3e-11) avoids the cancellation of the closed form in float.
 // Above, the closed form with sin/cos of the argument reduced to [-pi, pi]
 // by a two-constant Cody-Waite step and evaluated by the SFU (__sinf/__cosf,
-// absolute error < 4e-7 on the reduced argument): the error this leaves in W
-// is below 1.8e-6 / x^2 <= 5e-7 absolute (W(0) = 1), under the FP32 rounding
-// of the transforms it feeds.
+// absolute error < 4e-7 on the reduced argument), divided by x^3 with the
+// fast division (2 ulp): the error this leaves in W is below
+// 1.8e-6 / x^2 + 3e-7 |W| <= 7e-7 absolute (W(0) = 1), under the FP32
+// rounding of the transforms it feeds.
 __device__ __forceinline__ float w_tophat(float x) {
   if (x < 2.0f) {
     const float y = x * x;
@@ -52,8 +53,7 @@ __device__ __forceinline__ float w_tophat(float x) {
   float r = fmaf(-k, 6.28318548202514648f, x);
   r = fmaf(-k, -1.7484555314695172e-07f, r);
   const float s = __sinf(r), c = __cosf(r);
-  const float ix = __frcp_rn(x);
-  return 3.0f * fmaf(-x, c, s) * ix * ix * ix;
+  return __fdividef(3.0f * fmaf(-x, c, s), x * x * x);  // 2 ulp; x^3 < 2^126 here
 }
 
 // Signed frequency index of position i on an N-point axis (:309-311).

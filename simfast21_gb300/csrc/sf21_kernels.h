@@ -43,14 +43,18 @@ cudaError_t launch_prologue(long n3, const float* delta, const float* src, const
 cudaError_t launch_alpha(const float* partials, int nblocks, float* alpha, cudaStream_t st);
 int prologue_blocks(long n3);
 
-// Dilation of the first-hit radius field and the final xHII box of one set:
-// three max-plus passes (c, b, a); the last one also applies the single-cell
-// fill and the cap.
-cudaError_t dilate_setup(int N);
-cudaError_t launch_dt_rows(int N, const uint8_t* rc, const int* nmax, int vmax, int* out, cudaStream_t st);
-cudaError_t launch_dt_b(int N, const int* in, int vmax, int* out, cudaStream_t st);
-cudaError_t launch_dt_a_finish(int N, const int* in, int vmax, uint64_t zeta, const float* src, const float* rec0,
-                               const float* fres, const PrologueArgs& pa, float* xhii, cudaStream_t st);
+// Dilation of the first-hit radius field and the final xHII box of one set
+// (kernels_dt.cu): three max-plus passes (a: rc -> i1, b: i1 -> i2,
+// c: i2 -> xhii); the last one also applies the single-cell fill and the cap.
+// finish_prep, once per redshift: source chain before zeta (double bits) and
+// 1 - fresid rounded down / to nearest per voxel.
+cudaError_t dt_setup(int N);
+cudaError_t launch_dt_pa(int N, const uint8_t* rc, const int* nmax, int* i1, cudaStream_t st);
+cudaError_t launch_dt_pb(int N, const int* i1, int* i2, cudaStream_t st);
+cudaError_t launch_dt_pc_finish(int N, const int* i2, uint64_t zeta, const uint64_t* chain, const float* rec0,
+                                const float2* om, float* xhii, cudaStream_t st);
+cudaError_t launch_finish_prep(long n3, const float* src, const float* fres, const PrologueArgs& pa, uint64_t* chain,
+                               float2* om, cudaStream_t st);
 cudaError_t launch_fill0(long n3, uint64_t zeta, const float* src, const float* rec0,
                          const PrologueArgs& pa, float* fill, cudaStream_t st);
 
@@ -64,16 +68,27 @@ cudaError_t launch_plane_filter(int N, const float2* spec, const Batch& bt, cons
 // TMA-pipelined persistent strided passes (kernels_pipe.cu).  The K work
 // boxes must be consecutive N^3 slices of one allocation starting at work0.
 struct PipeMaps {
-  CUtensorMap b_rows;  // tiles of rows along b (ky pass)
-  CUtensorMap a_rows;  // tiles of rows along a (kx pass)
+  CUtensorMap b_rows;     // tiles of rows along b (ky pass), natural layout
+  CUtensorMap a_rows;     // tiles of rows along a (kx pass), natural layout
+  CUtensorMap b_rows_cb;  // the same over the column-block-major layout
+  CUtensorMap a_rows_cb;
 };
 bool pipe_supported(int N);
 cudaError_t pipe_setup(int N);
 cudaError_t pipe_make_maps(int N, PipeMaps* pm, int K, void* work_base);
 // mode 0: ky inverse pass in place over the batch's boxes; mode 1: kx inverse
-// pass + centre test + first-hit update.  nsm = persistent CTAs.
-cudaError_t launch_pipe(int N, int mode, const PipeMaps& pm, const Batch& bt, float2* work0, uint8_t* rc,
-                        const float* alpha, const float2* tw, int* err, int nsm, cudaStream_t st);
+// pass + centre test + first-hit update.  layout 0: natural work boxes,
+// 1: column-block major (kernels_cb.cu).  nsm = persistent CTAs.
+cudaError_t launch_pipe(int N, int mode, int layout, const PipeMaps& pm, const Batch& bt, float2* work0,
+                        uint8_t* rc, const float* alpha, const float2* tw, int* err, int nsm, cudaStream_t st);
+
+// Radius pipeline over column-block-major work boxes (kernels_cb.cu):
+// c-axis filter pass, in-place b-axis pass, a-axis pass + centre test.
+cudaError_t cb_setup(int N);
+cudaError_t launch_rows_filter_cb(int N, const float2* spec, const Batch& bt, const float2* tw, cudaStream_t st);
+cudaError_t launch_cols_b_cb(int N, const Batch& bt, const float2* tw, cudaStream_t st);
+cudaError_t launch_cols_a_test_cb(int N, const Batch& bt, uint8_t* rc, const float* alpha, const float2* tw,
+                                  cudaStream_t st);
 
 // Criterion and adjoint (kernels_adj.cu).
 cudaError_t adj_setup(int N);

@@ -34,6 +34,9 @@ EXPORTS = [
 ]
 
 
+NPATH = 7  # radius pipelines (FilterBank.path)
+
+
 class HIIError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__(f"{_STATUS.get(code, code)}: {msg}")
@@ -158,11 +161,12 @@ class FilterBank:
 
     def path(self):
         """(pipeline in use: 1 = three axis passes, 2 = plane clusters,
-        3 = TMA-pipelined ky pass, 4 = TMA-pipelined ky and kx passes;
-        {pipeline: tuned ms of one batch})."""
-        ms = (ctypes.c_double * 4)()
-        p = self._lib.sf21_hii_path(self._h, ms, 4)
-        return p, {i + 1: ms[i] for i in range(4)}
+        3 = TMA-pipelined ky pass, 4 = TMA-pipelined ky and kx passes, and over
+        column-block-major work boxes 5 = three axis passes, 6 = TMA ky pass,
+        7 = TMA ky and kx passes; {pipeline: tuned ms of one batch})."""
+        ms = (ctypes.c_double * NPATH)()
+        p = self._lib.sf21_hii_path(self._h, ms, NPATH)
+        return p, {i + 1: ms[i] for i in range(NPATH)}
 
     def check(self):
         """Raise if a bounded device wait expired since the last check."""

@@ -256,3 +256,52 @@ def write_base_dir(base: str, w: Workload, zmin: float, zmax: float, dz: float,
         delta.tofile(os.path.join(base, box_name("delta", z, w.N, L_file)))
         sfrd.tofile(os.path.join(base, box_name("sfrd", z, w.N, L_file)))
     return zs
+
+
+def make_boxes_torch(N: int, L: float, z: float, seed: int, device="cuda", sigma: float = 0.8,
+                     occupancy: float = 0.02):
+    """The same generators on the GPU with torch (for large timing boxes, e.g.
+    1024^3, where the numpy path would dominate the run): returns float32
+    CUDA tensors (delta, sfrd).  Same distributions, not the same numbers as
+    make_boxes."""
+    import torch
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    white = torch.randn((N, N, N), generator=g, device=device, dtype=torch.float32)
+    wk = torch.fft.rfftn(white)
+    del white
+    f = torch.fft.fftfreq(N, d=1.0 / N, device=device)
+    h = torch.arange(N // 2 + 1, device=device, dtype=torch.float32)
+    kk = f[:, None, None] ** 2 + f[None, :, None] ** 2 + h[None, None, :] ** 2
+    amp = torch.where(kk > 0, kk.clamp(min=1e-30) ** (-0.5), torch.zeros_like(kk))
+    wk *= amp
+    del amp, kk
+    gr = torch.fft.irfftn(wk, s=(N, N, N))
+    del wk
+    gr -= gr.mean()
+    gr /= gr.std()
+    delta = torch.exp(sigma * gr - 0.5 * sigma * sigma) - 1.0
+    del gr
+    w = torch.exp(1.5 * delta.double().flatten()[:: max(1, N ** 3 // (1 << 21))])
+    lo, hi = -80.0, 80.0
+    for _ in range(60):
+        mid = 0.5 * (lo + hi)
+        if float(torch.clamp(math.exp(mid) * w, max=1.0).mean()) < occupancy:
+            lo = mid
+        else:
+            hi = mid
+    p = torch.clamp(math.exp(0.5 * (lo + hi)) * torch.exp(1.5 * delta), max=1.0)
+    host = torch.rand((N, N, N), generator=g, device=device) < p
+    del p
+    n = int(host.sum())
+    u = torch.rand(n, generator=g, device=device, dtype=torch.float64)
+    a = -0.9
+    m = (1e8 ** a + u * (1e12 ** a - 1e8 ** a)) ** (1.0 / a)
+    m32 = m.float().double()
+    c1, c2, c3, c4 = 1.575e39, 9.367608e07, 0.44, 2.27044695e00
+    rion = c1 * m32 * (1.0 + z) ** c4 * (m32 / c2) ** c3 * torch.exp(-((c2 / m32) ** 3.0)) / V_NORM
+    sfr = rion / qion(z)
+    dx = L / N
+    sfrd = torch.zeros((N, N, N), device=device, dtype=torch.float32)
+    sfrd[host] = (SOURCE_SCALE * sfr / dx ** 3).float()
+    return delta.float().contiguous(), sfrd

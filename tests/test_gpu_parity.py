@@ -165,22 +165,24 @@ def test_plain_form_matches_reference(hii, oracle_lib):
 
 @pytest.mark.parametrize("N,L", [(64, 50.0), (128, 100.0)])
 def test_radius_pipelines_agree(hii, N, L):
-    """The three radius pipelines -- three axis passes, the cluster plane pass
-    (filter + kz + ky in distributed shared memory) and the TMA-pipelined
-    persistent strided passes -- run the same arithmetic: identical outputs."""
+    """The radius pipelines -- three axis passes, the cluster plane pass
+    (filter + kz + ky in distributed shared memory), the TMA-pipelined
+    persistent strided passes, and the same over column-block-major work
+    boxes -- run the same arithmetic: identical outputs."""
     w = synth.Workload(N=N, L=L, zs=[8.0], zeta=40.0, Rmax=L / 2, factor=1.1, seed=21)
     delta, sfrd = synth.make_boxes(w, 8.0)
     sets = [(40.0, L / 2, w.Nbins), (15.0, L / 5, 20)]
-    banks = {p: hii.FilterBank(N, L, 0.71, sets, path=p) for p in (1, 2, 3, 4)}
+    paths = range(1, hii.NPATH + 1)
+    banks = {p: hii.FilterBank(N, L, 0.71, sets, path=p) for p in paths}
     ref_x, ref_n = banks[1].run_z(8.0, delta, sfrd)
-    for p in (2, 3, 4):
+    for p in paths[1:]:
         assert banks[p].path()[0] == p
         x, n = banks[p].run_z(8.0, delta, sfrd)
         assert np.array_equal(ref_x.view(np.uint32), x.view(np.uint32)), p
         for s in range(len(sets)):
             assert np.array_equal(banks[1].first_hit(8.0, delta, sfrd, s), banks[p].first_hit(8.0, delta, sfrd, s))
-    banks[3].check()
-    banks[4].check()
+    for p in paths:
+        banks[p].check()
 
 
 def test_halo_source_on_gpu_bit_exact(hii, oracle_lib):
@@ -215,3 +217,67 @@ def test_halo_source_larger_catalogue(hii, oracle_lib):
     got = fb.halo_source(7.5, cat)
     want = oracle_lib.halo_smoothed(p, 7.5, cat)
     assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+def test_xhii_256_redshift_series(hii, oracle_lib):
+    """Plain GPU drop-in configuration: 256^3, L = 200 Mpc/h, zeta = 30, Rmax =
+    60 Mpc/h, factor 1.05, density scaled by the linear growth factor over 20
+    redshifts from 12 to 6.  All 20 run on the GPU; the first and the last are
+    checked against the CPU restatement outside the tolerance band."""
+    zs = [12.0 - 6.0 * i / 19 for i in range(20)]
+    w = synth.Workload(N=256, L=200.0, zs=zs, zeta=30.0, Rmax=60.0, factor=1.05, seed=1236, z_ref=8.0)
+    sp = P.StageParams(nthreads=16, zmin=6.0, zmax=12.0, dz=6.0 / 19, L=200.0, hubble=0.71, N_halo=256, N=256,
+                       fesc=30.0, xHlim=0.999, Rmax=60.0, Nbins=w.Nbins, use_sfr=True)
+    fb = _bank(hii, sp)
+    g_unit = synth.gaussian_field(w.N, w.seed)
+    neutral = []
+    for i, z in enumerate(zs):
+        delta, sfrd = synth.make_boxes(w, z, g_unit)
+        x, nf = fb.run_z(z, delta, sfrd)
+        neutral.append(float(nf[0]))
+        if i in (0, len(zs) - 1):
+            ref, b, lo, hi = _bounds(oracle_lib, sp, z, delta, sfrd)
+            certain = b["ionised_lo"] == b["ionised_hi"]
+            assert np.array_equal(x[0][certain].view(np.uint32), ref["xhii"][certain].view(np.uint32))
+            assert np.all((x[0] == lo) | (x[0] == hi))
+            print(f"z={z:.3f}: neutral {nf[0]:.6f}, band voxels {int((~certain).sum())}, "
+                  f"differences from the restatement {int((x[0] != ref['xhii']).sum())}")
+    assert all(0.0 <= v <= 1.0 for v in neutral)
+
+
+def test_filtered_fields_cufft_crosscheck(hii, oracle_lib):
+    """cuFFT as a cross-check only: at 256^3 the library's filtered fields and
+    the same filter applied with cuFFT in complex64 are compared with the FP64
+    fields; the library's error stays within the 1e-5 bound and within a small
+    factor of cuFFT's own FP32 error."""
+    import torch
+    N, L, z = 256, 200.0, 8.0
+    w = synth.Workload(N=N, L=L, zs=[z], zeta=30.0, Rmax=60.0, factor=1.05, seed=4321)
+    delta, sfrd = synth.make_boxes(w, z)
+    fb = hii.FilterBank(N, L, 0.71, [(30.0, 60.0, w.Nbins)])
+    p = oracle_lib.params(N, L, 0.71, 60.0, w.Nbins, 30.0, max_radii=1)  # prologue + one radius
+    ex = oracle_lib.run_z_sfr(p, z, delta, sfrd, extras=True)
+    rec0, ion0 = ex["rec0"], ex["ion0"]
+    radii, nf = fb.radii()
+    dk = 2 * P.PI / L
+    f = torch.fft.fftfreq(N, d=1.0 / N, device="cuda")
+    h = torch.arange(N // 2 + 1, device="cuda", dtype=torch.float32)
+    kmag = dk * torch.sqrt(f[:, None, None] ** 2 + f[None, :, None] ** 2 + h[None, None, :] ** 2)
+    R0 = torch.fft.rfftn(torch.from_numpy(rec0).cuda())
+    H0 = torch.fft.rfftn(torch.from_numpy(ion0).cuda())
+    for ridx in (0, nf // 2, nf - 1):
+        R = radii[ridx]
+        rec, ion = fb.filtered(z, delta, sfrd, ridx)
+        d64, h64 = F.filtered_fields(rec0, ion0, R, dk)
+        x = (kmag * R).double()
+        W = torch.where(x < 0.03, 1.0 - x * x / 10.0, 3.0 * (torch.sin(x) - x * torch.cos(x)) / x.clamp(min=1e-30) ** 3)
+        W = W.float()
+        rc = (torch.fft.irfftn(R0 * W, s=(N, N, N)) * N ** 3).cpu().numpy()
+        hc = (torch.fft.irfftn(H0 * W, s=(N, N, N)) * N ** 3).cpu().numpy()
+        for ours, cu, ref in ((rec, rc, d64), (ion, hc, h64)):
+            scale = np.abs(ref).max()
+            e_ours = np.abs(ours - ref).max() / scale
+            e_cu = np.abs(cu - ref).max() / scale
+            print(f"R={R:.3f}: library {e_ours:.2e}, cuFFT {e_cu:.2e} (of max |field|)")
+            assert e_ours <= TOL_FIELD
+            assert e_ours <= 4.0 * e_cu + 1e-7
