@@ -62,8 +62,17 @@ struct SetInfo {
 
 // Radius pipelines: 1 three axis passes, 2 plane clusters + kx pass,
 // 3 TMA ky + kx pass, 4 TMA ky + TMA kx, and over column-block-major work
-// boxes: 5 three axis passes, 6 TMA ky + kx pass, 7 TMA ky + TMA kx.
-constexpr int NPATH = 7;
+// boxes: 5 three axis passes, 6 TMA ky + kx pass, 7 TMA ky + TMA kx,
+// 8 fused filter + ky pass through L2 + kx pass.
+constexpr int NPATH = 8;
+// Planes between a plane's row tasks and its column tasks in the fused
+// pipeline: enough for the row tasks to finish first, few enough that the
+// (DELAY + 1) planes x K slices in flight stay well inside L2 (~24 MB).
+static int fused_delay(long N, int K) {
+  const double plane_bytes = (double)K * N * N * 8.0;
+  int d = (int)(24.0e6 / plane_bytes);
+  return d < 2 ? 2 : (d > 8 ? 8 : d);
+}
 
 struct sf21_hii_ctx {
   int device = 0;
@@ -115,6 +124,7 @@ struct sf21_hii_ctx {
   float2 *d_spec = nullptr, *d_tw = nullptr;
   std::vector<float2*> d_work;
   uint8_t* d_rc = nullptr;
+  int* d_fctl = nullptr;  // queue + per-plane counters of the fused pipeline
   PrologueArgs pa;   // scalars of the redshift being processed (kernel arguments)
   int pro_blocks = 0;
   std::string err;
@@ -206,7 +216,7 @@ static void free_ctx(sf21_hii_ctx* c) {
   void* ptrs[] = {c->d_delta, c->d_src, c->d_rec0, c->d_fres, c->d_partials, c->d_alpha,
                   c->d_xhii, c->d_spec, c->d_tw, c->d_rc, c->d_mask, c->d_flag, c->d_box2,
                   c->d_C, c->d_A, c->d_acc, c->d_zpart, c->d_g, c->d_gd, c->d_gs, c->d_halos, c->d_fine,
-                  c->d_hscratch, c->d_chain, c->d_om};
+                  c->d_hscratch, c->d_chain, c->d_om, c->d_fctl};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->d_work_base) cudaFree(c->d_work_base);
@@ -321,6 +331,7 @@ extern "C" int sf21_hii_create(const sf21_hii_config* cfg, sf21_hii_ctx** out) {
   CREATE_CUDA(cudaMalloc(&c->d_xhii, box_f));
   CREATE_CUDA(cudaMalloc(&c->d_spec, box_c));
   CREATE_CUDA(cudaMalloc(&c->d_rc, c->n3));
+  CREATE_CUDA(cudaMalloc(&c->d_fctl, sizeof(int) * (N + 1)));
   c->d_work.assign(K, nullptr);
   CREATE_CUDA(cudaMalloc(&c->d_work_base, box_c * K));
   for (int k = 0; k < K; ++k) c->d_work[k] = c->d_work_base + (size_t)k * c->n3;
@@ -481,9 +492,12 @@ static int enqueue_batch(sf21_hii_ctx* c, const Batch& bt, cudaStream_t st) {
   }
   if (c->path >= 5) {  // column-block-major work boxes
     int e0 = mark(c, st);
-    CTX_CUDA(c, launch_rows_filter_cb(N, c->d_spec, bt, c->d_tw, st));
-    int e1 = mark(c, st);
-    if (c->path == 5)
+    if (c->path != 8) CTX_CUDA(c, launch_rows_filter_cb(N, c->d_spec, bt, c->d_tw, st));
+    int e1 = mark(c, st);  // pipeline 8: the filter pass is inside the fused kernel below
+    if (c->path == 8)
+      CTX_CUDA(c, launch_rows_cols_b_fused(N, c->d_spec, bt, c->d_tw, c->d_fctl, fused_delay(N, bt.K), c->d_err,
+                                           c->nsm, st));
+    else if (c->path == 5)
       CTX_CUDA(c, launch_cols_b_cb(N, bt, c->d_tw, st));
     else
       CTX_CUDA(c, launch_pipe(N, 0, 1, c->pmaps, bt, c->d_work_base, c->d_rc, c->d_alpha, c->d_tw, c->d_err,

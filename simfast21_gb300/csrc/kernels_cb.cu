@@ -38,28 +38,21 @@ __device__ __forceinline__ long cb_index(int a, int b, int c) {
 
 // c-axis inverse pass with the top-hat filter of the K radii of the batch
 // (get_HIIbubbles.c:305-322): spectrum row (a, b) read once, K filtered
-// transformed rows written column-block major.
+// transformed rows written column-block major.  One row per N/8 threads
+// (j = thread index in the row, sline = this row's exchange line).
 template <int N>
-__global__ void __launch_bounds__(CbGeom<N>::RTHREADS)
-k_rows_filter_cb(const float2* __restrict__ spec, Batch bt, const float2* __restrict__ gtw) {
+__device__ __forceinline__ void rows_filter_row(const float2* __restrict__ spec, const Batch& bt,
+                                                const float2* stw, float2* sline, int a, int b, int j) {
   using G = CbGeom<N>;
-  using L = LineGeom<N>;
-  __shared__ float2 stw[N];
-  __shared__ float2 sbuf[G::ROWS * L::LS];
-  for (int t = threadIdx.x; t < N; t += blockDim.x) stw[t] = gtw[t];
-  const int row_in_cta = threadIdx.x / G::RT;
-  const int j = threadIdx.x % G::RT;
-  const long row = (long)blockIdx.x * G::ROWS + row_in_cta;
-  const int a = (int)(row / N), b = (int)(row % N);
   const int ka = kfreq(a, N), kb = kfreq(b, N);
   const int kab = ka * ka + kb * kb;
   float2 z[8];
   float kmag[8];
-  const float2* src = spec + row * N;
+  const float2* src = spec + ((long)a * N + b) * N;
 #pragma unroll
   for (int r = 0; r < 8; ++r) {
     const int c = j + r * (N / 8);
-    z[r] = src[c];
+    z[r] = __ldg(src + c);
     const int kc = kfreq(c, N);
     kmag[r] = sqrtf((float)(kab + kc * kc));
   }
@@ -72,7 +65,7 @@ k_rows_filter_cb(const float2* __restrict__ spec, Batch bt, const float2* __rest
       const float w = w_tophat(dkR * kmag[r]);
       v[r] = make_float2(z[r].x * w, z[r].y * w);
     }
-    fft_line<N, true>(v, sbuf + row_in_cta * L::LS, stw, j);
+    fft_line<N, true>(v, sline, stw, j);
     if constexpr ((N / 8) % G::CW == 0) {
       // c = j + r N/8: column block j/CW + r (N/8)/CW, offset j mod CW
       float2* dst = bt.r[k].work + cb_index<N>(a, b, j);
@@ -85,6 +78,20 @@ k_rows_filter_cb(const float2* __restrict__ spec, Batch bt, const float2* __rest
       for (int r = 0; r < 8; ++r) dst[cb_index<N>(a, b, j + r * (N / 8))] = v[r];
     }
   }
+}
+
+template <int N>
+__global__ void __launch_bounds__(CbGeom<N>::RTHREADS)
+k_rows_filter_cb(const float2* __restrict__ spec, Batch bt, const float2* __restrict__ gtw) {
+  using G = CbGeom<N>;
+  using L = LineGeom<N>;
+  __shared__ float2 stw[N];
+  __shared__ float2 sbuf[G::ROWS * L::LS];
+  for (int t = threadIdx.x; t < N; t += blockDim.x) stw[t] = gtw[t];
+  const int row_in_cta = threadIdx.x / G::RT;
+  const int j = threadIdx.x % G::RT;
+  const long row = (long)blockIdx.x * G::ROWS + row_in_cta;
+  rows_filter_row<N>(spec, bt, stw, sbuf + row_in_cta * L::LS, (int)(row / N), (int)(row % N), j);
 }
 
 // b-axis inverse pass in place: tile (a, column block) is one contiguous run
@@ -102,6 +109,39 @@ struct KGeom {
   static constexpr size_t SMEM = (size_t)(N + KW * LineGeom<N>::LS) * sizeof(float2);
 };
 
+// One column of a b-axis tile for all K radii (loads via L2 only: in the
+// fused kernel the data were written by other CTAs of the same launch).
+template <int N>
+__device__ __forceinline__ void cols_b_column(const Batch& bt, const float2* stw, float2* sline, long off, int j) {
+  using G = CbGeom<N>;
+  auto load = [&](float2 (&v)[8], int k) {
+    const float2* box = bt.r[k].work + off;
+#pragma unroll
+    for (int r = 0; r < 8; ++r) v[r] = __ldcg(box + (j + r * (N / 8)) * G::CW);
+  };
+  auto store = [&](const float2 (&v)[8], int k) {
+    float2* box = bt.r[k].work + off;
+#pragma unroll
+    for (int r = 0; r < 8; ++r) box[(j + r * (N / 8)) * G::CW] = v[r];
+  };
+  // two register sets in turn: the loads of radius k + 1 are in flight during
+  // the transform of radius k
+  float2 va[8], vb[8];
+  load(va, 0);
+  for (int k = 0; k < bt.K; k += 2) {
+    if (k + 1 < bt.K) load(vb, k + 1);
+    __syncthreads();
+    fft_line<N, true>(va, sline, stw, j);
+    store(va, k);
+    if (k + 1 < bt.K) {
+      if (k + 2 < bt.K) load(va, k + 2);
+      __syncthreads();
+      fft_line<N, true>(vb, sline, stw, j);
+      store(vb, k + 1);
+    }
+  }
+}
+
 template <int N>
 __global__ void __launch_bounds__(KGeom<N>::THREADS, (KGeom<N>::THREADS <= 512 ? 2 : 1))
 k_cols_b_cb(Batch bt, const float2* __restrict__ gtw) {
@@ -117,24 +157,102 @@ k_cols_b_cb(Batch bt, const float2* __restrict__ gtw) {
   const int col = threadIdx.x % X::KW;
   const int j = threadIdx.x / X::KW;
   const long off = (long)tile * N * G::CW + half * X::KW + col;  // element (b = 0) of this column
-  float2 v[8], nx[8];
-#pragma unroll
-  for (int r = 0; r < 8; ++r) v[r] = bt.r[0].work[off + (j + r * (N / 8)) * G::CW];
-  for (int k = 0; k < bt.K; ++k) {
-    if (k + 1 < bt.K) {
-      const float2* nbox = bt.r[k + 1].work + off;
-#pragma unroll
-      for (int r = 0; r < 8; ++r) nx[r] = nbox[(j + r * (N / 8)) * G::CW];
-    }
+  cols_b_column<N>(bt, stw, sbuf + col * L::LS, off, j);
+}
+
+// ---------------------------------------------------------------------------
+// Fused c-axis filter pass + b-axis pass through L2 (pipeline 8).  One
+// persistent CTA per SM takes tasks from a queue in a fixed order: the row
+// tasks of kx plane s (CW rows each, all K radii) and, DELAY planes behind,
+// the column tasks of plane s - DELAY (one column block, all K radii).  A
+// column task waits until every row task of its plane has published its
+// rows (per-plane counter, release/acquire), so the plane's K work slices
+// are read back while they are still in L2: the b-axis pass costs no HBM
+// traffic beyond the final write-back.  Row tasks never wait and tasks are
+// taken in queue order, so every task a column task waits for is already
+// held by a running CTA: no deadlock whatever the residency.  Each wait is
+// bounded; on expiry the CTA records the error in *err and carries on.
+// ctl: [0] queue head, [1 + a] row tasks finished in plane a (N + 1 ints,
+// zeroed before each launch).
+
+__device__ __forceinline__ int ld_acquire_gpu(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+template <int N>
+__global__ void __launch_bounds__(KGeom<N>::THREADS, 1)
+k_rows_cols_b_fused(const float2* __restrict__ spec, Batch bt, const float2* __restrict__ gtw, int* ctl,
+                    int delay, int* __restrict__ err) {
+  using G = CbGeom<N>;
+  using L = LineGeom<N>;
+  constexpr int T = KGeom<N>::THREADS;   // = CW N/8
+  constexpr int NB = G::NBLK;            // row tasks and column tasks per plane
+  extern __shared__ float2 dsm[];
+  float2* stw = dsm;
+  float2* sbuf = dsm + N;
+  __shared__ int s_task;
+  for (int t = threadIdx.x; t < N; t += blockDim.x) stw[t] = gtw[t];
+  int* next = ctl;
+  int* done = ctl + 1;
+  const long total = 2L * N * NB;
+  const long lead = (long)delay * NB;                // leading row tasks
+  const long mid = 2L * NB * (N - delay);            // interleaved steps
+  for (;;) {
+    __syncthreads();  // s_task free, previous task's exchanges done
+    if (threadIdx.x == 0) s_task = atomicAdd(next, 1);
     __syncthreads();
-    fft_line<N, true>(v, sbuf + col * L::LS, stw, j);
-    float2* box = bt.r[k].work + off;
-#pragma unroll
-    for (int r = 0; r < 8; ++r) box[(j + r * (N / 8)) * G::CW] = v[r];
-#pragma unroll
-    for (int r = 0; r < 8; ++r) v[r] = nx[r];
+    const long t = s_task;
+    if (t >= total) break;
+    bool row_task;
+    int plane, blk;
+    if (t < lead) {
+      row_task = true;
+      plane = (int)(t / NB);
+      blk = (int)(t % NB);
+    } else if (t < lead + mid) {
+      const long u = t - lead;
+      const long step = u / (2 * NB), w = u % (2 * NB);
+      row_task = w < NB;
+      plane = row_task ? (int)(step + delay) : (int)step;
+      blk = (int)(w % NB);
+    } else {
+      const long v = t - lead - mid;
+      row_task = false;
+      plane = (int)(N - delay + v / NB);
+      blk = (int)(v % NB);
+    }
+    if (row_task) {
+      // rows b = blk CW .. blk CW + CW - 1 of plane `plane`
+      const int row_in = threadIdx.x / (N / 8);
+      const int j = threadIdx.x % (N / 8);
+      rows_filter_row<N>(spec, bt, stw, sbuf + row_in * L::LS, plane, blk * G::CW + row_in, j);
+      __threadfence();
+      __syncthreads();
+      if (threadIdx.x == 0) atomicAdd(done + plane, 1);
+    } else {
+      if (threadIdx.x == 0) {
+        bool ok = false;
+        for (uint32_t it = 0; it < (1u << 22); ++it) {
+          if (ld_acquire_gpu(done + plane) >= NB) {
+            ok = true;
+            break;
+          }
+          __nanosleep(64);
+        }
+        if (!ok) atomicExch(err, 2);
+      }
+      __syncthreads();
+      __threadfence();
+      const int col = threadIdx.x % G::CW;
+      const int j = threadIdx.x / G::CW;
+      const long off = ((long)blk * N + plane) * N * G::CW + col;
+      cols_b_column<N>(bt, stw, sbuf + col * L::LS, off, j);
+    }
   }
 }
+
 
 // a-axis inverse pass of the K radii + centre test + first-hit update
 // (get_HIIbubbles.c:335-352; for floats h, d > 0, (double)h/d >= 1 <=> h >= d).
@@ -163,36 +281,47 @@ k_cols_a_test_cb(Batch bt, uint8_t* __restrict__ rc, const float* __restrict__ a
   const int cc = half * X::KW + col;                       // column within the block
   const long base = ((long)cb * N * N + b) * G::CW + cc;    // element (a = 0, b, cb CW + cc)
   const long astride = (long)N * G::CW;
-  uint32_t hit_lo = 0xFFFFFFFFu, hit_hi = 0xFFFFFFFFu;      // 8 first-hit bytes
-  float2 v[8], nx[8];
-#pragma unroll
-  for (int r = 0; r < 8; ++r) v[r] = bt.r[0].work[base + (long)(j + r * (N / 8)) * astride];
-  for (int k = 0; k < bt.K; ++k) {
-    if (k + 1 < bt.K) {
-      const float2* nbox = bt.r[k + 1].work + base;
-#pragma unroll
-      for (int r = 0; r < 8; ++r) nx[r] = nbox[(long)(j + r * (N / 8)) * astride];
-    }
-    __syncthreads();
-    fft_line<N, true>(v, sbuf + col * L::LS, stw, j);
-    const uint32_t ridx = (uint32_t)bt.r[k].ridx;
+  // bit 8 (r & 3) + k of m[r / 4]: element r is a centre at radius k of the
+  // batch (radius indices increase with k, so the lowest bit is the first hit)
+  uint32_t m[2] = {0u, 0u};
+  const float zmul = bt.zmul;
+  auto test = [&](const float2 (&v)[8], int k) {
+    const uint32_t bit = 1u << k;
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
       const float rec = v[r].x * alpha;  // alpha * rec_R (exact: power of two)
-      const float ion = v[r].y * bt.zmul;
+      const float ion = v[r].y * zmul;
       const bool centre = (v[r].y > 0.0f) && (!(rec > 0.0f) || ion >= rec);
-      uint32_t& h = r < 4 ? hit_lo : hit_hi;
-      const int sh = 8 * (r & 3);
-      if (centre && ridx < ((h >> sh) & 0xFFu)) h = (h & ~(0xFFu << sh)) | (ridx << sh);
+      if (centre) m[r >> 2] |= bit << (8 * (r & 3));
     }
+  };
+  auto load = [&](float2 (&v)[8], int k) {
+    const float2* box = bt.r[k].work + base;
 #pragma unroll
-    for (int r = 0; r < 8; ++r) v[r] = nx[r];
+    for (int r = 0; r < 8; ++r) v[r] = box[(long)(j + r * (N / 8)) * astride];
+  };
+  // two register sets in turn: the loads of radius k + 1 are in flight during
+  // the transform of radius k
+  float2 va[8], vb[8];
+  load(va, 0);
+  for (int k = 0; k < bt.K; k += 2) {
+    if (k + 1 < bt.K) load(vb, k + 1);
+    __syncthreads();
+    fft_line<N, true>(va, sbuf + col * L::LS, stw, j);
+    test(va, k);
+    if (k + 1 < bt.K) {
+      if (k + 2 < bt.K) load(va, k + 2);
+      __syncthreads();
+      fft_line<N, true>(vb, sbuf + col * L::LS, stw, j);
+      test(vb, k + 1);
+    }
   }
   const int c = cb * G::CW + cc;
 #pragma unroll
   for (int r = 0; r < 8; ++r) {
-    const uint32_t h = ((r < 4 ? hit_lo : hit_hi) >> (8 * (r & 3))) & 0xFFu;
-    if (h != RC_NONE) {
+    const uint32_t byte = (m[r >> 2] >> (8 * (r & 3))) & 0xFFu;
+    if (byte) {
+      const uint32_t h = (uint32_t)bt.r[__ffs(byte) - 1].ridx;
       const long idx = ((long)(j + r * (N / 8)) * N + b) * N + c;
       const uint8_t old = rc[idx];
       if (h < old) rc[idx] = (uint8_t)h;
@@ -207,6 +336,9 @@ struct CbLaunch {
     cudaError_t e;
     if ((e = cudaFuncSetAttribute(k_cols_b_cb<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)KGeom<N>::SMEM)))
       return e;
+    if ((e = cudaFuncSetAttribute(k_rows_cols_b_fused<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)fused_smem())))
+      return e;
     return cudaFuncSetAttribute(k_cols_a_test_cb<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)KGeom<N>::SMEM);
   }
@@ -217,6 +349,15 @@ struct CbLaunch {
   static cudaError_t cols_b(const Batch& bt, const float2* tw, cudaStream_t st) {
     using X = KGeom<N>;
     k_cols_b_cb<N><<<(unsigned)((long)N * G::NBLK * X::SPLIT), X::THREADS, X::SMEM, st>>>(bt, tw);
+    return cudaGetLastError();
+  }
+  static size_t fused_smem() { return (size_t)(N + G::CW * LineGeom<N>::LS) * sizeof(float2); }
+  static cudaError_t fused(const float2* spec, const Batch& bt, const float2* tw, int* ctl, int delay, int* err,
+                           int nsm, cudaStream_t st) {
+    if (KGeom<N>::THREADS != G::CW * (N / 8) || delay < 1 || delay >= N) return cudaErrorInvalidValue;
+    cudaError_t e = cudaMemsetAsync(ctl, 0, sizeof(int) * (N + 1), st);
+    if (e != cudaSuccess) return e;
+    k_rows_cols_b_fused<N><<<nsm, KGeom<N>::THREADS, fused_smem(), st>>>(spec, bt, tw, ctl, delay, err);
     return cudaGetLastError();
   }
   static cudaError_t cols_a_test(const Batch& bt, uint8_t* rc, const float* alpha, const float2* tw,
@@ -245,6 +386,10 @@ cudaError_t launch_rows_filter_cb(int N, const float2* spec, const Batch& bt, co
 }
 cudaError_t launch_cols_b_cb(int N, const Batch& bt, const float2* tw, cudaStream_t st) {
   SF21_CB_DISPATCH(N, LL::cols_b(bt, tw, st));
+}
+cudaError_t launch_rows_cols_b_fused(int N, const float2* spec, const Batch& bt, const float2* tw, int* ctl, int delay,
+                                    int* err, int nsm, cudaStream_t st) {
+  SF21_CB_DISPATCH(N, LL::fused(spec, bt, tw, ctl, delay, err, nsm, st));
 }
 cudaError_t launch_cols_a_test_cb(int N, const Batch& bt, uint8_t* rc, const float* alpha, const float2* tw,
                                   cudaStream_t st) {

@@ -19,7 +19,7 @@ struct RadiusArg {
   float2* work;   // N^3 complex work buffer for this radius
 };
 
-struct Batch {
+struct Batch {    // radius indices r[k].ridx increase with k
   int K;          // radii in this batch (<= KMAX)
   int set;        // parameter set
   float zmul;     // ionisation-rate multiplier of the set (zeta)
