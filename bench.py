@@ -198,7 +198,6 @@ PIPELINES = {
     5: ("cb_three_pass", "column-block-major work boxes, three axis passes"),
     6: ("cb_tma_ky", "column-block-major work boxes, ky pass TMA-pipelined"),
     7: ("cb_tma_ky_kx", "column-block-major work boxes, ky and kx passes TMA-pipelined"),
-    8: ("cb_fused_rows_ky", "column-block-major work boxes, filter + ky pass fused through L2, kx pass"),
 }
 
 

@@ -170,6 +170,78 @@ __device__ __forceinline__ void fft_line(float2 (&v)[8], float2* s, const float2
   }
 }
 
+// The same with two exchange buffers used in turn (s0, s1: LineGeom<N>::LS
+// float2 each): one barrier per exchange instead of two.  A buffer is written
+// only after the barrier that follows the last read of it, so when the
+// number of exchanges per call is even (N = 128, 256, 512) consecutive calls
+// need no barrier between them; for an odd count (FftPP<N>::CALL_SYNC) the
+// caller keeps a __syncthreads() before each call.
+template <int N>
+struct FftPP {
+  static constexpr int LOG = LineGeom<N>::LOG;
+  static constexpr int Q = LOG / 3;
+  static constexpr int RB = LOG % 3;
+  static constexpr int EXCH = (RB == 0) ? Q - 1 : Q;  // shared-memory exchanges per call
+  static constexpr bool CALL_SYNC = (EXCH % 2) != 0;
+};
+
+template <int N, bool INV>
+__device__ __forceinline__ void fft_line_pp(float2 (&v)[8], float2* s0, float2* s1, const float2* tw, int j) {
+  constexpr int Q = FftPP<N>::Q;
+  constexpr int RB = FftPP<N>::RB;
+  constexpr int N8 = N / 8;
+  int Ns = 1;
+  float2* cur = s0;  // buffer written by the next exchange
+#pragma unroll
+  for (int st = 0; st < Q; ++st) {
+    if (st > 0) {
+      float2* prev = (st & 1) ? s0 : s1;  // written by the previous exchange
+#pragma unroll
+      for (int r = 0; r < 8; ++r) v[r] = prev[padx(j + r * N8)];
+      const int jm = j & (Ns - 1);
+      const float2* tws = tw + tw_stage_off(st);
+#pragma unroll
+      for (int r = 1; r < 8; ++r) v[r] = cmul(v[r], twid<INV>(tws, (r - 1) * Ns + jm));
+    }
+    dft8<INV>(v);
+    const bool keep = (st == Q - 1) && (RB == 0);
+    if (!keep) {
+      cur = (st & 1) ? s1 : s0;
+      const int base = (j / Ns) * Ns * 8 + (j & (Ns - 1));
+#pragma unroll
+      for (int r = 0; r < 8; ++r) cur[padx(base + r * Ns)] = v[r];
+      __syncthreads();
+    }
+    Ns *= 8;
+  }
+  const float2* s = cur;
+  if (RB == 1) {
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      const int j2 = j + m * N8;
+      float2 a = s[padx(j2)];
+      float2 b = cmul(s[padx(j2 + N / 2)], twid<INV>(tw + tw_tail_off(N), j2));
+      v[m] = cadd(a, b);
+      v[m + 4] = csub(a, b);
+    }
+  } else if (RB == 2) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int j4 = j + h * N8;
+      const float2* twt = tw + tw_tail_off(N);
+      float2 a0 = s[padx(j4)];
+      float2 a1 = cmul(s[padx(j4 + N / 4)], twid<INV>(twt, j4));
+      float2 a2 = cmul(s[padx(j4 + N / 2)], twid<INV>(twt, N / 4 + j4));
+      float2 a3 = cmul(s[padx(j4 + 3 * N / 4)], twid<INV>(twt, N / 2 + j4));
+      dft4<INV>(a0, a1, a2, a3);
+      v[0 + h] = a0;
+      v[2 + h] = a1;
+      v[4 + h] = a2;
+      v[6 + h] = a3;
+    }
+  }
+}
+
 // Host: the twiddle table of an N-point line in the layout above (N entries,
 // the unused tail is zero).  out[t] = (cos, sin) of the angle, in double.
 inline void twiddle_layout(int N, double* re, double* im) {

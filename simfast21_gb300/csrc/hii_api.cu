@@ -62,17 +62,8 @@ struct SetInfo {
 
 // Radius pipelines: 1 three axis passes, 2 plane clusters + kx pass,
 // 3 TMA ky + kx pass, 4 TMA ky + TMA kx, and over column-block-major work
-// boxes: 5 three axis passes, 6 TMA ky + kx pass, 7 TMA ky + TMA kx,
-// 8 fused filter + ky pass through L2 + kx pass.
-constexpr int NPATH = 8;
-// Planes between a plane's row tasks and its column tasks in the fused
-// pipeline: enough for the row tasks to finish first, few enough that the
-// (DELAY + 1) planes x K slices in flight stay well inside L2 (~24 MB).
-static int fused_delay(long N, int K) {
-  const double plane_bytes = (double)K * N * N * 8.0;
-  int d = (int)(24.0e6 / plane_bytes);
-  return d < 2 ? 2 : (d > 8 ? 8 : d);
-}
+// boxes: 5 three axis passes, 6 TMA ky + kx pass, 7 TMA ky + TMA kx.
+constexpr int NPATH = 7;
 
 struct sf21_hii_ctx {
   int device = 0;
@@ -99,6 +90,11 @@ struct sf21_hii_ctx {
   int nsm = 0;
   std::vector<SetInfo> sets;
   cudaStream_t stream = nullptr;
+  // host-buffer entry points: downloads of set s overlap the compute of set
+  // s + 1 (second stream, two staging boxes used in turn)
+  cudaStream_t copy_stream = nullptr;
+  float* d_xhii2 = nullptr;
+  cudaEvent_t ev_done[2] = {nullptr, nullptr}, ev_copied[2] = {nullptr, nullptr};
   float *d_delta = nullptr, *d_src = nullptr, *d_rec0 = nullptr, *d_fres = nullptr;
   uint64_t* d_chain = nullptr;  // source chain before zeta (double bits), per redshift
   float2* d_om = nullptr;       // 1 - fresid rounded down / to nearest, per redshift
@@ -124,7 +120,6 @@ struct sf21_hii_ctx {
   float2 *d_spec = nullptr, *d_tw = nullptr;
   std::vector<float2*> d_work;
   uint8_t* d_rc = nullptr;
-  int* d_fctl = nullptr;  // queue + per-plane counters of the fused pipeline
   PrologueArgs pa;   // scalars of the redshift being processed (kernel arguments)
   int pro_blocks = 0;
   std::string err;
@@ -216,7 +211,7 @@ static void free_ctx(sf21_hii_ctx* c) {
   void* ptrs[] = {c->d_delta, c->d_src, c->d_rec0, c->d_fres, c->d_partials, c->d_alpha,
                   c->d_xhii, c->d_spec, c->d_tw, c->d_rc, c->d_mask, c->d_flag, c->d_box2,
                   c->d_C, c->d_A, c->d_acc, c->d_zpart, c->d_g, c->d_gd, c->d_gs, c->d_halos, c->d_fine,
-                  c->d_hscratch, c->d_chain, c->d_om, c->d_fctl};
+                  c->d_hscratch, c->d_chain, c->d_om, c->d_xhii2};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->d_work_base) cudaFree(c->d_work_base);
@@ -225,6 +220,11 @@ static void free_ctx(sf21_hii_ctx* c) {
     if (s.d_nmax) cudaFree(s.d_nmax);
   for (cudaEvent_t e : c->ev) cudaEventDestroy(e);
   if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  for (int i = 0; i < 2; ++i) {
+    if (c->ev_done[i]) cudaEventDestroy(c->ev_done[i]);
+    if (c->ev_copied[i]) cudaEventDestroy(c->ev_copied[i]);
+  }
+  if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -331,7 +331,6 @@ extern "C" int sf21_hii_create(const sf21_hii_config* cfg, sf21_hii_ctx** out) {
   CREATE_CUDA(cudaMalloc(&c->d_xhii, box_f));
   CREATE_CUDA(cudaMalloc(&c->d_spec, box_c));
   CREATE_CUDA(cudaMalloc(&c->d_rc, c->n3));
-  CREATE_CUDA(cudaMalloc(&c->d_fctl, sizeof(int) * (N + 1)));
   c->d_work.assign(K, nullptr);
   CREATE_CUDA(cudaMalloc(&c->d_work_base, box_c * K));
   for (int k = 0; k < K; ++k) c->d_work[k] = c->d_work_base + (size_t)k * c->n3;
@@ -492,12 +491,9 @@ static int enqueue_batch(sf21_hii_ctx* c, const Batch& bt, cudaStream_t st) {
   }
   if (c->path >= 5) {  // column-block-major work boxes
     int e0 = mark(c, st);
-    if (c->path != 8) CTX_CUDA(c, launch_rows_filter_cb(N, c->d_spec, bt, c->d_tw, st));
-    int e1 = mark(c, st);  // pipeline 8: the filter pass is inside the fused kernel below
-    if (c->path == 8)
-      CTX_CUDA(c, launch_rows_cols_b_fused(N, c->d_spec, bt, c->d_tw, c->d_fctl, fused_delay(N, bt.K), c->d_err,
-                                           c->nsm, st));
-    else if (c->path == 5)
+    CTX_CUDA(c, launch_rows_filter_cb(N, c->d_spec, bt, c->d_tw, st));
+    int e1 = mark(c, st);
+    if (c->path == 5)
       CTX_CUDA(c, launch_cols_b_cb(N, bt, c->d_tw, st));
     else
       CTX_CUDA(c, launch_pipe(N, 0, 1, c->pmaps, bt, c->d_work_base, c->d_rc, c->d_alpha, c->d_tw, c->d_err,
@@ -651,6 +647,82 @@ extern "C" int sf21_hii_run_z_device(sf21_hii_ctx* c, double z, int kind, const 
   return SF21_OK;
 }
 
+// Radius loops and finish of every set, with each xHII box downloaded to
+// the host while the GPU works on the next set: set s is written into
+// staging box s mod 2 on the compute stream, copied out on the copy stream,
+// and the staging box is reused only after its copy has completed.  Each
+// set's neutral fraction is the serial double sum of the reference
+// (:473-477), on a host thread once the box has arrived.
+static int run_sets_to_host(sf21_hii_ctx* c, cudaStream_t st, float* xhii, double* neutral) {
+  const size_t bf = sizeof(float) * c->n3;
+  if (!c->copy_stream) {
+    CTX_CUDA(c, cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+    for (int i = 0; i < 2; ++i) {
+      CTX_CUDA(c, cudaEventCreateWithFlags(&c->ev_done[i], cudaEventDisableTiming));
+      CTX_CUDA(c, cudaEventCreateWithFlags(&c->ev_copied[i], cudaEventDisableTiming));
+    }
+  }
+  if (!c->d_xhii2) CTX_CUDA(c, cudaMalloc(&c->d_xhii2, bf));
+  float* stage[2] = {c->d_xhii, c->d_xhii2};
+  std::vector<std::thread> sums;
+  int status = SF21_OK;
+  const int ns = (int)c->sets.size();
+  auto start_sum = [&](int s) {
+    if (!neutral) return;
+    const float* dst = xhii + (size_t)s * c->n3;
+    const long n3 = c->n3;
+    double* out = neutral + s;
+    sums.emplace_back([dst, n3, out]() {
+      double acc = 0.;
+      for (long i = 0; i < n3; ++i) acc += 1.0 - dst[i];
+      *out = acc / n3;
+    });
+  };
+  int copied = 0;  // sets whose download has been waited for
+  for (int s = 0; s < ns && status == SF21_OK; ++s) {
+    const int b = s & 1;
+    cudaError_t e = cudaSuccess;
+    if (s >= 2) e = cudaStreamWaitEvent(st, c->ev_copied[b], 0);  // staging box free again
+    if (e == cudaSuccess && (status = enqueue_radii(c, s, st)) == SF21_OK &&
+        (status = enqueue_finish(c, s, stage[b], st)) == SF21_OK) {
+      e = cudaEventRecord(c->ev_done[b], st);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(c->copy_stream, c->ev_done[b], 0);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(xhii + (size_t)s * c->n3, stage[b], bf, cudaMemcpyDeviceToHost, c->copy_stream);
+      if (e == cudaSuccess) e = cudaEventRecord(c->ev_copied[b], c->copy_stream);
+      // the previous set's box has been on its way while this set was enqueued
+      if (e == cudaSuccess && s >= 1) {
+        e = cudaEventSynchronize(c->ev_copied[(s - 1) & 1]);
+        if (e == cudaSuccess) start_sum(copied++);
+      }
+    }
+    if (e != cudaSuccess) {
+      c->err = std::string("xHII download failed: ") + cudaGetErrorString(e);
+      status = SF21_E_CUDA;
+    }
+  }
+  if (status == SF21_OK && copied < ns) {
+    cudaError_t e = cudaEventSynchronize(c->ev_copied[(ns - 1) & 1]);
+    if (e == cudaSuccess) {
+      start_sum(copied++);
+    } else {
+      c->err = std::string("xHII download failed: ") + cudaGetErrorString(e);
+      status = SF21_E_CUDA;
+    }
+  }
+  cudaStreamSynchronize(c->copy_stream);
+  for (std::thread& t : sums) t.join();
+  if (status == SF21_OK) {
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+      c->err = std::string("stream failed: ") + cudaGetErrorString(e);
+      status = SF21_E_CUDA;
+    }
+  }
+  if (status == SF21_OK) status = check_device_flag(c);
+  return status;
+}
+
 extern "C" int sf21_hii_run_z(sf21_hii_ctx* c, double z, int kind, const float* delta, const float* src,
                               float* xhii, double* neutral) {
   int rc = check_run_args(c, kind, delta, src, xhii);
@@ -661,34 +733,7 @@ extern "C" int sf21_hii_run_z(sf21_hii_ctx* c, double z, int kind, const float* 
   CTX_CUDA(c, cudaMemcpyAsync(c->d_delta, delta, bf, cudaMemcpyHostToDevice, st));
   CTX_CUDA(c, cudaMemcpyAsync(c->d_src, src, bf, cudaMemcpyHostToDevice, st));
   if ((rc = enqueue_front(c, z, kind, c->d_delta, c->d_src, st))) return rc;
-  // Each set's neutral fraction is the serial double sum of the reference
-  // (:473-477); it runs on a host thread while the GPU works on the next set.
-  std::vector<std::thread> sums;
-  int status = SF21_OK;
-  for (int s = 0; s < (int)c->sets.size() && status == SF21_OK; ++s) {
-    if ((status = enqueue_radii(c, s, st))) break;
-    if ((status = enqueue_finish(c, s, c->d_xhii, st))) break;
-    float* dst = xhii + (size_t)s * c->n3;
-    cudaError_t e = cudaMemcpyAsync(dst, c->d_xhii, bf, cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) {
-      c->err = std::string("xHII download failed: ") + cudaGetErrorString(e);
-      status = SF21_E_CUDA;
-      break;
-    }
-    if (neutral) {
-      const long n3 = c->n3;
-      double* out = neutral + s;
-      sums.emplace_back([dst, n3, out]() {
-        double acc = 0.;
-        for (long i = 0; i < n3; ++i) acc += 1.0 - dst[i];
-        *out = acc / n3;
-      });
-    }
-  }
-  for (std::thread& t : sums) t.join();
-  if (status == SF21_OK) status = check_device_flag(c);
-  return status;
+  return run_sets_to_host(c, st, xhii, neutral);
 }
 
 // ---- check hooks -------------------------------------------------------------
@@ -1090,30 +1135,5 @@ extern "C" int sf21_hii_run_z_halos(sf21_hii_ctx* c, double z, const float* delt
   if (rc) return rc;
   CTX_CUDA(c, cudaMemcpyAsync(c->d_delta, delta, bf, cudaMemcpyHostToDevice, st));
   if ((rc = enqueue_front(c, z, SF21_SRC_RION, c->d_delta, c->d_src, st))) return rc;
-  std::vector<std::thread> sums;
-  int status = SF21_OK;
-  for (int s = 0; s < (int)c->sets.size() && status == SF21_OK; ++s) {
-    if ((status = enqueue_radii(c, s, st))) break;
-    if ((status = enqueue_finish(c, s, c->d_xhii, st))) break;
-    float* dst = xhii + (size_t)s * c->n3;
-    cudaError_t e = cudaMemcpyAsync(dst, c->d_xhii, bf, cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) {
-      c->err = std::string("xHII download failed: ") + cudaGetErrorString(e);
-      status = SF21_E_CUDA;
-      break;
-    }
-    if (neutral) {
-      const long n3 = c->n3;
-      double* out = neutral + s;
-      sums.emplace_back([dst, n3, out]() {
-        double acc = 0.;
-        for (long i = 0; i < n3; ++i) acc += 1.0 - dst[i];
-        *out = acc / n3;
-      });
-    }
-  }
-  for (std::thread& t : sums) t.join();
-  if (status == SF21_OK) status = check_device_flag(c);
-  return status;
+  return run_sets_to_host(c, st, xhii, neutral);
 }

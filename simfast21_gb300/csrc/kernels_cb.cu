@@ -42,7 +42,7 @@ __device__ __forceinline__ long cb_index(int a, int b, int c) {
 // (j = thread index in the row, sline = this row's exchange line).
 template <int N>
 __device__ __forceinline__ void rows_filter_row(const float2* __restrict__ spec, const Batch& bt,
-                                                const float2* stw, float2* sline, int a, int b, int j) {
+                                                const float2* stw, float2* s0, float2* s1, int a, int b, int j) {
   using G = CbGeom<N>;
   const int ka = kfreq(a, N), kb = kfreq(b, N);
   const int kab = ka * ka + kb * kb;
@@ -65,7 +65,8 @@ __device__ __forceinline__ void rows_filter_row(const float2* __restrict__ spec,
       const float w = w_tophat(dkR * kmag[r]);
       v[r] = make_float2(z[r].x * w, z[r].y * w);
     }
-    fft_line<N, true>(v, sline, stw, j);
+    if (FftPP<N>::CALL_SYNC) __syncthreads();
+    fft_line_pp<N, true>(v, s0, s1, stw, j);
     if constexpr ((N / 8) % G::CW == 0) {
       // c = j + r N/8: column block j/CW + r (N/8)/CW, offset j mod CW
       float2* dst = bt.r[k].work + cb_index<N>(a, b, j);
@@ -86,12 +87,13 @@ k_rows_filter_cb(const float2* __restrict__ spec, Batch bt, const float2* __rest
   using G = CbGeom<N>;
   using L = LineGeom<N>;
   __shared__ float2 stw[N];
-  __shared__ float2 sbuf[G::ROWS * L::LS];
+  __shared__ float2 sbuf[2 * G::ROWS * L::LS];  // two exchange lines per row
   for (int t = threadIdx.x; t < N; t += blockDim.x) stw[t] = gtw[t];
   const int row_in_cta = threadIdx.x / G::RT;
   const int j = threadIdx.x % G::RT;
   const long row = (long)blockIdx.x * G::ROWS + row_in_cta;
-  rows_filter_row<N>(spec, bt, stw, sbuf + row_in_cta * L::LS, (int)(row / N), (int)(row % N), j);
+  rows_filter_row<N>(spec, bt, stw, sbuf + row_in_cta * L::LS, sbuf + (G::ROWS + row_in_cta) * L::LS,
+                     (int)(row / N), (int)(row % N), j);
 }
 
 // b-axis inverse pass in place: tile (a, column block) is one contiguous run
@@ -106,18 +108,18 @@ struct KGeom {
   static constexpr int KW = CbGeom<N>::CW;  // columns per CTA
   static constexpr int SPLIT = CbGeom<N>::CW / KW;
   static constexpr int THREADS = KW * (N / 8);
-  static constexpr size_t SMEM = (size_t)(N + KW * LineGeom<N>::LS) * sizeof(float2);
+  static constexpr size_t SMEM = (size_t)(N + 2 * KW * LineGeom<N>::LS) * sizeof(float2);  // two lines each
 };
 
-// One column of a b-axis tile for all K radii (loads via L2 only: in the
-// fused kernel the data were written by other CTAs of the same launch).
+// One column of a b-axis tile for all K radii.
 template <int N>
-__device__ __forceinline__ void cols_b_column(const Batch& bt, const float2* stw, float2* sline, long off, int j) {
+__device__ __forceinline__ void cols_b_column(const Batch& bt, const float2* stw, float2* s0, float2* s1, long off,
+                                              int j) {
   using G = CbGeom<N>;
   auto load = [&](float2 (&v)[8], int k) {
     const float2* box = bt.r[k].work + off;
 #pragma unroll
-    for (int r = 0; r < 8; ++r) v[r] = __ldcg(box + (j + r * (N / 8)) * G::CW);
+    for (int r = 0; r < 8; ++r) v[r] = box[(j + r * (N / 8)) * G::CW];
   };
   auto store = [&](const float2 (&v)[8], int k) {
     float2* box = bt.r[k].work + off;
@@ -128,15 +130,16 @@ __device__ __forceinline__ void cols_b_column(const Batch& bt, const float2* stw
   // the transform of radius k
   float2 va[8], vb[8];
   load(va, 0);
+  __syncthreads();  // twiddles and the previous use of the exchange lines
   for (int k = 0; k < bt.K; k += 2) {
     if (k + 1 < bt.K) load(vb, k + 1);
-    __syncthreads();
-    fft_line<N, true>(va, sline, stw, j);
+    if (FftPP<N>::CALL_SYNC && k > 0) __syncthreads();
+    fft_line_pp<N, true>(va, s0, s1, stw, j);
     store(va, k);
     if (k + 1 < bt.K) {
       if (k + 2 < bt.K) load(va, k + 2);
-      __syncthreads();
-      fft_line<N, true>(vb, sline, stw, j);
+      if (FftPP<N>::CALL_SYNC) __syncthreads();
+      fft_line_pp<N, true>(vb, s0, s1, stw, j);
       store(vb, k + 1);
     }
   }
@@ -157,102 +160,8 @@ k_cols_b_cb(Batch bt, const float2* __restrict__ gtw) {
   const int col = threadIdx.x % X::KW;
   const int j = threadIdx.x / X::KW;
   const long off = (long)tile * N * G::CW + half * X::KW + col;  // element (b = 0) of this column
-  cols_b_column<N>(bt, stw, sbuf + col * L::LS, off, j);
+  cols_b_column<N>(bt, stw, sbuf + col * L::LS, sbuf + (X::KW + col) * L::LS, off, j);
 }
-
-// ---------------------------------------------------------------------------
-// Fused c-axis filter pass + b-axis pass through L2 (pipeline 8).  One
-// persistent CTA per SM takes tasks from a queue in a fixed order: the row
-// tasks of kx plane s (CW rows each, all K radii) and, DELAY planes behind,
-// the column tasks of plane s - DELAY (one column block, all K radii).  A
-// column task waits until every row task of its plane has published its
-// rows (per-plane counter, release/acquire), so the plane's K work slices
-// are read back while they are still in L2: the b-axis pass costs no HBM
-// traffic beyond the final write-back.  Row tasks never wait and tasks are
-// taken in queue order, so every task a column task waits for is already
-// held by a running CTA: no deadlock whatever the residency.  Each wait is
-// bounded; on expiry the CTA records the error in *err and carries on.
-// ctl: [0] queue head, [1 + a] row tasks finished in plane a (N + 1 ints,
-// zeroed before each launch).
-
-__device__ __forceinline__ int ld_acquire_gpu(const int* p) {
-  int v;
-  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-
-template <int N>
-__global__ void __launch_bounds__(KGeom<N>::THREADS, 1)
-k_rows_cols_b_fused(const float2* __restrict__ spec, Batch bt, const float2* __restrict__ gtw, int* ctl,
-                    int delay, int* __restrict__ err) {
-  using G = CbGeom<N>;
-  using L = LineGeom<N>;
-  constexpr int T = KGeom<N>::THREADS;   // = CW N/8
-  constexpr int NB = G::NBLK;            // row tasks and column tasks per plane
-  extern __shared__ float2 dsm[];
-  float2* stw = dsm;
-  float2* sbuf = dsm + N;
-  __shared__ int s_task;
-  for (int t = threadIdx.x; t < N; t += blockDim.x) stw[t] = gtw[t];
-  int* next = ctl;
-  int* done = ctl + 1;
-  const long total = 2L * N * NB;
-  const long lead = (long)delay * NB;                // leading row tasks
-  const long mid = 2L * NB * (N - delay);            // interleaved steps
-  for (;;) {
-    __syncthreads();  // s_task free, previous task's exchanges done
-    if (threadIdx.x == 0) s_task = atomicAdd(next, 1);
-    __syncthreads();
-    const long t = s_task;
-    if (t >= total) break;
-    bool row_task;
-    int plane, blk;
-    if (t < lead) {
-      row_task = true;
-      plane = (int)(t / NB);
-      blk = (int)(t % NB);
-    } else if (t < lead + mid) {
-      const long u = t - lead;
-      const long step = u / (2 * NB), w = u % (2 * NB);
-      row_task = w < NB;
-      plane = row_task ? (int)(step + delay) : (int)step;
-      blk = (int)(w % NB);
-    } else {
-      const long v = t - lead - mid;
-      row_task = false;
-      plane = (int)(N - delay + v / NB);
-      blk = (int)(v % NB);
-    }
-    if (row_task) {
-      // rows b = blk CW .. blk CW + CW - 1 of plane `plane`
-      const int row_in = threadIdx.x / (N / 8);
-      const int j = threadIdx.x % (N / 8);
-      rows_filter_row<N>(spec, bt, stw, sbuf + row_in * L::LS, plane, blk * G::CW + row_in, j);
-      __threadfence();
-      __syncthreads();
-      if (threadIdx.x == 0) atomicAdd(done + plane, 1);
-    } else {
-      if (threadIdx.x == 0) {
-        bool ok = false;
-        for (uint32_t it = 0; it < (1u << 22); ++it) {
-          if (ld_acquire_gpu(done + plane) >= NB) {
-            ok = true;
-            break;
-          }
-          __nanosleep(64);
-        }
-        if (!ok) atomicExch(err, 2);
-      }
-      __syncthreads();
-      __threadfence();
-      const int col = threadIdx.x % G::CW;
-      const int j = threadIdx.x / G::CW;
-      const long off = ((long)blk * N + plane) * N * G::CW + col;
-      cols_b_column<N>(bt, stw, sbuf + col * L::LS, off, j);
-    }
-  }
-}
-
 
 // a-axis inverse pass of the K radii + centre test + first-hit update
 // (get_HIIbubbles.c:335-352; for floats h, d > 0, (double)h/d >= 1 <=> h >= d).
@@ -302,17 +211,20 @@ k_cols_a_test_cb(Batch bt, uint8_t* __restrict__ rc, const float* __restrict__ a
   };
   // two register sets in turn: the loads of radius k + 1 are in flight during
   // the transform of radius k
+  float2* s0 = sbuf + col * L::LS;
+  float2* s1 = sbuf + (X::KW + col) * L::LS;
   float2 va[8], vb[8];
   load(va, 0);
+  __syncthreads();  // twiddles
   for (int k = 0; k < bt.K; k += 2) {
     if (k + 1 < bt.K) load(vb, k + 1);
-    __syncthreads();
-    fft_line<N, true>(va, sbuf + col * L::LS, stw, j);
+    if (FftPP<N>::CALL_SYNC && k > 0) __syncthreads();
+    fft_line_pp<N, true>(va, s0, s1, stw, j);
     test(va, k);
     if (k + 1 < bt.K) {
       if (k + 2 < bt.K) load(va, k + 2);
-      __syncthreads();
-      fft_line<N, true>(vb, sbuf + col * L::LS, stw, j);
+      if (FftPP<N>::CALL_SYNC) __syncthreads();
+      fft_line_pp<N, true>(vb, s0, s1, stw, j);
       test(vb, k + 1);
     }
   }
@@ -336,9 +248,6 @@ struct CbLaunch {
     cudaError_t e;
     if ((e = cudaFuncSetAttribute(k_cols_b_cb<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)KGeom<N>::SMEM)))
       return e;
-    if ((e = cudaFuncSetAttribute(k_rows_cols_b_fused<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)fused_smem())))
-      return e;
     return cudaFuncSetAttribute(k_cols_a_test_cb<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)KGeom<N>::SMEM);
   }
@@ -349,15 +258,6 @@ struct CbLaunch {
   static cudaError_t cols_b(const Batch& bt, const float2* tw, cudaStream_t st) {
     using X = KGeom<N>;
     k_cols_b_cb<N><<<(unsigned)((long)N * G::NBLK * X::SPLIT), X::THREADS, X::SMEM, st>>>(bt, tw);
-    return cudaGetLastError();
-  }
-  static size_t fused_smem() { return (size_t)(N + G::CW * LineGeom<N>::LS) * sizeof(float2); }
-  static cudaError_t fused(const float2* spec, const Batch& bt, const float2* tw, int* ctl, int delay, int* err,
-                           int nsm, cudaStream_t st) {
-    if (KGeom<N>::THREADS != G::CW * (N / 8) || delay < 1 || delay >= N) return cudaErrorInvalidValue;
-    cudaError_t e = cudaMemsetAsync(ctl, 0, sizeof(int) * (N + 1), st);
-    if (e != cudaSuccess) return e;
-    k_rows_cols_b_fused<N><<<nsm, KGeom<N>::THREADS, fused_smem(), st>>>(spec, bt, tw, ctl, delay, err);
     return cudaGetLastError();
   }
   static cudaError_t cols_a_test(const Batch& bt, uint8_t* rc, const float* alpha, const float2* tw,
@@ -386,10 +286,6 @@ cudaError_t launch_rows_filter_cb(int N, const float2* spec, const Batch& bt, co
 }
 cudaError_t launch_cols_b_cb(int N, const Batch& bt, const float2* tw, cudaStream_t st) {
   SF21_CB_DISPATCH(N, LL::cols_b(bt, tw, st));
-}
-cudaError_t launch_rows_cols_b_fused(int N, const float2* spec, const Batch& bt, const float2* tw, int* ctl, int delay,
-                                    int* err, int nsm, cudaStream_t st) {
-  SF21_CB_DISPATCH(N, LL::fused(spec, bt, tw, ctl, delay, err, nsm, st));
 }
 cudaError_t launch_cols_a_test_cb(int N, const Batch& bt, uint8_t* rc, const float* alpha, const float2* tw,
                                   cudaStream_t st) {

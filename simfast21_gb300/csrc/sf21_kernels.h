@@ -89,10 +89,6 @@ cudaError_t launch_rows_filter_cb(int N, const float2* spec, const Batch& bt, co
 cudaError_t launch_cols_b_cb(int N, const Batch& bt, const float2* tw, cudaStream_t st);
 cudaError_t launch_cols_a_test_cb(int N, const Batch& bt, uint8_t* rc, const float* alpha, const float2* tw,
                                   cudaStream_t st);
-// Fused c-axis filter pass + b-axis pass (persistent, nsm CTAs; the b-axis
-// tiles of a plane are read back from L2).  ctl: N + 1 ints of scratch.
-cudaError_t launch_rows_cols_b_fused(int N, const float2* spec, const Batch& bt, const float2* tw, int* ctl, int delay,
-                                    int* err, int nsm, cudaStream_t st);
 
 // Criterion and adjoint (kernels_adj.cu).
 cudaError_t adj_setup(int N);

@@ -34,7 +34,7 @@ EXPORTS = [
 ]
 
 
-NPATH = 8  # radius pipelines (FilterBank.path)
+NPATH = 7  # radius pipelines (FilterBank.path)
 
 
 class HIIError(RuntimeError):
@@ -163,8 +163,7 @@ class FilterBank:
         """(pipeline in use: 1 = three axis passes, 2 = plane clusters,
         3 = TMA-pipelined ky pass, 4 = TMA-pipelined ky and kx passes, and over
         column-block-major work boxes 5 = three axis passes, 6 = TMA ky pass,
-        7 = TMA ky and kx passes, 8 = fused filter + ky pass through L2;
-        {pipeline: tuned ms of one batch})."""
+        7 = TMA ky and kx passes; {pipeline: tuned ms of one batch})."""
         ms = (ctypes.c_double * NPATH)()
         p = self._lib.sf21_hii_path(self._h, ms, NPATH)
         return p, {i + 1: ms[i] for i in range(NPATH)}
