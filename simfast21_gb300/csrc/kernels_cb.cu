@@ -38,12 +38,15 @@ __device__ __forceinline__ long cb_index(int a, int b, int c) {
 
 // c-axis inverse pass with the top-hat filter of the K radii of the batch
 // (get_HIIbubbles.c:305-322): spectrum row (a, b) read once, K filtered
-// transformed rows written column-block major.  One row per N/8 threads
-// (j = thread index in the row, sline = this row's exchange line).
+// transformed rows written column-block major.  One row per T = N/8 threads
+// (j = thread index in the row, s0/s1 = this row's two exchange lines).
+// (Sharing the N/2 + 1 distinct window values of a row through shared memory
+// or warp shuffles measured slower than evaluating W per element.)
 template <int N>
 __device__ __forceinline__ void rows_filter_row(const float2* __restrict__ spec, const Batch& bt,
                                                 const float2* stw, float2* s0, float2* s1, int a, int b, int j) {
   using G = CbGeom<N>;
+  constexpr int T = N / 8;
   const int ka = kfreq(a, N), kb = kfreq(b, N);
   const int kab = ka * ka + kb * kb;
   float2 z[8];
@@ -51,7 +54,7 @@ __device__ __forceinline__ void rows_filter_row(const float2* __restrict__ spec,
   const float2* src = spec + ((long)a * N + b) * N;
 #pragma unroll
   for (int r = 0; r < 8; ++r) {
-    const int c = j + r * (N / 8);
+    const int c = j + r * T;
     z[r] = __ldg(src + c);
     const int kc = kfreq(c, N);
     kmag[r] = sqrtf((float)(kab + kc * kc));
@@ -100,15 +103,17 @@ k_rows_filter_cb(const float2* __restrict__ spec, Batch bt, const float2* __rest
 // of N CW values per radius.  A CTA takes KW of the CW columns and walks the K
 // radii, issuing the loads of radius k + 1 before the transform of radius k.
 // blockIdx.x = (cb N + a) (CW / KW) + column half.
-// (A CTA takes the whole column block: with 16 columns a warp covers 16
+// A CTA takes the whole column block: with 16 columns a warp covers 16
 // lines x 2 threads, whose shared-memory exchanges of the line FFT are free of
-// bank conflicts; 8-column CTAs conflicted and stalled on the MIO pipe.)
+// bank conflicts.  (Half blocks of 8 columns, two CTAs per SM, measured
+// slower even with a conflict-free exchange padding.)
 template <int N>
 struct KGeom {
   static constexpr int KW = CbGeom<N>::CW;  // columns per CTA
   static constexpr int SPLIT = CbGeom<N>::CW / KW;
   static constexpr int THREADS = KW * (N / 8);
-  static constexpr size_t SMEM = (size_t)(N + 2 * KW * LineGeom<N>::LS) * sizeof(float2);  // two lines each
+  static constexpr int LS = LineGeom<N>::LS;  // float2 per exchange line
+  static constexpr size_t SMEM = (size_t)(N + 2 * KW * LS) * sizeof(float2);  // two lines each
 };
 
 // One column of a b-axis tile for all K radii.
@@ -150,7 +155,6 @@ __global__ void __launch_bounds__(KGeom<N>::THREADS, (KGeom<N>::THREADS <= 512 ?
 k_cols_b_cb(Batch bt, const float2* __restrict__ gtw) {
   using G = CbGeom<N>;
   using X = KGeom<N>;
-  using L = LineGeom<N>;
   extern __shared__ float2 dsm[];
   float2* stw = dsm;
   float2* sbuf = dsm + N;
@@ -160,11 +164,11 @@ k_cols_b_cb(Batch bt, const float2* __restrict__ gtw) {
   const int col = threadIdx.x % X::KW;
   const int j = threadIdx.x / X::KW;
   const long off = (long)tile * N * G::CW + half * X::KW + col;  // element (b = 0) of this column
-  cols_b_column<N>(bt, stw, sbuf + col * L::LS, sbuf + (X::KW + col) * L::LS, off, j);
+  cols_b_column<N>(bt, stw, sbuf + col * X::LS, sbuf + (X::KW + col) * X::LS, off, j);
 }
 
 // a-axis inverse pass of the K radii + centre test + first-hit update
-// (get_HIIbubbles.c:335-352; for floats h, d > 0, (double)h/d >= 1 <=> h >= d).
+// (get_HIIbubbles.c:335-352; centre test: is_centre).
 // A CTA takes KW of the CW columns of one column block (fixed b) and walks
 // the K radii; the loads of radius k + 1 are issued before the transform of
 // radius k, so every warp keeps a tile in flight while it computes.
@@ -175,7 +179,6 @@ k_cols_a_test_cb(Batch bt, uint8_t* __restrict__ rc, const float* __restrict__ a
                  const float2* __restrict__ gtw) {
   using G = CbGeom<N>;
   using X = KGeom<N>;
-  using L = LineGeom<N>;
   extern __shared__ float2 dsm[];
   float2* stw = dsm;
   float2* sbuf = dsm + N;
@@ -198,10 +201,7 @@ k_cols_a_test_cb(Batch bt, uint8_t* __restrict__ rc, const float* __restrict__ a
     const uint32_t bit = 1u << k;
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
-      const float rec = v[r].x * alpha;  // alpha * rec_R (exact: power of two)
-      const float ion = v[r].y * zmul;
-      const bool centre = (v[r].y > 0.0f) && (!(rec > 0.0f) || ion >= rec);
-      if (centre) m[r >> 2] |= bit << (8 * (r & 3));
+      if (is_centre(v[r], alpha, zmul)) m[r >> 2] |= bit << (8 * (r & 3));
     }
   };
   auto load = [&](float2 (&v)[8], int k) {
@@ -211,8 +211,8 @@ k_cols_a_test_cb(Batch bt, uint8_t* __restrict__ rc, const float* __restrict__ a
   };
   // two register sets in turn: the loads of radius k + 1 are in flight during
   // the transform of radius k
-  float2* s0 = sbuf + col * L::LS;
-  float2* s1 = sbuf + (X::KW + col) * L::LS;
+  float2* s0 = sbuf + col * X::LS;
+  float2* s1 = sbuf + (X::KW + col) * X::LS;
   float2 va[8], vb[8];
   load(va, 0);
   __syncthreads();  // twiddles

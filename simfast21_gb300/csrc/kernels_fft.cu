@@ -174,9 +174,7 @@ k_cols(float2* box0, Batch bt, int axis, const float2* __restrict__ gtw) {
 // Last inverse pass (a axis) of a batch, fused with the centre test and the
 // first-hit radius update.  Each CTA runs all K radii of the batch on the
 // same tile, keeps the smallest radius index at which each voxel is a centre
-// and updates rc (uint8 per voxel of the set) once.
-//   centre <=> ion > 0 && (rec <= 0 || ion * zeta >= rec)
-// (get_HIIbubbles.c:339-348; for floats h, d > 0, (double)h/d >= 1 <=> h >= d).
+// and updates rc (uint8 per voxel of the set) once (centre test: is_centre).
 template <int N>
 __global__ void __launch_bounds__(ColGeom<N>::THREADS)
 k_cols_a_test(Batch bt, uint8_t* __restrict__ rc, const float* __restrict__ alpha_ptr,
@@ -208,10 +206,7 @@ k_cols_a_test(Batch bt, uint8_t* __restrict__ rc, const float* __restrict__ alph
     const int ridx = bt.r[k].ridx;
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
-      const float rec = v[r].x * alpha;  // alpha * rec_R (exact: power of two)
-      const float ion = v[r].y * bt.zmul;
-      const bool centre = (v[r].y > 0.0f) && (!(rec > 0.0f) || ion >= rec);
-      if (centre && ridx < hit[r]) hit[r] = ridx;
+      if (is_centre(v[r], alpha, bt.zmul) && ridx < hit[r]) hit[r] = ridx;
     }
   }
 #pragma unroll

@@ -198,10 +198,7 @@ k_pipe(const __grid_constant__ CUtensorMap tmap, Batch bt, float2* __restrict__ 
       const int ridx = bt.r[k].ridx;
 #pragma unroll
       for (int r = 0; r < 8; ++r) {
-        const float rec = v[r].x * alpha;
-        const float ion = v[r].y * bt.zmul;
-        const bool centre = (v[r].y > 0.0f) && (!(rec > 0.0f) || ion >= rec);
-        if (centre && ridx < hit[r]) hit[r] = ridx;
+        if (is_centre(v[r], alpha, bt.zmul) && ridx < hit[r]) hit[r] = ridx;
       }
       if (k == per_tile - 1) {
 #pragma unroll

@@ -20,16 +20,14 @@ static unsigned el_grid(long n) {
   return (unsigned)(b < 152 * 32 ? b : 152 * 32);
 }
 
-// Centre mask of the filtered packed box (:335-352): mask = 1 where
-// ion > 0 && (rec <= 0 || ion*zeta >= rec); flag = 1 if any.
+// Centre mask of the filtered packed box (:335-352, is_centre); flag = 1 if
+// any.
 __global__ void k_plain_centres(long n3, const float2* __restrict__ box, const float* __restrict__ alpha_ptr,
                                 float zmul, float* __restrict__ mask, int* __restrict__ flag) {
   const float alpha = *alpha_ptr;
   int any = 0;
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += (long)gridDim.x * blockDim.x) {
-    const float2 v = box[i];
-    const float rec = v.x * alpha;
-    const bool c = (v.y > 0.0f) && (!(rec > 0.0f) || v.y * zmul >= rec);
+    const bool c = is_centre(box[i], alpha, zmul);
     mask[i] = c ? 1.0f : 0.0f;
     any |= c;
   }

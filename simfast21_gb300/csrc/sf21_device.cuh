@@ -29,12 +29,13 @@ struct Batch {    // radius indices r[k].ridx increase with k
 // Real-space top-hat window in k-space, W(x) = 3 (sin x - x cos x) / x^3
 // (auxiliary.c:350-359).  Below x = 2 the Taylor series in x^2 (to x^14,
 // truncation < 3e-11) avoids the cancellation of the closed form in float.
-// Above, the closed form with sin/cos of the argument reduced to [-pi, pi]
-// by a two-constant Cody-Waite step and evaluated by the SFU (__sinf/__cosf,
-// absolute error < 4e-7 on the reduced argument), divided by x^3 with the
-// fast division (2 ulp): the error this leaves in W is below
-// 1.8e-6 / x^2 + 3e-7 |W| <= 7e-7 absolute (W(0) = 1), under the FP32
-// rounding of the transforms it feeds.
+// Above, the closed form with sin/cos from the SFU (__sinf/__cosf: absolute
+// error < 4e-7 on [-pi, pi]; a larger argument is reduced as x / 2 pi in
+// single precision, which adds at most |x| 2^-24 to the angle) divided by x^3
+// with the fast division (2 ulp).  With e = 4e-7 + 6e-8 x the error left in
+// W is below 3 e (1 + x) / x^3 + 3e-7 |W| <= 6e-7 absolute for x >= 2
+// (W(0) = 1), and falls as 1/x for large x: under the FP32 rounding of the
+// transforms it feeds.
 __device__ __forceinline__ float w_tophat(float x) {
   if (x < 2.0f) {
     const float y = x * x;
@@ -48,12 +49,19 @@ __device__ __forceinline__ float w_tophat(float x) {
     p = fmaf(p, y, 1.0f);
     return p;
   }
-  // x = k 2 pi + r, 2 pi = 6.28318548202514648 (float) - 1.7484555e-7
-  const float k = rintf(x * 0.159154943091895336f);
-  float r = fmaf(-k, 6.28318548202514648f, x);
-  r = fmaf(-k, -1.7484555314695172e-07f, r);
-  const float s = __sinf(r), c = __cosf(r);
+  const float s = __sinf(x), c = __cosf(x);
   return __fdividef(3.0f * fmaf(-x, c, s), x * x * x);  // 2 ulp; x^3 < 2^126 here
+}
+
+// Centre test (get_HIIbubbles.c:339-348) on a packed filtered value
+// v = (rec_R, alpha * ion1_R), ion = ion1 * zeta:
+//   centre <=> ion > 0 && (rec <= 0 || ion >= rec)
+// (for floats h, d > 0, (double)h/d >= 1 <=> h >= d).  With zeta >= 0, ion > 0
+// and rec <= 0 already give ion >= rec, so the test reduces to
+// v.y > 0 && v.y * zeta >= v.x * alpha (alpha a power of two: exact scaling).
+// The one difference, a NaN rec, does not arise from finite boxes.
+__device__ __forceinline__ bool is_centre(float2 v, float alpha, float zeta) {
+  return (v.y > 0.0f) && (v.y * zeta >= v.x * alpha);
 }
 
 // Signed frequency index of position i on an N-point axis (:309-311).

@@ -180,11 +180,17 @@ class FilterBank:
             raise HIIError(-n, "bad set index")
         return [buf[i] for i in range(n)], nf.value
 
-    def run_z(self, z: float, delta, src, src_kind: int = SF21_SRC_SFRD):
-        """xHII boxes (nsets, N, N, N) and neutral fractions (nsets,)."""
+    def run_z(self, z: float, delta, src, src_kind: int = SF21_SRC_SFRD, out=None):
+        """xHII boxes (nsets, N, N, N) and neutral fractions (nsets,).  `out`:
+        an optional C-contiguous float32 array of that shape to write into
+        (e.g. pinned host memory)."""
         d = _f32(delta, self.n3)
         s = _f32(src, self.n3)
-        out = np.empty((len(self.sets), self.N, self.N, self.N), np.float32)
+        shape = (len(self.sets), self.N, self.N, self.N)
+        if out is None:
+            out = np.empty(shape, np.float32)
+        elif out.shape != shape or out.dtype != np.float32 or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError(f"out must be a C-contiguous float32 array of shape {shape}")
         neutral = (ctypes.c_double * len(self.sets))()
         self._check(self._lib.sf21_hii_run_z(self._h, z, src_kind, _ptr(d), _ptr(s), _ptr(out), neutral))
         return out, np.array(neutral[:], dtype=np.float64)
