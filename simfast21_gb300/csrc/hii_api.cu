@@ -503,7 +503,7 @@ static int enqueue_batch(sf21_hii_ctx* c, const Batch& bt, cudaStream_t st) {
       CTX_CUDA(c, launch_pipe(N, 1, 1, c->pmaps, bt, c->d_work_base, c->d_rc, c->d_alpha, c->d_tw, c->d_err,
                               c->nsm, st));
     else
-      CTX_CUDA(c, launch_cols_a_test_cb(N, bt, c->d_rc, c->d_alpha, c->d_tw, st));
+      CTX_CUDA(c, launch_cols_a_test_cb(N, bt, c->d_rc, c->d_alpha, c->d_tw, c->nsm, st));
     int e3 = mark(c, st);
     span(c, KD_IROWS, e0, e1);
     span(c, KD_ICB, e1, e2);

@@ -99,10 +99,14 @@ k_rows_filter_cb(const float2* __restrict__ spec, Batch bt, const float2* __rest
                      (int)(row / N), (int)(row % N), j);
 }
 
-// b-axis inverse pass in place: tile (a, column block) is one contiguous run
-// of N CW values per radius.  A CTA takes KW of the CW columns and walks the K
-// radii, issuing the loads of radius k + 1 before the transform of radius k.
-// blockIdx.x = (cb N + a) (CW / KW) + column half.
+// b-axis inverse pass in place: tile (a, column block) = one contiguous run
+// of N CW values per radius.  One CTA per tile (blockIdx.x = cb N + a) walks
+// the K radii with two register sets in turn, the loads of radius k + 1 in
+// flight during the transform of radius k.  (A persistent form with
+// prefetch across tiles, as in the a-axis pass below, measured 5 % slower
+// here: this pass is at the HBM roofline and the hardware's dynamic tile
+// order keeps the concurrent tiles' accesses closer together.)
+//
 // A CTA takes the whole column block: with 16 columns a warp covers 16
 // lines x 2 threads, whose shared-memory exchanges of the line FFT are free of
 // bank conflicts.  (Half blocks of 8 columns, two CTAs per SM, measured
@@ -110,17 +114,24 @@ k_rows_filter_cb(const float2* __restrict__ spec, Batch bt, const float2* __rest
 template <int N>
 struct KGeom {
   static constexpr int KW = CbGeom<N>::CW;  // columns per CTA
-  static constexpr int SPLIT = CbGeom<N>::CW / KW;
   static constexpr int THREADS = KW * (N / 8);
   static constexpr int LS = LineGeom<N>::LS;  // float2 per exchange line
   static constexpr size_t SMEM = (size_t)(N + 2 * KW * LS) * sizeof(float2);  // two lines each
+  static constexpr int PER_SM = THREADS <= 512 ? 2 : 1;
 };
 
-// One column of a b-axis tile for all K radii.
 template <int N>
-__device__ __forceinline__ void cols_b_column(const Batch& bt, const float2* stw, float2* s0, float2* s1, long off,
-                                              int j) {
+__global__ void __launch_bounds__(KGeom<N>::THREADS, KGeom<N>::PER_SM)
+k_cols_b_cb(Batch bt, const float2* __restrict__ gtw) {
   using G = CbGeom<N>;
+  using X = KGeom<N>;
+  extern __shared__ float2 dsm[];
+  float2* stw = dsm;
+  float2* sbuf = dsm + N;
+  for (int t = threadIdx.x; t < N; t += blockDim.x) stw[t] = gtw[t];
+  const int col = threadIdx.x % X::KW;
+  const int j = threadIdx.x / X::KW;
+  const long off = (long)blockIdx.x * N * G::CW + col;  // element (b = 0) of this column
   auto load = [&](float2 (&v)[8], int k) {
     const float2* box = bt.r[k].work + off;
 #pragma unroll
@@ -131,11 +142,11 @@ __device__ __forceinline__ void cols_b_column(const Batch& bt, const float2* stw
 #pragma unroll
     for (int r = 0; r < 8; ++r) box[(j + r * (N / 8)) * G::CW] = v[r];
   };
-  // two register sets in turn: the loads of radius k + 1 are in flight during
-  // the transform of radius k
+  float2* s0 = sbuf + col * X::LS;
+  float2* s1 = sbuf + (X::KW + col) * X::LS;
   float2 va[8], vb[8];
   load(va, 0);
-  __syncthreads();  // twiddles and the previous use of the exchange lines
+  __syncthreads();  // twiddles
   for (int k = 0; k < bt.K; k += 2) {
     if (k + 1 < bt.K) load(vb, k + 1);
     if (FftPP<N>::CALL_SYNC && k > 0) __syncthreads();
@@ -150,33 +161,19 @@ __device__ __forceinline__ void cols_b_column(const Batch& bt, const float2* stw
   }
 }
 
-template <int N>
-__global__ void __launch_bounds__(KGeom<N>::THREADS, (KGeom<N>::THREADS <= 512 ? 2 : 1))
-k_cols_b_cb(Batch bt, const float2* __restrict__ gtw) {
-  using G = CbGeom<N>;
-  using X = KGeom<N>;
-  extern __shared__ float2 dsm[];
-  float2* stw = dsm;
-  float2* sbuf = dsm + N;
-  for (int t = threadIdx.x; t < N; t += blockDim.x) stw[t] = gtw[t];
-  const int tile = blockIdx.x / X::SPLIT;
-  const int half = blockIdx.x % X::SPLIT;
-  const int col = threadIdx.x % X::KW;
-  const int j = threadIdx.x / X::KW;
-  const long off = (long)tile * N * G::CW + half * X::KW + col;  // element (b = 0) of this column
-  cols_b_column<N>(bt, stw, sbuf + col * X::LS, sbuf + (X::KW + col) * X::LS, off, j);
-}
-
 // a-axis inverse pass of the K radii + centre test + first-hit update
-// (get_HIIbubbles.c:335-352; centre test: is_centre).
-// A CTA takes KW of the CW columns of one column block (fixed b) and walks
-// the K radii; the loads of radius k + 1 are issued before the transform of
-// radius k, so every warp keeps a tile in flight while it computes.
-// blockIdx.x = (cb N + b) (CW / KW) + column half.
+// (get_HIIbubbles.c:335-352; centre test: is_centre).  Persistent (5 %
+// faster here than one CTA per tile): CTA i
+// takes tiles i, i + gridDim.x, ... (tile = cb N + b: one column block of
+// one b) and walks each tile's K radii.  The steps (tile, radius) use two
+// register sets in turn and the loads of the next step -- the next radius,
+// or radius 0 of the next tile -- are issued before the transform of the
+// current one, so every warp keeps a tile in flight while it computes, also
+// across tiles.
 template <int N>
-__global__ void __launch_bounds__(KGeom<N>::THREADS, (KGeom<N>::THREADS <= 512 ? 2 : 1))
+__global__ void __launch_bounds__(KGeom<N>::THREADS, KGeom<N>::PER_SM)
 k_cols_a_test_cb(Batch bt, uint8_t* __restrict__ rc, const float* __restrict__ alpha_ptr,
-                 const float2* __restrict__ gtw) {
+                 const float2* __restrict__ gtw, int ntiles) {
   using G = CbGeom<N>;
   using X = KGeom<N>;
   extern __shared__ float2 dsm[];
@@ -184,19 +181,16 @@ k_cols_a_test_cb(Batch bt, uint8_t* __restrict__ rc, const float* __restrict__ a
   float2* sbuf = dsm + N;
   for (int t = threadIdx.x; t < N; t += blockDim.x) stw[t] = gtw[t];
   const float alpha = *alpha_ptr;
-  const int tile = blockIdx.x / X::SPLIT;
-  const int half = blockIdx.x % X::SPLIT;
-  const int cb = tile / N;
-  const int b = tile % N;
+  const float zmul = bt.zmul;
+  const int K = bt.K;
   const int col = threadIdx.x % X::KW;
   const int j = threadIdx.x / X::KW;
-  const int cc = half * X::KW + col;                       // column within the block
-  const long base = ((long)cb * N * N + b) * G::CW + cc;    // element (a = 0, b, cb CW + cc)
   const long astride = (long)N * G::CW;
+  // element (a = 0, b, cb CW + col) of tile cb N + b
+  auto tile_base = [&](int tile) { return ((long)(tile / N) * N * N + tile % N) * G::CW + col; };
   // bit 8 (r & 3) + k of m[r / 4]: element r is a centre at radius k of the
   // batch (radius indices increase with k, so the lowest bit is the first hit)
   uint32_t m[2] = {0u, 0u};
-  const float zmul = bt.zmul;
   auto test = [&](const float2 (&v)[8], int k) {
     const uint32_t bit = 1u << k;
 #pragma unroll
@@ -204,40 +198,56 @@ k_cols_a_test_cb(Batch bt, uint8_t* __restrict__ rc, const float* __restrict__ a
       if (is_centre(v[r], alpha, zmul)) m[r >> 2] |= bit << (8 * (r & 3));
     }
   };
-  auto load = [&](float2 (&v)[8], int k) {
-    const float2* box = bt.r[k].work + base;
+  auto load = [&](float2 (&v)[8], int tile, int k) {
+    const float2* box = bt.r[k].work + tile_base(tile);
 #pragma unroll
     for (int r = 0; r < 8; ++r) v[r] = box[(long)(j + r * (N / 8)) * astride];
   };
-  // two register sets in turn: the loads of radius k + 1 are in flight during
-  // the transform of radius k
+  auto flush = [&](int tile) {  // first-hit update of the tile, once per tile
+    const int b = tile % N;
+    const int c = (tile / N) * G::CW + col;
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      const uint32_t byte = (m[r >> 2] >> (8 * (r & 3))) & 0xFFu;
+      if (byte) {
+        const uint32_t h = (uint32_t)bt.r[__ffs(byte) - 1].ridx;
+        const long idx = ((long)(j + r * (N / 8)) * N + b) * N + c;
+        const uint8_t old = rc[idx];
+        if (h < old) rc[idx] = (uint8_t)h;
+      }
+    }
+    m[0] = m[1] = 0u;
+  };
   float2* s0 = sbuf + col * X::LS;
   float2* s1 = sbuf + (X::KW + col) * X::LS;
+  int tile = blockIdx.x, k = 0;
+  if (tile >= ntiles) return;
   float2 va[8], vb[8];
-  load(va, 0);
+  load(va, tile, 0);
   __syncthreads();  // twiddles
-  for (int k = 0; k < bt.K; k += 2) {
-    if (k + 1 < bt.K) load(vb, k + 1);
-    if (FftPP<N>::CALL_SYNC && k > 0) __syncthreads();
+  for (bool first = true;; first = false) {
+    // step (tile, k) in va; the next step goes to vb
+    int kb = k + 1, tb = tile;
+    if (kb == K) { kb = 0; tb += gridDim.x; }
+    const bool has_b = tb < ntiles;
+    if (has_b) load(vb, tb, kb);
+    if (FftPP<N>::CALL_SYNC && !first) __syncthreads();
     fft_line_pp<N, true>(va, s0, s1, stw, j);
     test(va, k);
-    if (k + 1 < bt.K) {
-      if (k + 2 < bt.K) load(va, k + 2);
-      if (FftPP<N>::CALL_SYNC) __syncthreads();
-      fft_line_pp<N, true>(vb, s0, s1, stw, j);
-      test(vb, k + 1);
-    }
-  }
-  const int c = cb * G::CW + cc;
-#pragma unroll
-  for (int r = 0; r < 8; ++r) {
-    const uint32_t byte = (m[r >> 2] >> (8 * (r & 3))) & 0xFFu;
-    if (byte) {
-      const uint32_t h = (uint32_t)bt.r[__ffs(byte) - 1].ridx;
-      const long idx = ((long)(j + r * (N / 8)) * N + b) * N + c;
-      const uint8_t old = rc[idx];
-      if (h < old) rc[idx] = (uint8_t)h;
-    }
+    if (k == K - 1) flush(tile);
+    if (!has_b) break;
+    // step (tb, kb) in vb; the next step goes to va
+    int kc = kb + 1, tc = tb;
+    if (kc == K) { kc = 0; tc += gridDim.x; }
+    const bool has_c = tc < ntiles;
+    if (has_c) load(va, tc, kc);
+    if (FftPP<N>::CALL_SYNC) __syncthreads();
+    fft_line_pp<N, true>(vb, s0, s1, stw, j);
+    test(vb, kb);
+    if (kb == K - 1) flush(tb);
+    if (!has_c) break;
+    tile = tc;
+    k = kc;
   }
 }
 
@@ -255,15 +265,19 @@ struct CbLaunch {
     k_rows_filter_cb<N><<<(unsigned)((long)N * N / G::ROWS), G::RTHREADS, 0, st>>>(spec, bt, tw);
     return cudaGetLastError();
   }
+  static int grid(int nsm) {
+    const int ntiles = N * G::NBLK;
+    return ntiles < nsm * KGeom<N>::PER_SM ? ntiles : nsm * KGeom<N>::PER_SM;
+  }
   static cudaError_t cols_b(const Batch& bt, const float2* tw, cudaStream_t st) {
     using X = KGeom<N>;
-    k_cols_b_cb<N><<<(unsigned)((long)N * G::NBLK * X::SPLIT), X::THREADS, X::SMEM, st>>>(bt, tw);
+    k_cols_b_cb<N><<<(unsigned)(N * G::NBLK), X::THREADS, X::SMEM, st>>>(bt, tw);
     return cudaGetLastError();
   }
-  static cudaError_t cols_a_test(const Batch& bt, uint8_t* rc, const float* alpha, const float2* tw,
+  static cudaError_t cols_a_test(const Batch& bt, uint8_t* rc, const float* alpha, const float2* tw, int nsm,
                                  cudaStream_t st) {
     using X = KGeom<N>;
-    k_cols_a_test_cb<N><<<(unsigned)((long)N * G::NBLK * X::SPLIT), X::THREADS, X::SMEM, st>>>(bt, rc, alpha, tw);
+    k_cols_a_test_cb<N><<<grid(nsm), X::THREADS, X::SMEM, st>>>(bt, rc, alpha, tw, N * G::NBLK);
     return cudaGetLastError();
   }
 };
@@ -287,9 +301,9 @@ cudaError_t launch_rows_filter_cb(int N, const float2* spec, const Batch& bt, co
 cudaError_t launch_cols_b_cb(int N, const Batch& bt, const float2* tw, cudaStream_t st) {
   SF21_CB_DISPATCH(N, LL::cols_b(bt, tw, st));
 }
-cudaError_t launch_cols_a_test_cb(int N, const Batch& bt, uint8_t* rc, const float* alpha, const float2* tw,
+cudaError_t launch_cols_a_test_cb(int N, const Batch& bt, uint8_t* rc, const float* alpha, const float2* tw, int nsm,
                                   cudaStream_t st) {
-  SF21_CB_DISPATCH(N, LL::cols_a_test(bt, rc, alpha, tw, st));
+  SF21_CB_DISPATCH(N, LL::cols_a_test(bt, rc, alpha, tw, nsm, st));
 }
 
 }  // namespace sf21

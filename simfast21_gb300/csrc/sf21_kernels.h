@@ -87,7 +87,7 @@ cudaError_t launch_pipe(int N, int mode, int layout, const PipeMaps& pm, const B
 cudaError_t cb_setup(int N);
 cudaError_t launch_rows_filter_cb(int N, const float2* spec, const Batch& bt, const float2* tw, cudaStream_t st);
 cudaError_t launch_cols_b_cb(int N, const Batch& bt, const float2* tw, cudaStream_t st);
-cudaError_t launch_cols_a_test_cb(int N, const Batch& bt, uint8_t* rc, const float* alpha, const float2* tw,
+cudaError_t launch_cols_a_test_cb(int N, const Batch& bt, uint8_t* rc, const float* alpha, const float2* tw, int nsm,
                                   cudaStream_t st);
 
 // Criterion and adjoint (kernels_adj.cu).
