@@ -337,6 +337,11 @@ def run_ours(args, w, rank, world):
         "inv_plane_filter": n3 * 8.0 * (1 + K_avg),      # spectrum read once, K boxes written
     }.get(dom, None)
     achieved = alg / (per_launch_ms / 1e3) / 1e9 if alg else None
+    # DRAM traffic per launch (dram__bytes_read + dram__bytes_write) from the
+    # ncu capture of the same kernels at 512^3, K = 8, per voxel*radius
+    # (profiles/radius_kernels_cb_single512.md), scaled to this launch's radii
+    traffic_b = {"inv_cols_b": 15.94, "inv_cols_a_test": 8.00, "inv_rows_filter": 8.94}.get(dom)
+    traffic = traffic_b * n3 * K_avg if (traffic_b and path >= 5) else None
     # whole radius pipeline against the 16 B per voxel*radius algorithmic traffic
     pipe_ms = sum(kinds.get(k, (0, 0))[0] for k in ("inv_rows_filter", "inv_cols_b", "inv_cols_a_test",
                                                      "inv_plane_filter"))
@@ -397,7 +402,8 @@ def run_ours(args, w, rank, world):
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
                          "unit": "GB/s", "frac": (achieved / hbm) if achieved else None,
-                         "peak_source": peak_kind, "traffic": None,
+                         "peak_source": peak_kind, "traffic": traffic,
+                         "traffic_source": "ncu capture, 512^3 K=8, scaled per launch" if traffic else None,
                          "pipeline_16B_per_voxel_radius_gbs": pipe_gbs,
                          "pipeline_frac": (pipe_gbs / hbm) if pipe_gbs else None},
             "kernels_ms_per_step": {k: round(v[0] / steps, 3) for k, v in kinds.items()},
