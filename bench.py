@@ -40,17 +40,20 @@ from simfast21_gb300 import synth  # noqa: E402
 
 
 # ---------------------------------------------------------------------------
-def workload(name: str):
-    """(N, L, z, sets, seed, label) of a named workload."""
+def workload(name: str, rank: int = 0):
+    """(N, L, z, sets, seed, label) of a named workload.  Under torchrun each
+    rank is one replica with its own parameter sets (the batched workloads
+    draw them from a rank-dependent seed): per-GPU work is fixed, units
+    differ between ranks (weak scaling, no collective on the data path)."""
     h = 0.71
     if name == "batched512":
         N, L, z, seed = 512, 300.0, 7.0, 1236
-        rng = np.random.default_rng(seed)
+        rng = np.random.default_rng(seed + 7919 * rank)
         zetas = np.exp(rng.uniform(np.log(10.0), np.log(100.0), 64))
         rmaxs = rng.uniform(10.0, 60.0, 64)
     elif name == "batched256":
         N, L, z, seed = 256, 150.0, 7.0, 1236
-        rng = np.random.default_rng(seed)
+        rng = np.random.default_rng(seed + 7919 * rank)
         zetas = np.exp(rng.uniform(np.log(10.0), np.log(100.0), 16))
         rmaxs = rng.uniform(5.0, 30.0, 16)
     elif name == "single512":
@@ -73,6 +76,21 @@ def workload(name: str):
         nb = max(1, int(round(math.log(rmax / dx) / math.log(factor))))
         sets.append((float(zt), float(rmax), nb))
     return dict(N=N, L=L, z=z, hubble=h, sets=sets, seed=seed, name=name)
+
+
+def reduce_across_ranks(ms: float, units: float, device):
+    """(max of ms, sum of units) over the ranks of the default process group
+    (identity without one): the job's step time and the units all ranks
+    processed in it."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return ms, units
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    u = torch.tensor([units], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(u.item())
 
 
 def describe(w):
@@ -300,11 +318,8 @@ def run_ours(args, w, rank, world):
     ms = ev0.elapsed_time(ev1) / args.steps
     prof = fb.profile_read()
     fb.profile(False)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = units * world / (ms / 1e3)
+    ms, job_units = reduce_across_ranks(ms, units, "cuda")
+    value = job_units / (ms / 1e3)
 
     # e2e through the host-buffer C-ABI call
     h_delta = torch.from_numpy(delta).pin_memory().numpy()
@@ -318,7 +333,8 @@ def run_ours(args, w, rank, world):
         x, neutral = fb.run_z(w["z"], h_delta, h_src, out=h_out)
     e2e_s = (time.perf_counter() - t0) / e2e_steps
     barrier()
-    e2e_val = units * world / e2e_s
+    e2e_s, _ = reduce_across_ranks(e2e_s, units, "cuda")
+    e2e_val = job_units / e2e_s
 
     # roofline of the dominant kernel kind (largest device-time share)
     hbm, peak_kind = peaks()
@@ -361,7 +377,7 @@ def run_ours(args, w, rank, world):
     plain_units = float(n3) * len(fb.radii(plain_set)[0])
     plain = {"value": plain_units / (plain_ms / 1e3), "unit": "voxel*radii/s", "ms": plain_ms,
              "set": plain_set, "radii": len(fb.radii(plain_set)[0]),
-             "batched_per_set_speedup": (value / world) / (plain_units / (plain_ms / 1e3))}
+             "batched_per_set_speedup": (units / (ms / 1e3)) / (plain_units / (plain_ms / 1e3))}
     del d_plain
 
     # differentiation: criterion forward and hand-written VJP (bwd/fwd),
@@ -431,7 +447,7 @@ def main():
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
-    w = workload(args.workload)
+    w = workload(args.workload, rank)
     if args.impl == "reference":
         run_reference(args, w, rank)
         return
