@@ -185,6 +185,27 @@ struct FftPP {
   static constexpr bool CALL_SYNC = (EXCH % 2) != 0;
 };
 
+// Padded exchange indices as one per-thread base plus compile-time offsets
+// (identical to padx() of the full index, checked over every N, j and r):
+//   padx(j + r N/8)       = padx(j) + r (N/8 + N/128)          (N/8 % 16 == 0)
+//   padx(8 j + r)         = 8 j + (j >> 1) + r                  (Ns = 1)
+//   padx(b8 + 8 r)        = (j/8) 68 + (j & 7) + 8 r + (r >> 1) (Ns = 8)
+//   padx(bNs + r Ns)      = padx(bNs) + r (Ns + Ns/16)          (Ns % 16 == 0)
+// with bNs = (j/Ns) 8 Ns + j mod Ns, the store base of the exchange.
+template <int N>
+__device__ __forceinline__ int pp_load_index(int j, int r) {
+  constexpr int N8 = N / 8;
+  if constexpr (N8 % 16 == 0) return padx(j) + r * (N8 + N8 / 16);
+  else return padx(j + r * N8);
+}
+template <int Ns>
+__device__ __forceinline__ int pp_store_index(int j, int r) {
+  if constexpr (Ns == 1) return 8 * j + (j >> 1) + r;
+  else if constexpr (Ns == 8) return (j >> 3) * 68 + (j & 7) + 8 * r + (r >> 1);
+  else if constexpr (Ns % 16 == 0) return padx((j / Ns) * Ns * 8 + (j & (Ns - 1))) + r * (Ns + Ns / 16);
+  else return padx((j / Ns) * Ns * 8 + (j & (Ns - 1)) + r * Ns);
+}
+
 template <int N, bool INV>
 __device__ __forceinline__ void fft_line_pp(float2 (&v)[8], float2* s0, float2* s1, const float2* tw, int j) {
   constexpr int Q = FftPP<N>::Q;
@@ -197,7 +218,7 @@ __device__ __forceinline__ void fft_line_pp(float2 (&v)[8], float2* s0, float2* 
     if (st > 0) {
       float2* prev = (st & 1) ? s0 : s1;  // written by the previous exchange
 #pragma unroll
-      for (int r = 0; r < 8; ++r) v[r] = prev[padx(j + r * N8)];
+      for (int r = 0; r < 8; ++r) v[r] = prev[pp_load_index<N>(j, r)];
       const int jm = j & (Ns - 1);
       const float2* tws = tw + tw_stage_off(st);
 #pragma unroll
@@ -207,9 +228,16 @@ __device__ __forceinline__ void fft_line_pp(float2 (&v)[8], float2* s0, float2* 
     const bool keep = (st == Q - 1) && (RB == 0);
     if (!keep) {
       cur = (st & 1) ? s1 : s0;
-      const int base = (j / Ns) * Ns * 8 + (j & (Ns - 1));
+      if (st == 0) {
 #pragma unroll
-      for (int r = 0; r < 8; ++r) cur[padx(base + r * Ns)] = v[r];
+        for (int r = 0; r < 8; ++r) cur[pp_store_index<1>(j, r)] = v[r];
+      } else if (st == 1) {
+#pragma unroll
+        for (int r = 0; r < 8; ++r) cur[pp_store_index<8>(j, r)] = v[r];
+      } else {
+#pragma unroll
+        for (int r = 0; r < 8; ++r) cur[pp_store_index<64>(j, r)] = v[r];
+      }
       __syncthreads();
     }
     Ns *= 8;
