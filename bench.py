@@ -391,6 +391,30 @@ def run_ours(args, w, rank, world):
         if args.grad_large:
             grad["box1024"] = grad_metrics(1024, 500.0, 7.0, 30.0, 80.0, 1.12, 5555, stream, dev, kmax=4)
 
+    # power spectrum of the density box (tools/power3d_f.c, Bartlett window):
+    # the library's GPU form (device box in, binned P(k) on the host) and,
+    # as its CPU baseline, the restatement of the tool on the host cores
+    pk = None
+    if not args.no_pk:
+        dl = w["L"] / N
+        fb.power_spectrum_device(d_delta.data_ptr(), dl, 1, stream=sptr)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        reps = 3
+        for _ in range(reps):
+            fb.power_spectrum_device(d_delta.data_ptr(), dl, 1, stream=sptr)
+        pk_ms = (time.perf_counter() - t0) / reps * 1e3
+        pk = {"N": N, "window": "Bartlett", "gpu_ms": pk_ms,
+              "gpu_voxels_per_s": n3 / (pk_ms / 1e3)}
+        if rank == 0 and not args.no_cpu_baseline:
+            from oracle import pk_oracle as K
+            t0 = time.perf_counter()
+            K.power_spectrum(delta, dl, 1)
+            cpu_ms = (time.perf_counter() - t0) * 1e3
+            pk["cpu_baseline"] = {"ms": cpu_ms, "cores": os.cpu_count() or 1, "kind": "port",
+                                  "sample": "restatement of tools/power3d_f.c (numpy/scipy float32 FFT), "
+                                            "same box"}
+
     # CPU baseline (rank 0 only)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -426,6 +450,7 @@ def run_ours(args, w, rank, world):
             "clocks": clk.summary(),
             "plain_gpu": plain,
             "differentiation": grad,
+            "power_spectrum": pk,
             "cpu_baseline": cpu,
         }
         print(json.dumps(out))
@@ -441,6 +466,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--kmax", type=int, default=0, help="radii per spectrum read (0 = library default)")
     ap.add_argument("--no-grad", action="store_true", help="skip the bwd/fwd measurement")
+    ap.add_argument("--no-pk", action="store_true", help="skip the power-spectrum measurement")
     ap.add_argument("--grad-large", action="store_true", help="also time fwd+bwd at 1024^3 (peak HBM)")
     ap.add_argument("--path", type=int, default=0,
                     help="radius pipeline: 0 = tuned, else one of PIPELINES")

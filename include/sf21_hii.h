@@ -142,6 +142,19 @@ int sf21_hii_halo_source_noalloc(double z, long N_halo, long N_smoothed, long nh
 int sf21_hii_run_z_halos(sf21_hii_ctx *ctx, double z, const float *delta, long nhalos, const void *halos,
                          float *xhii, double *neutral);
 
+/* Power spectrum of a box of the context's size N^3 (cubic boxes only), the
+ * reference's tools/power3d_f.c:124-194: window per axis (flag 0 top hat,
+ * 1 Bartlett, 2 Welch, power3d_f.c:205-211), r2c transform, |F|^2 summed in
+ * spherical bins round(|k|/dk), dk = 2 pi / (N dl), divided by the bin count,
+ * the window's sum of squares and multiplied by dl^3.  Writes k[b] = b dk and
+ * P[b] for b < min(nk, cap); returns nk = round(sqrt(3) N/2) + 1, or minus
+ * an SF21_E_* code.  Host box / device box (enqueued on stream, then
+ * synchronised). */
+int sf21_hii_power_spectrum(sf21_hii_ctx *ctx, const float *box, int flag, double dl, double *k, double *P,
+                            int cap);
+int sf21_hii_power_spectrum_device(sf21_hii_ctx *ctx, const float *box_dev, int flag, double dl, double *k,
+                                   double *P, int cap, void *stream);
+
 /* Radius list of a set exactly as the reference iterates it (:192, 298-461):
  * writes up to cap radii (Mpc/h, descending), returns the count (or <0 on
  * error); *n_fft receives how many take the FFT branch (R >= 2 dx). */

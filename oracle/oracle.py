@@ -14,6 +14,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libsf21oracle.so")
 REF_EXE = os.path.join(HERE, "_ref", "get_HIIbubbles.x")
+PK_EXE = os.path.join(HERE, "_ref", "power3d_f.x")  # tools/power3d_f.c, built by make ref
 
 
 class _Params(ctypes.Structure):

@@ -19,8 +19,11 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libsf21hii.so")
 DRIVER = os.path.join(HERE, "sf21_hii")
 DRIVER_SRC = [os.path.join(HERE, "driver", f) for f in ("sf21_hii_main.c", "sf21_stage.c")]
+PK_DRIVER = os.path.join(HERE, "sf21_power3d_f")  # drop-in for tools/power3d_f.c
+PK_DRIVER_SRC = [os.path.join(HERE, "driver", "sf21_power3d_main.c")]
 SOURCES = ["kernels_fft.cu", "kernels_plane.cu", "kernels_pipe.cu", "kernels_adj.cu", "kernels_elem.cu",
-           "kernels_plain.cu", "kernels_halo.cu", "kernels_cb.cu", "kernels_dt.cu", "hii_api.cu"]
+           "kernels_plain.cu", "kernels_halo.cu", "kernels_cb.cu", "kernels_dt.cu", "kernels_pk.cu",
+           "hii_api.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3"]
 
@@ -41,23 +44,29 @@ def _deps_mtime(roots=None) -> float:
     return t
 
 
-def build_driver(force: bool = False) -> str:
-    """The sf21_hii executable (drop-in for get_HIIbubbles.x), linked to the
-    library with an $ORIGIN rpath."""
+def _link_exe(exe: str, srcs, force: bool) -> str:
     deps = max(_deps_mtime([os.path.join(HERE, "driver"), os.path.join(HERE, "..", "include")]),
                os.path.getmtime(LIB))
-    if not force and os.path.exists(DRIVER) and os.path.getmtime(DRIVER) >= deps:
-        return DRIVER
+    if not force and os.path.exists(exe) and os.path.getmtime(exe) >= deps:
+        return exe
     cc = shutil.which("gcc") or shutil.which("cc")
     if not cc:
-        raise RuntimeError("no C compiler for the sf21_hii driver")
+        raise RuntimeError("no C compiler for the drivers")
     cmd = [cc, "-O2", "-std=c99", "-ffp-contract=off", "-Wall", "-I", os.path.join(HERE, "..", "include"),
-           *DRIVER_SRC, "-o", DRIVER + ".tmp", "-L", HERE, "-lsf21hii", "-Wl,-rpath,$ORIGIN", "-lm"]
+           *srcs, "-o", exe + ".tmp", "-L", HERE, "-lsf21hii", "-Wl,-rpath,$ORIGIN", "-lm"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
-        raise RuntimeError(f"driver build failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(DRIVER + ".tmp", DRIVER)
-    return DRIVER
+        raise RuntimeError(f"{os.path.basename(exe)} build failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(exe + ".tmp", exe)
+    return exe
+
+
+def build_driver(force: bool = False) -> str:
+    """The sf21_hii executable (drop-in for get_HIIbubbles.x) and
+    sf21_power3d_f (drop-in for tools/power3d_f), linked to the library with
+    an $ORIGIN rpath; returns the sf21_hii path."""
+    _link_exe(PK_DRIVER, PK_DRIVER_SRC, force)
+    return _link_exe(DRIVER, DRIVER_SRC, force)
 
 
 def build(force: bool = False, verbose: bool = False) -> str:

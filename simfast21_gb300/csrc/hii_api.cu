@@ -111,6 +111,11 @@ struct sf21_hii_ctx {
   void* d_halos = nullptr;
   long halo_cap = 0;
   float* d_fine = nullptr;
+  // power-spectrum buffers (allocated on first use)
+  float2* d_pk = nullptr;
+  float* d_pk_w = nullptr;
+  float* d_pk_part = nullptr;
+  unsigned long long* d_pk_cnt = nullptr;
   void* d_hscratch = nullptr;
   size_t hscratch_bytes = 0;
   // plain-form buffers (allocated on first use)
@@ -211,7 +216,8 @@ static void free_ctx(sf21_hii_ctx* c) {
   void* ptrs[] = {c->d_delta, c->d_src, c->d_rec0, c->d_fres, c->d_partials, c->d_alpha,
                   c->d_xhii, c->d_spec, c->d_tw, c->d_rc, c->d_mask, c->d_flag, c->d_box2,
                   c->d_C, c->d_A, c->d_acc, c->d_zpart, c->d_g, c->d_gd, c->d_gs, c->d_halos, c->d_fine,
-                  c->d_hscratch, c->d_chain, c->d_om, c->d_xhii2};
+                  c->d_hscratch, c->d_chain, c->d_om, c->d_xhii2, c->d_pk, c->d_pk_w, c->d_pk_part,
+                  c->d_pk_cnt};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->d_work_base) cudaFree(c->d_work_base);
@@ -1136,4 +1142,83 @@ extern "C" int sf21_hii_run_z_halos(sf21_hii_ctx* c, double z, const float* delt
   CTX_CUDA(c, cudaMemcpyAsync(c->d_delta, delta, bf, cudaMemcpyHostToDevice, st));
   if ((rc = enqueue_front(c, z, SF21_SRC_RION, c->d_delta, c->d_src, st))) return rc;
   return run_sets_to_host(c, st, xhii, neutral);
+}
+
+// ---- power spectrum (tools/power3d_f.c:124-194) -------------------------------
+// Window factor per axis, the reference's wind() (power3d_f.c:205-211).
+static double pk_axis_window(int x, int n, int flag) {
+  const double m = (double)(n - 1);
+  if (flag == 1) return 1 - fabs(x - m / 2.) / m * 2.;
+  if (flag == 2) return 1 - ((x - m / 2.) / m * 2.) * ((x - m / 2.) / m * 2.);
+  return 1.0;
+}
+
+static int power_spectrum_device(sf21_hii_ctx* c, const float* box_dev, int flag, double dl, double* k, double* P,
+                                 int cap, cudaStream_t st, int* nk_out) {
+  if (!box_dev || !(dl > 0) || flag < 0 || flag > 2 || cap < 0 || (cap > 0 && (!k || !P)))
+    CTX_FAIL(c, SF21_E_ARG, "power spectrum: bad arguments");
+  const int N = (int)c->N;
+  const int nk = pk_nbins(N);
+  const int grid = pk_bin_grid(N);
+  if (!c->d_pk) CTX_CUDA(c, cudaMalloc(&c->d_pk, sizeof(float2) * c->n3));
+  if (!c->d_pk_w) CTX_CUDA(c, cudaMalloc(&c->d_pk_w, sizeof(float) * N));
+  if (!c->d_pk_part) CTX_CUDA(c, cudaMalloc(&c->d_pk_part, sizeof(float) * (size_t)grid * nk));
+  if (!c->d_pk_cnt) CTX_CUDA(c, cudaMalloc(&c->d_pk_cnt, sizeof(unsigned long long) * nk));
+  std::vector<float> wax(N);
+  double s1 = 0.;
+  for (int x = 0; x < N; ++x) {
+    const double w = pk_axis_window(x, N, flag);
+    wax[x] = (float)w;
+    s1 += w * w;
+  }
+  const double wsum = s1 * s1 * s1;  // the window is separable: sum of its square = product of the axis sums
+  float2* packed = c->d_work[0];
+  Batch none;
+  memset(&none, 0, sizeof(none));
+  CTX_CUDA(c, cudaMemcpyAsync(c->d_pk_w, wax.data(), sizeof(float) * N, cudaMemcpyHostToDevice, st));
+  CTX_CUDA(c, launch_pk_pack(N, box_dev, c->d_pk_w, packed, st));
+  CTX_CUDA(c, launch_fwd_rows(N, packed, c->d_pk, nullptr, c->d_tw, st));
+  CTX_CUDA(c, launch_cols(N, c->d_pk, none, 1, 1, false, c->d_tw, st));
+  CTX_CUDA(c, launch_cols(N, c->d_pk, none, 1, 0, false, c->d_tw, st));
+  CTX_CUDA(c, cudaMemsetAsync(c->d_pk_cnt, 0, sizeof(unsigned long long) * nk, st));
+  CTX_CUDA(c, launch_pk_bin(N, c->d_pk, nk, c->d_pk_part, c->d_pk_cnt, st));
+  std::vector<float> part((size_t)grid * nk);
+  std::vector<unsigned long long> cnt(nk);
+  CTX_CUDA(c, cudaMemcpyAsync(part.data(), c->d_pk_part, sizeof(float) * part.size(), cudaMemcpyDeviceToHost, st));
+  CTX_CUDA(c, cudaMemcpyAsync(cnt.data(), c->d_pk_cnt, sizeof(unsigned long long) * nk, cudaMemcpyDeviceToHost, st));
+  CTX_CUDA(c, cudaStreamSynchronize(st));
+  const double dk = 2.0 * kPI / (N * dl);
+  const double dl3 = dl * dl * dl;
+  for (int b = 0; b < nk && b < cap; ++b) {
+    double sum = 0.;
+    for (int g = 0; g < grid; ++g) sum += (double)part[(size_t)g * nk + b];
+    const double n = cnt[b] ? (double)cnt[b] : 1.0;
+    k[b] = b * dk;
+    P[b] = sum / n / wsum * dl3;
+  }
+  *nk_out = nk;
+  return SF21_OK;
+}
+
+extern "C" int sf21_hii_power_spectrum_device(sf21_hii_ctx* c, const float* box_dev, int flag, double dl, double* k,
+                                              double* P, int cap, void* stream) {
+  if (!c) return -SF21_E_ARG;
+  if (cudaSetDevice(c->device) != cudaSuccess) return -SF21_E_CUDA;
+  int nk = 0;
+  const int rc =
+      power_spectrum_device(c, box_dev, flag, dl, k, P, cap, stream ? (cudaStream_t)stream : c->stream, &nk);
+  return rc ? -rc : nk;  // nk >= 1, or minus a status code
+}
+
+extern "C" int sf21_hii_power_spectrum(sf21_hii_ctx* c, const float* box, int flag, double dl, double* k, double* P,
+                                       int cap) {
+  if (!c || !box) return -SF21_E_ARG;
+  if (cudaSetDevice(c->device) != cudaSuccess) return -SF21_E_CUDA;
+  if (cudaMemcpyAsync(c->d_delta, box, sizeof(float) * c->n3, cudaMemcpyHostToDevice, c->stream) != cudaSuccess) {
+    c->err = "power spectrum: box upload failed";
+    return -SF21_E_CUDA;
+  }
+  int nk = 0;
+  const int rc = power_spectrum_device(c, c->d_delta, flag, dl, k, P, cap, c->stream, &nk);
+  return rc ? -rc : nk;
 }

@@ -116,6 +116,14 @@ int halo_source_noalloc(double z, long N_halo, long N_smooth, long nh, const voi
 // Error text of the context-free entry points (hii_api.cu).
 void set_global_error(const char* msg);
 
+// Power spectrum (kernels_pk.cu): window into a complex box, spherical binning
+// of |F|^2 over the half-spectrum (per-CTA float sums, exact counts).
+int pk_nbins(int N);
+int pk_bin_grid(int N);
+cudaError_t launch_pk_pack(int N, const float* box, const float* wax, float2* out, cudaStream_t st);
+cudaError_t launch_pk_bin(int N, const float2* spec, int nk, float* partials, unsigned long long* counts,
+                          cudaStream_t st);
+
 // Plain form (kernels_plain.cu).
 cudaError_t launch_plain_centres(long n3, const float2* box, const float* alpha, float zmul, float* mask, int* flag,
                                  cudaStream_t st);

@@ -30,7 +30,7 @@ EXPORTS = [
     "sf21_hii_first_hit", "sf21_hii_run_z_plain_device", "sf21_hii_criterion", "sf21_hii_criterion_device",
     "sf21_hii_vjp", "sf21_hii_vjp_device", "sf21_hii_path", "sf21_hii_check", "sf21_hii_halo_source",
     "sf21_hii_run_z_halos", "sf21_hii_profile", "sf21_hii_profile_read", "sf21_hii_profile_name",
-    "sf21_hii_halo_source_noalloc",
+    "sf21_hii_halo_source_noalloc", "sf21_hii_power_spectrum", "sf21_hii_power_spectrum_device",
 ]
 
 
@@ -87,6 +87,8 @@ def load_library(path: str = LIB_PATH):
     L.sf21_hii_run_z_halos.argtypes = [vp, ctypes.c_double, fp, ctypes.c_long, vp, fp, dp]
     L.sf21_hii_halo_source_noalloc.argtypes = [ctypes.c_double, ctypes.c_long, ctypes.c_long, ctypes.c_long,
                                                vp, vp, vp]
+    L.sf21_hii_power_spectrum.argtypes = [vp, fp, ctypes.c_int, ctypes.c_double, dp, dp, ctypes.c_int]
+    L.sf21_hii_power_spectrum_device.argtypes = [vp, vp, ctypes.c_int, ctypes.c_double, dp, dp, ctypes.c_int, vp]
     L.sf21_hii_check.argtypes = [vp]
     L.sf21_hii_profile.argtypes = [vp, ctypes.c_int]
     L.sf21_hii_profile_read.argtypes = [vp, dp, ctypes.POINTER(ctypes.c_long), ctypes.c_int]
@@ -209,6 +211,30 @@ class FilterBank:
         self._check(self._lib.sf21_hii_run_z_plain_device(self._h, z, src_kind, ctypes.c_void_p(delta_ptr),
                                                           ctypes.c_void_p(src_ptr), s, ctypes.c_void_p(xhii_ptr),
                                                           ctypes.c_void_p(stream or None)))
+
+    # ---- power spectrum (tools/power3d_f.c) ----------------------------------
+    def power_spectrum(self, box, dl: float, flag: int = 0):
+        """(k, P(k)) of an N^3 float box as tools/power3d_f.c computes it
+        (flag: 0 top hat, 1 Bartlett, 2 Welch window)."""
+        b = _f32(box, self.n3)
+        cap = 2 * self.N
+        k = (ctypes.c_double * cap)()
+        P = (ctypes.c_double * cap)()
+        n = self._lib.sf21_hii_power_spectrum(self._h, _ptr(b), flag, dl, k, P, cap)
+        if n < 0:
+            self._check(-n)
+        return np.array(k[:n]), np.array(P[:n])
+
+    def power_spectrum_device(self, box_ptr: int, dl: float, flag: int = 0, stream: int = 0):
+        """The same for a device box (pointer); returns after the stream finished."""
+        cap = 2 * self.N
+        k = (ctypes.c_double * cap)()
+        P = (ctypes.c_double * cap)()
+        n = self._lib.sf21_hii_power_spectrum_device(self._h, ctypes.c_void_p(box_ptr), flag, dl, k, P, cap,
+                                                     ctypes.c_void_p(stream or None))
+        if n < 0:
+            self._check(-n)
+        return np.array(k[:n]), np.array(P[:n])
 
     # ---- halo-catalogue source (use_SFR = F) ---------------------------------
     def halo_source(self, z: float, catalogue: np.ndarray) -> np.ndarray:

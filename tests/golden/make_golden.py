@@ -8,6 +8,8 @@ compressed .npz files next to this script:
   hii_n32_sfr.npz   N=32,  L=25 Mpc/h, z = 7, 8 (SFR boxes, use_SFR = T)
   hii_n64_sfr.npz   N=64,  L=50 Mpc/h, z = 8
   hii_n32_halo.npz  N=32 (N_halo=64), L=25 Mpc/h, z = 8 (halo catalogue, use_SFR = F)
+  pk_n32.npz        power3d_f on a 32^3 lognormal box, dl = 0.75, window flags 0, 1, 2
+  pk_n64.npz        power3d_f on a 64^3 lognormal box, dl = 1.5, Bartlett window
 
 Each holds the ini values, the input boxes per redshift, the xHII boxes the
 reference wrote, and its x_HI text output.  Needs the reference sources (only
@@ -90,7 +92,32 @@ def case_halo(name: str, N: int, N_halo: int, L: float, z: float, seed: int):
         shutil.rmtree(base)
 
 
+def case_pk(name: str, N: int, dl: float, seed: int, flags=(0, 1, 2)):
+    """The reference's power-spectrum tool (tools/power3d_f.c, built by
+    ``make -C oracle ref``) on a seeded lognormal density box: input box and,
+    per window flag, the printed output (text, k and P columns)."""
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True)
+    box = synth.lognormal_delta(synth.gaussian_field(N, seed), 0.8).astype(np.float32)
+    tmp = tempfile.mkdtemp(prefix="sf21pk_")
+    try:
+        path = os.path.join(tmp, "box.dat")
+        box.tofile(path)
+        out = {"box": box, "dl": np.float64(dl), "flags": np.array(flags)}
+        for f in flags:
+            r = subprocess.run([O.PK_EXE, "4", str(N), str(N), str(N), repr(dl), str(f), path, "4"],
+                               capture_output=True, text=True, check=True)
+            rows = [ln.split() for ln in r.stdout.splitlines() if ln and not ln.startswith("#")]
+            out[f"text_{f}"] = r.stdout.replace(path, "box.dat")
+            out[f"k_{f}"] = np.array([float(x[0]) for x in rows])
+            out[f"P_{f}"] = np.array([float(x[1]) for x in rows])
+        np.savez_compressed(os.path.join(HERE, name), **out)
+    finally:
+        shutil.rmtree(tmp)
+
+
 if __name__ == "__main__":
     case_sfr("hii_n32_sfr.npz", 32, 25.0, 7.0, 8.0, seed=101)
     case_sfr("hii_n64_sfr.npz", 64, 50.0, 8.0, 8.0, seed=202)
     case_halo("hii_n32_halo.npz", 32, 64, 25.0, 8.0, seed=303)
+    case_pk("pk_n32.npz", 32, 0.75, seed=404)
+    case_pk("pk_n64.npz", 64, 1.5, seed=505, flags=(1,))
