@@ -1,5 +1,6 @@
 /*
- * FFTW3 single-precision API subset, implemented by fftw_shim.c.
+ * FFTW3 API subset (single precision, and the double-precision twin used by
+ * the reference's t21.c), implemented by fftw_shim.c.
  *
  * ORACLE / TEST INFRASTRUCTURE ONLY.  FFTW3 is not installed in the build
  * container nor on the GPU host, so this header lets the reference's own
@@ -50,6 +51,19 @@ fftwf_plan fftwf_plan_dft_c2r_3d(int n0, int n1, int n2, fftwf_complex *in,
                                  float *out, unsigned flags);
 void fftwf_execute(const fftwf_plan p);
 void fftwf_destroy_plan(fftwf_plan p);
+
+/* double precision (t21.c:104-111, 222, 243) */
+typedef double _Complex fftw_complex;
+typedef struct sf21_shim_plan_d *fftw_plan;
+void *fftw_malloc(size_t n);
+void fftw_free(void *p);
+int fftw_init_threads(void);
+void fftw_plan_with_nthreads(int nthreads);
+void fftw_cleanup_threads(void);
+fftw_plan fftw_plan_dft_r2c_3d(int n0, int n1, int n2, double *in, fftw_complex *out, unsigned flags);
+fftw_plan fftw_plan_dft_c2r_3d(int n0, int n1, int n2, fftw_complex *in, double *out, unsigned flags);
+void fftw_execute(const fftw_plan p);
+void fftw_destroy_plan(fftw_plan p);
 
 #ifdef __cplusplus
 }
