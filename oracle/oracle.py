@@ -15,6 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libsf21oracle.so")
 REF_EXE = os.path.join(HERE, "_ref", "get_HIIbubbles.x")
 PK_EXE = os.path.join(HERE, "_ref", "power3d_f.x")  # tools/power3d_f.c, built by make ref
+T21_EXE = os.path.join(HERE, "_ref", "t21.x")  # t21.c, built by make ref
 
 
 class _Params(ctypes.Structure):

@@ -10,6 +10,8 @@ compressed .npz files next to this script:
   hii_n32_halo.npz  N=32 (N_halo=64), L=25 Mpc/h, z = 8 (halo catalogue, use_SFR = F)
   pk_n32.npz        power3d_f on a 32^3 lognormal box, dl = 0.75, window flags 0, 1, 2
   pk_n64.npz        power3d_f on a 64^3 lognormal box, dl = 1.5, Bartlett window
+  t21_n32.npz       t21.c on 32^3 boxes, z = 9, 8, 7, Lya/X-rays off, Vel_comp 3
+  t21_n32_lya.npz   the same with Lya/X-rays on (Zminsfr = 8), Vel_comp 1
 
 Each holds the ini values, the input boxes per redshift, the xHII boxes the
 reference wrote, and its x_HI text output.  Needs the reference sources (only
@@ -115,9 +117,60 @@ def case_pk(name: str, N: int, dl: float, seed: int, flags=(0, 1, 2)):
         shutil.rmtree(tmp)
 
 
+def case_t21(name: str, N: int, L: float, seed: int, vel_comp: int, lya: bool):
+    """The reference's t21.c (built by ``make -C oracle ref``) on a seeded base
+    directory: density and xHII boxes for z = 9, 8, 7 and, with Lya/X-rays on
+    (Zminsfr = 8, so z = 9 and 8 use them), x_c, x_alpha and T_K boxes.
+    Stores the inputs, the deltaTb boxes and the two text outputs."""
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True)
+    w = synth.Workload(N=N, L=L, zs=[], zeta=30.0, Rmax=L / 2, factor=1.1, seed=seed)
+    base = tempfile.mkdtemp(prefix="sf21t21_")
+    rng = np.random.default_rng(seed)
+    try:
+        ini = synth.ini_text(w, 7.0, 9.0, 1.0, nthreads=4)
+        ini += f"Vel_comp = {vel_comp}\nuse_Lya_xrays = {'T' if lya else 'F'}\nZminsfr = 8.0\n"
+        with open(os.path.join(base, "simfast21.ini"), "w") as f:
+            f.write(ini)
+        for d in ("delta", "Ionization", "Output_text_files", "x_c", "Lya", "xrays"):
+            os.makedirs(os.path.join(base, d), exist_ok=True)
+        out = {"ini": ini, "zs": np.array([9.0, 8.0, 7.0]), "vel_comp": np.int64(vel_comp), "lya": np.int64(lya)}
+        g = synth.gaussian_field(N, seed)
+        Lmpc = L / w.hubble
+        for z in (9.0, 8.0, 7.0):
+            delta = synth.lognormal_delta(g, 0.8 * synth.growth(z) / synth.growth(8.0)).astype(np.float32)
+            xhii = np.clip(rng.random(delta.shape) * 1.6 - 0.3, 0.0, 1.0).astype(np.float32)
+            tag = f"z{z:.3f}_N{N}_L{Lmpc:.1f}.dat"
+            delta.tofile(os.path.join(base, "delta", "deltanl_" + tag))
+            xhii.tofile(os.path.join(base, "Ionization", "xHII_" + tag))
+            out[f"delta_{z:.0f}"] = delta
+            out[f"xhii_{z:.0f}"] = xhii
+            if lya:
+                xc = (rng.random(delta.shape) * 0.5).astype(np.float32)
+                xa = (rng.random(delta.shape) * 2.0).astype(np.float32)
+                tk = (10.0 + rng.random(delta.shape) * 500.0).astype(np.float32)
+                xc.tofile(os.path.join(base, "x_c", "xc_" + tag))
+                xa.tofile(os.path.join(base, "Lya", "xalpha_" + tag))
+                tk.tofile(os.path.join(base, "xrays", "TempX_" + tag))
+                out[f"xc_{z:.0f}"], out[f"xalpha_{z:.0f}"], out[f"tempx_{z:.0f}"] = xc, xa, tk
+        r = subprocess.run([O.T21_EXE, base], capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(r.stdout + r.stderr)
+        for z in (9.0, 8.0, 7.0):
+            tag = f"z{z:.3f}_N{N}_L{Lmpc:.1f}.dat"
+            out[f"tb_{z:.0f}"] = np.fromfile(os.path.join(base, "deltaTb", "deltaTb_" + tag), dtype=np.float32)
+        txt = os.path.join(base, "Output_text_files")
+        out["t21_av_txt"] = open(os.path.join(txt, f"t21_av_N{N}_L{Lmpc:.1f}.dat")).read()
+        out["TS_av_txt"] = open(os.path.join(txt, f"TS_av_N{N}_L{Lmpc:.1f}.dat")).read()
+        np.savez_compressed(os.path.join(HERE, name), **out)
+    finally:
+        shutil.rmtree(base)
+
+
 if __name__ == "__main__":
     case_sfr("hii_n32_sfr.npz", 32, 25.0, 7.0, 8.0, seed=101)
     case_sfr("hii_n64_sfr.npz", 64, 50.0, 8.0, 8.0, seed=202)
     case_halo("hii_n32_halo.npz", 32, 64, 25.0, 8.0, seed=303)
     case_pk("pk_n32.npz", 32, 0.75, seed=404)
     case_pk("pk_n64.npz", 64, 1.5, seed=505, flags=(1,))
+    case_t21("t21_n32.npz", 32, 25.0, seed=606, vel_comp=3, lya=False)
+    case_t21("t21_n32_lya.npz", 32, 25.0, seed=707, vel_comp=1, lya=True)
