@@ -415,6 +415,24 @@ def run_ours(args, w, rank, world):
                                   "sample": "restatement of tools/power3d_f.c (numpy/scipy float32 FFT), "
                                             "same box"}
 
+    # 21-cm brightness temperature of the density box with set 0's xHII
+    # (t21.c, Lya/X-rays off): host boxes in and out through sf21_t21_run_z,
+    # and the restatement of t21.c (double, numpy) on the host as its baseline
+    t21 = None
+    if not args.no_pk:
+        xh = np.ascontiguousarray(x[0])
+        fb.t21(w["z"], delta, xh)
+        t0 = time.perf_counter()
+        fb.t21(w["z"], delta, xh)
+        g_ms = (time.perf_counter() - t0) * 1e3
+        t21 = {"N": N, "gpu_ms_host_buffers": g_ms}
+        if rank == 0 and not args.no_cpu_baseline:
+            from oracle import t21_oracle as T
+            t0 = time.perf_counter()
+            T.t21_box(w["z"], delta, xh, w["L"], T.Cosmo(0.27, 0.046, 0.73, w["hubble"]), 3)
+            t21["cpu_baseline"] = {"ms": (time.perf_counter() - t0) * 1e3, "cores": os.cpu_count() or 1,
+                                   "kind": "port", "sample": "restatement of t21.c (numpy, double), same boxes"}
+
     # CPU baseline (rank 0 only)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -451,6 +469,7 @@ def run_ours(args, w, rank, world):
             "plain_gpu": plain,
             "differentiation": grad,
             "power_spectrum": pk,
+            "t21": t21,
             "cpu_baseline": cpu,
         }
         print(json.dumps(out))
@@ -466,7 +485,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--kmax", type=int, default=0, help="radii per spectrum read (0 = library default)")
     ap.add_argument("--no-grad", action="store_true", help="skip the bwd/fwd measurement")
-    ap.add_argument("--no-pk", action="store_true", help="skip the power-spectrum measurement")
+    ap.add_argument("--no-pk", action="store_true", help="skip the power-spectrum and 21-cm measurements")
     ap.add_argument("--grad-large", action="store_true", help="also time fwd+bwd at 1024^3 (peak HBM)")
     ap.add_argument("--path", type=int, default=0,
                     help="radius pipeline: 0 = tuned, else one of PIPELINES")

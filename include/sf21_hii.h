@@ -155,6 +155,25 @@ int sf21_hii_power_spectrum(sf21_hii_ctx *ctx, const float *box, int flag, doubl
 int sf21_hii_power_spectrum_device(sf21_hii_ctx *ctx, const float *box_dev, int flag, double dl, double *k,
                                    double *P, int cap, void *stream);
 
+/* 21-cm brightness temperature of one redshift, the reference's t21.c:114-255
+ * on a context of the box's size: line-of-sight velocity gradient of the
+ * density (FFT, k_axis^2/k^2 with axis = vel_comp: 1 first index, 2 second,
+ * else third; inverse; times -dD/dt / L^3 / H(z) dx^3 / D(z); clamped to
+ * [-0.5, 1]), spin-temperature factor (1 when xc, xalpha and tempx are NULL,
+ * i.e. Lya/X-rays off or z below Zminsfr; else x/(1+x) (1 - Tcmb/TK), x = xc +
+ * xalpha), T_b = 23 mK (1 + delta) t / (1 + dv) (0.7/h) (Omega_b h^2/0.02)
+ * sqrt(0.15/Omega_m/h^2 (1+z)/10) (1 - xHII), in K, as float.  Host boxes of
+ * N^3 floats; *tb_mean and *ts_mean (may be NULL) receive the box means of
+ * T_b and of Tcmb/(1 - t) (the latter only with the spin boxes).  Growth,
+ * dD/dt and H(z) are computed on the host as auxiliary.c:224-291 does. */
+typedef struct {
+  double omega_m, omega_b, omega_lambda; /* omega_matter, omega_baryon, omega_lambda */
+  int vel_comp;                          /* Vel_comp */
+} sf21_t21_cosmo;
+int sf21_t21_run_z(sf21_hii_ctx *ctx, const sf21_t21_cosmo *cosmo, double z, const float *delta, const float *xhii,
+                   const float *xc, const float *xalpha, const float *tempx, float *tb, double *tb_mean,
+                   double *ts_mean);
+
 /* Radius list of a set exactly as the reference iterates it (:192, 298-461):
  * writes up to cap radii (Mpc/h, descending), returns the count (or <0 on
  * error); *n_fft receives how many take the FFT branch (R >= 2 dx). */

@@ -116,6 +116,9 @@ struct sf21_hii_ctx {
   float* d_pk_w = nullptr;
   float* d_pk_part = nullptr;
   unsigned long long* d_pk_cnt = nullptr;
+  // 21-cm brightness-temperature buffers (allocated on first use)
+  float* d_t21 = nullptr;  // xc, xalpha, TK, T_b boxes
+  float* d_t21_part = nullptr;
   void* d_hscratch = nullptr;
   size_t hscratch_bytes = 0;
   // plain-form buffers (allocated on first use)
@@ -217,7 +220,7 @@ static void free_ctx(sf21_hii_ctx* c) {
                   c->d_xhii, c->d_spec, c->d_tw, c->d_rc, c->d_mask, c->d_flag, c->d_box2,
                   c->d_C, c->d_A, c->d_acc, c->d_zpart, c->d_g, c->d_gd, c->d_gs, c->d_halos, c->d_fine,
                   c->d_hscratch, c->d_chain, c->d_om, c->d_xhii2, c->d_pk, c->d_pk_w, c->d_pk_part,
-                  c->d_pk_cnt};
+                  c->d_pk_cnt, c->d_t21, c->d_t21_part};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->d_work_base) cudaFree(c->d_work_base);
@@ -1221,4 +1224,91 @@ extern "C" int sf21_hii_power_spectrum(sf21_hii_ctx* c, const float* box, int fl
   int nk = 0;
   const int rc = power_spectrum_device(c, c->d_delta, flag, dl, k, P, cap, c->stream, &nk);
   return rc ? -rc : nk;
+}
+
+// ---- 21-cm brightness temperature (t21.c:114-255) ----------------------------
+namespace {
+constexpr double kH0 = 3.24078e-18;  // h/sec, Input_variables.h:108
+constexpr double kTcmb0 = 2.725;     // K, t21.c:25
+struct T21Cosmo {
+  double om, ob, ol, h;
+  double Hz(double z) const { return h * kH0 * sqrt(om * (1. + z) * (1. + z) * (1. + z) + ol); }  // auxiliary.c:224
+  double int_growth(double zz) const {  // auxiliary.c:243-257
+    const double dz = 0.001;
+    double intg = 0., z;
+    const double hz0 = Hz(0.);
+    for (z = zz + dz / 2.; z < zz + 100.; z += dz) {
+      const double hub = Hz(z) / hz0;
+      intg += (1. + z) / hub / hub / hub;
+    }
+    return intg * dz;
+  }
+  double growth(double z) const { return Hz(z) / Hz(0) * int_growth(z) / int_growth(0.); }  // :262-266
+  double dgrowth_dt(double z) const {  // :285-291, dz/dt = -H(z) (1 + z)
+    const double dz = 1e-3;
+    return (growth(z + dz / 2.) - growth(z - dz / 2.)) / dz * (-Hz(z) * (1.0 + z));
+  }
+};
+}  // namespace
+
+extern "C" int sf21_t21_run_z(sf21_hii_ctx* c, const sf21_t21_cosmo* cosmo, double z, const float* delta,
+                              const float* xhii, const float* xc, const float* xalpha, const float* tempx,
+                              float* tb, double* tb_mean, double* ts_mean) {
+  if (!c) return SF21_E_ARG;
+  if (!cosmo || !delta || !xhii || !tb) CTX_FAIL(c, SF21_E_ARG, "t21: null argument");
+  const bool spin = xc != nullptr;
+  if (spin != (xalpha != nullptr) || spin != (tempx != nullptr))
+    CTX_FAIL(c, SF21_E_ARG, "t21: xc, xalpha and tempx must be all given or all NULL");
+  CTX_CUDA(c, cudaSetDevice(c->device));
+  cudaStream_t st = c->stream;
+  const long n3 = c->n3;
+  const int N = (int)c->N;
+  const size_t bf = sizeof(float) * n3;
+  const int nb = t21_blocks(n3);
+  if (!c->d_pk) CTX_CUDA(c, cudaMalloc(&c->d_pk, sizeof(float2) * n3));
+  if (!c->d_t21) CTX_CUDA(c, cudaMalloc(&c->d_t21, 4 * bf));
+  if (!c->d_t21_part) CTX_CUDA(c, cudaMalloc(&c->d_t21_part, sizeof(float) * 2 * nb));
+  float* d_xc = c->d_t21;
+  float* d_xa = d_xc + n3;
+  float* d_tk = d_xa + n3;
+  float* d_tb = d_tk + n3;
+  CTX_CUDA(c, cudaMemcpyAsync(c->d_delta, delta, bf, cudaMemcpyHostToDevice, st));
+  CTX_CUDA(c, cudaMemcpyAsync(c->d_xhii, xhii, bf, cudaMemcpyHostToDevice, st));
+  if (spin) {
+    CTX_CUDA(c, cudaMemcpyAsync(d_xc, xc, bf, cudaMemcpyHostToDevice, st));
+    CTX_CUDA(c, cudaMemcpyAsync(d_xa, xalpha, bf, cudaMemcpyHostToDevice, st));
+    CTX_CUDA(c, cudaMemcpyAsync(d_tk, tempx, bf, cudaMemcpyHostToDevice, st));
+  }
+  // scalars in double on the host, as the reference
+  const T21Cosmo cs{cosmo->omega_m, cosmo->omega_b, cosmo->omega_lambda, c->hubble};
+  const double L = c->L, dx = c->dx, h = c->hubble;
+  T21Args ta;
+  ta.scale = (float)(-cs.dgrowth_dt(z) / L / L / L / cs.Hz(z) * dx * dx * dx / cs.growth(z));
+  ta.pref = (float)(23.0 / 1000. * (0.7 / h) * (cs.ob * h * h / 0.02) * sqrt((0.15 / cs.om / h / h) * (1. + z) / 10.));
+  ta.tcmb = (float)(kTcmb0 * (1. + z));
+  Batch none;
+  memset(&none, 0, sizeof(none));
+  float2* packed = c->d_work[0];
+  CTX_CUDA(c, launch_t21_pack(n3, c->d_delta, packed, st));
+  CTX_CUDA(c, launch_fwd_rows(N, packed, c->d_pk, nullptr, c->d_tw, st));
+  CTX_CUDA(c, launch_cols(N, c->d_pk, none, 1, 1, false, c->d_tw, st));
+  CTX_CUDA(c, launch_cols(N, c->d_pk, none, 1, 0, false, c->d_tw, st));
+  CTX_CUDA(c, launch_t21_kfilter(N, cosmo->vel_comp, c->d_pk, st));
+  CTX_CUDA(c, launch_inv_rows_plain(N, c->d_pk, c->d_tw, st));
+  CTX_CUDA(c, launch_cols(N, c->d_pk, none, 1, 1, true, c->d_tw, st));
+  CTX_CUDA(c, launch_cols(N, c->d_pk, none, 1, 0, true, c->d_tw, st));
+  CTX_CUDA(c, launch_t21_finish(n3, c->d_pk, c->d_delta, c->d_xhii, spin ? d_xc : nullptr, spin ? d_xa : nullptr,
+                                spin ? d_tk : nullptr, ta, d_tb, c->d_t21_part, st));
+  std::vector<float> part(2 * (size_t)nb);
+  CTX_CUDA(c, cudaMemcpyAsync(tb, d_tb, bf, cudaMemcpyDeviceToHost, st));
+  CTX_CUDA(c, cudaMemcpyAsync(part.data(), c->d_t21_part, sizeof(float) * part.size(), cudaMemcpyDeviceToHost, st));
+  CTX_CUDA(c, cudaStreamSynchronize(st));
+  double s_tb = 0., s_ts = 0.;
+  for (int b = 0; b < nb; ++b) {
+    s_tb += part[2 * b];
+    s_ts += part[2 * b + 1];
+  }
+  if (tb_mean) *tb_mean = s_tb / n3;
+  if (ts_mean) *ts_mean = spin ? s_ts / n3 : 0.0;
+  return SF21_OK;
 }

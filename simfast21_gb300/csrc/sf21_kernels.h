@@ -124,6 +124,22 @@ cudaError_t launch_pk_pack(int N, const float* box, const float* wax, float2* ou
 cudaError_t launch_pk_bin(int N, const float2* spec, int nk, float* partials, unsigned long long* counts,
                           cudaStream_t st);
 
+// 21-cm brightness temperature (kernels_t21.cu).
+struct T21Args {
+  float scale;  // -dg/dt / L^3 / H(z) dx^3 / D(z): Re(unnormalised inverse) -> dv
+  float pref;   // 23e-3 (0.7/h) (Omega_b h^2 / 0.02) sqrt(0.15/Omega_m/h^2 (1+z)/10)
+  float tcmb;   // Tcmb0 (1 + z)
+};
+int t21_blocks(long n3);
+cudaError_t launch_t21_pack(long n3, const float* delta, float2* out, cudaStream_t st);
+// axis: 1 = first index, 2 = second, otherwise the third (Vel_comp)
+cudaError_t launch_t21_kfilter(int N, int axis, float2* spec, cudaStream_t st);
+// xc, xalpha, tempx: all null (spin temperature >> Tcmb) or all set;
+// partials: 2 floats per block (sum of T_b, sum of Tcmb / (1 - t))
+cudaError_t launch_t21_finish(long n3, const float2* inv, const float* delta, const float* xhii, const float* xc,
+                              const float* xalpha, const float* tempx, const T21Args& ta, float* tb,
+                              float* partials, cudaStream_t st);
+
 // Plain form (kernels_plain.cu).
 cudaError_t launch_plain_centres(long n3, const float2* box, const float* alpha, float zmul, float* mask, int* flag,
                                  cudaStream_t st);

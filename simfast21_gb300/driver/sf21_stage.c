@@ -41,7 +41,14 @@ int sf21_read_params(const char *basedir, sf21_stage_params *p) {
       if (!strcmp(third, "F")) p->use_SFR = 0;
     } else if (!strcmp(first, "hii_param_sets")) {
       snprintf(p->param_sets_file, sizeof p->param_sets_file, "%s", third);
-    }
+    } else if (!strcmp(first, "omega_matter")) p->omega_m = atof(third);
+    else if (!strcmp(first, "omega_baryon")) p->omega_b = atof(third);
+    else if (!strcmp(first, "omega_lambda")) p->omega_l = atof(third);
+    else if (!strcmp(first, "Vel_comp")) p->vel_comp = atoi(third);
+    else if (!strcmp(first, "use_Lya_xrays")) {
+      if (!strcmp(third, "T")) p->use_Lya_xrays = 1;
+      if (!strcmp(third, "F")) p->use_Lya_xrays = 0;
+    } else if (!strcmp(first, "Zminsfr")) p->Zminsfr = atof(third);
   }
   fclose(f);
   /* Input_variables.c:121-133 */
@@ -49,6 +56,8 @@ int sf21_read_params(const char *basedir, sf21_stage_params *p) {
   p->bubble_Rmax = rmax_mpc * p->hubble;
   if (p->bubble_Rmax > p->L / 2.) p->bubble_Rmax = p->L / 2.;
   p->zmin = p->zmax - p->dz * (double)ceil((p->zmax - p->zmin) / p->dz);
+  p->Zminsfr = p->zmax - p->dz * (double)ceil((p->zmax - p->Zminsfr) / p->dz);
+  if (p->Zminsfr < p->zmin) p->Zminsfr = p->zmin;
   (void)kPI;
   return 0;
 }

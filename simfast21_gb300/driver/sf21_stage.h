@@ -17,9 +17,14 @@ typedef struct {
   int bubble_Nbins;
   int use_SFR;
   char param_sets_file[512]; /* optional key hii_param_sets (batched sets) */
+  /* keys of the 21-cm stage (t21.c) */
+  double omega_m, omega_b, omega_l; /* omega_matter, omega_baryon, omega_lambda */
+  int vel_comp;                     /* Vel_comp */
+  int use_Lya_xrays;                /* use_Lya_xrays (default F, Input_variables.c:35) */
+  double Zminsfr;                   /* re-snapped as Input_variables.c:134-137 */
 } sf21_stage_params;
 
-/* Input_variables.c:16-141 restricted to the keys of the HII stage.
+/* Input_variables.c:16-141 restricted to the keys of the HII and 21-cm stages.
  * Returns 0, or nonzero if the file is missing or malformed. */
 int sf21_read_params(const char *basedir, sf21_stage_params *p);
 

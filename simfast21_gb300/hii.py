@@ -31,6 +31,7 @@ EXPORTS = [
     "sf21_hii_vjp", "sf21_hii_vjp_device", "sf21_hii_path", "sf21_hii_check", "sf21_hii_halo_source",
     "sf21_hii_run_z_halos", "sf21_hii_profile", "sf21_hii_profile_read", "sf21_hii_profile_name",
     "sf21_hii_halo_source_noalloc", "sf21_hii_power_spectrum", "sf21_hii_power_spectrum_device",
+    "sf21_t21_run_z",
 ]
 
 
@@ -45,6 +46,11 @@ class HIIError(RuntimeError):
 
 class _Set(ctypes.Structure):
     _fields_ = [("fesc", ctypes.c_double), ("Rmax", ctypes.c_double), ("Nbins", ctypes.c_int)]
+
+
+class T21Cosmo(ctypes.Structure):
+    _fields_ = [("omega_m", ctypes.c_double), ("omega_b", ctypes.c_double), ("omega_lambda", ctypes.c_double),
+                ("vel_comp", ctypes.c_int)]
 
 
 class _Config(ctypes.Structure):
@@ -89,6 +95,7 @@ def load_library(path: str = LIB_PATH):
                                                vp, vp, vp]
     L.sf21_hii_power_spectrum.argtypes = [vp, fp, ctypes.c_int, ctypes.c_double, dp, dp, ctypes.c_int]
     L.sf21_hii_power_spectrum_device.argtypes = [vp, vp, ctypes.c_int, ctypes.c_double, dp, dp, ctypes.c_int, vp]
+    L.sf21_t21_run_z.argtypes = [vp, ctypes.POINTER(T21Cosmo), ctypes.c_double, fp, fp, fp, fp, fp, fp, dp, dp]
     L.sf21_hii_check.argtypes = [vp]
     L.sf21_hii_profile.argtypes = [vp, ctypes.c_int]
     L.sf21_hii_profile_read.argtypes = [vp, dp, ctypes.POINTER(ctypes.c_long), ctypes.c_int]
@@ -235,6 +242,22 @@ class FilterBank:
         if n < 0:
             self._check(-n)
         return np.array(k[:n]), np.array(P[:n])
+
+    # ---- 21-cm brightness temperature (t21.c) -------------------------------
+    def t21(self, z: float, delta, xhii, omega_m=0.27, omega_b=0.046, omega_lambda=0.73, vel_comp=3,
+            xc=None, xalpha=None, tempx=None):
+        """(T_b box in K, mean T_b, mean TS or None) for one redshift; the spin
+        boxes xc, xalpha, tempx all given (Lya/X-rays) or all None."""
+        d = _f32(delta, self.n3)
+        x = _f32(xhii, self.n3)
+        spin = [None if a is None else _f32(a, self.n3) for a in (xc, xalpha, tempx)]
+        out = np.empty((self.N,) * 3, np.float32)
+        m_tb, m_ts = ctypes.c_double(0), ctypes.c_double(0)
+        cosmo = T21Cosmo(omega_m, omega_b, omega_lambda, vel_comp)
+        self._check(self._lib.sf21_t21_run_z(self._h, ctypes.byref(cosmo), z, _ptr(d), _ptr(x),
+                                             *[_ptr(a) for a in spin], _ptr(out), ctypes.byref(m_tb),
+                                             ctypes.byref(m_ts)))
+        return out, m_tb.value, (m_ts.value if xc is not None else None)
 
     # ---- halo-catalogue source (use_SFR = F) ---------------------------------
     def halo_source(self, z: float, catalogue: np.ndarray) -> np.ndarray:
