@@ -14,7 +14,9 @@
  *
  * Semantics follow the published FFTW3 interface: row-major n0 x n1 x n2,
  * r2c output n0 x n1 x (n2/2+1), transforms unnormalised, forward sign -1,
- * c2r sign +1.  FFTW's own version is unpinned (makefile:8-9 links
+ * c2r sign +1; an in-place plan (same array for input and output, as the
+ * halo finder's c2r at get_halos.c:143) uses FFTW's padded real layout,
+ * rows of 2 (n2/2+1) reals.  FFTW's own version is unpinned (makefile:8-9 links
  * -lfftw3f_omp -lfftw3f with no version), so parity is pinned on the
  * mathematics of the DFT, not on FFTW's rounding.
  */

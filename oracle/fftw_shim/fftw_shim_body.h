@@ -19,6 +19,7 @@ typedef struct {
 struct SPLAN {
   int kind; /* 0 = r2c, 1 = c2r */
   int n0, n1, n2, n2h;
+  long rs; /* real row stride: n2, or 2 (n2/2+1) for an in-place plan */
   SREAL *real;
   SCPX *cplx;
   S(line_plan) p0, p1, p2, p2half;
@@ -200,6 +201,7 @@ SPLAN_T API(plan_dft_r2c_3d)(int n0, int n1, int n2, SREAL *in,
   p->kind = 0;
   p->real = in;
   p->cplx = (SCPX *)out;
+  p->rs = ((void *)in == (void *)out) ? 2L * p->n2h : p->n2;
   return p;
 }
 
@@ -212,6 +214,7 @@ SPLAN_T API(plan_dft_c2r_3d)(int n0, int n1, int n2, SCOMPLEX_T *in,
   p->kind = 1;
   p->real = out;
   p->cplx = (SCPX *)in;
+  p->rs = ((void *)in == (void *)out) ? 2L * p->n2h : p->n2;
   return p;
 }
 
@@ -319,7 +322,7 @@ void API(execute)(const SPLAN_T p) {
       SCPX *scr = (SCPX *)malloc(sizeof(SCPX) * (size_t)p->n2);
 #pragma omp for schedule(static)
       for (long r = 0; r < rows; r++)
-        S(row_r2c)(p, p->real + r * p->n2, p->cplx + r * n2h, buf, scr);
+        S(row_r2c)(p, p->real + r * p->rs, p->cplx + r * n2h, buf, scr);
       free(buf);
       free(scr);
     }
@@ -334,7 +337,7 @@ void API(execute)(const SPLAN_T p) {
       SCPX *scr = (SCPX *)malloc(sizeof(SCPX) * (size_t)p->n2);
 #pragma omp for schedule(static)
       for (long r = 0; r < rows; r++)
-        S(row_c2r)(p, p->cplx + r * n2h, p->real + r * p->n2, buf, scr);
+        S(row_c2r)(p, p->cplx + r * n2h, p->real + r * p->rs, buf, scr);
       free(buf);
       free(scr);
     }

@@ -1,10 +1,13 @@
 /*
  * GSL integration API subset: types and prototypes only.
  *
- * ORACLE / TEST INFRASTRUCTURE ONLY.  GSL is not installed here.  The
- * reference's auxiliary.c:18 includes this header for sigmaR()
- * (auxiliary.c:377-398), which the HII stage never calls.  The bodies in
- * gsl_stub.c abort, so an accidental call fails loudly.
+ * ORACLE / TEST INFRASTRUCTURE ONLY.  GSL is not installed here (the
+ * reference's makefile links -lgsl with no version).  The reference's
+ * auxiliary.c:18 includes this header for sigmaR() (auxiliary.c:377-398),
+ * which integrates with gsl_integration_qag and the 15-point Gauss-Kronrod
+ * rule; the halo finder reaches it through sigma() (get_halos.c:213, 304,
+ * 335).  gsl_stub.c restates that published algorithm (QUADPACK QAG/QK15,
+ * Piessens et al. 1983).
  */
 #ifndef SF21_ORACLE_GSL_INTEGRATION_STUB_H
 #define SF21_ORACLE_GSL_INTEGRATION_STUB_H

@@ -305,3 +305,110 @@ def make_boxes_torch(N: int, L: float, z: float, seed: int, device="cuda", sigma
     sfrd = torch.zeros((N, N, N), device=device, dtype=torch.float32)
     sfrd[host] = (SOURCE_SCALE * sfr / dx ** 3).float()
     return delta.float().contiguous(), sfrd
+
+
+# ---- halo finder (get_halos.c) ---------------------------------------------
+@dataclass
+class HaloWorkload:
+    """A base directory for the halo finder: a seeded Gaussian z = 0 linear
+    density box (unit-variance field with P(k) ~ k^slope times sigma) and the
+    simfast21.ini keys get_halos.c reads (Input_variables.c:46-90)."""
+    N: int
+    L_mpc: float          # sim_length (Mpc); the code works in Mpc/h = L_mpc * hubble
+    sigma: float = 3.0    # rms of the z = 0 cell-scale density
+    seed: int = 1
+    hubble: float = 0.7
+    subgrid: bool = False
+    Mmin: float = 1e8
+    dlm: float = 0.2
+    slope: float = -2.0   # P(k) ~ k^slope of the Gaussian field
+    smooth: int = 0       # > 0: the integer field of hash_field instead (that many box passes)
+
+    def density(self) -> np.ndarray:
+        if self.smooth > 0:
+            return hash_field(self.N, self.seed, self.smooth, self.sigma)
+        return (gaussian_field(self.N, self.seed, self.slope) * self.sigma).astype(np.float32)
+
+
+def _splitmix64(x: np.ndarray) -> np.ndarray:
+    z = x + np.uint64(0x9E3779B97F4A7C15)
+    z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+    z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    return z ^ (z >> np.uint64(31))
+
+
+def hash_field(N: int, seed: int, passes: int, sigma: float) -> np.ndarray:
+    """A density box that every machine reproduces bit for bit: integer white
+    noise in [-512, 512) from the splitmix64 hash of (seed, cell), smoothed by
+    `passes` rounds of the periodic 3-point box sum along each axis (integer
+    arithmetic, |values| < 2^24), times the power of two that brings its rms
+    closest to sigma (so the float32 values are exact).  Smoothing moves power
+    to large scales, which gives the halo finder large spheres."""
+    if passes > 3:
+        raise ValueError("at most 3 smoothing passes keep the sums below 2^24")
+    t = np.arange(N ** 3, dtype=np.uint64) + np.uint64(seed) * np.uint64(N ** 3)
+    w = ((_splitmix64(t) >> np.uint64(54)).astype(np.int64) - 512).reshape(N, N, N)
+    for _ in range(passes):
+        for ax in range(3):
+            w = w + np.roll(w, 1, ax) + np.roll(w, -1, ax)
+    rms = float(np.sqrt(np.mean(w.astype(np.float64) ** 2)))
+    k = int(round(math.log2(rms / sigma)))
+    return (w.astype(np.float32) * np.float32(2.0 ** -k)).astype(np.float32)
+
+
+def halo_ini_text(w: HaloWorkload, zmin: float, zmax: float, dz: float, nthreads: int = 8) -> str:
+    return "\n".join([
+        "# synthetic workload for the halo finder",
+        f"nthreads = {nthreads}",
+        f"zmax = {zmax!r}",
+        f"zmin = {zmin!r}",
+        f"dz = {dz!r}",
+        f"sim_length = {w.L_mpc!r}",
+        f"N_halo = {w.N}",
+        f"N_smoothed = {max(w.N // 2, 16)}",
+        "omega_matter = 0.27",
+        "omega_baryon = 0.046",
+        "omega_lambda = 0.73",
+        f"hubble = {w.hubble!r}",
+        "spectral_index = 0.96",
+        "sigma8 = 0.81",
+        "critical_overdensity = 1.68",
+        "STa = 0.73",
+        "STb = 0.34",
+        "STc = 0.81",
+        f"Use_subgrid = {'T' if w.subgrid else 'F'}",
+        f"halo_Mmin = {w.Mmin!r}",
+        f"halo_dlm = {w.dlm!r}",
+        "",
+    ])
+
+
+def halo_density_name(N: int, L_mpc: float) -> str:
+    """get_halos.c:128 (%ld, %.1f of L/h in Mpc)."""
+    return f"delta/delta_z0_N{N}_L{L_mpc:.1f}.dat"
+
+
+def halo_catalogue_name(z: float, N: int, L_mpc: float) -> str:
+    """get_halos.c:173, 180 (%.3f, %ld, %.1f)."""
+    return f"Halos/halo_z{z:.3f}_N{N}_L{L_mpc:.1f}.dat.catalog"
+
+
+def halo_redshifts(zmin: float, zmax: float, dz: float):
+    """The redshifts get_halos.c visits (:169): zmin re-snapped as
+    Input_variables.c:133, then zmax downwards by repeated subtraction."""
+    zmin = zmax - dz * float(math.ceil((zmax - zmin) / dz))
+    zs = []
+    z = zmax
+    while z > zmin - dz / 10:
+        zs.append(z)
+        z -= dz
+    return zs
+
+
+def write_halo_base_dir(base: str, w: HaloWorkload, zmin: float, zmax: float, dz: float, nthreads: int = 8):
+    os.makedirs(os.path.join(base, "delta"), exist_ok=True)
+    with open(os.path.join(base, "simfast21.ini"), "w") as f:
+        f.write(halo_ini_text(w, zmin, zmax, dz, nthreads))
+    d = w.density()
+    d.tofile(os.path.join(base, halo_density_name(w.N, w.L_mpc)))
+    return d

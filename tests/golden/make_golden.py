@@ -12,11 +12,18 @@ compressed .npz files next to this script:
   pk_n64.npz        power3d_f on a 64^3 lognormal box, dl = 1.5, Bartlett window
   t21_n32.npz       t21.c on 32^3 boxes, z = 9, 8, 7, Lya/X-rays off, Vel_comp 3
   t21_n32_lya.npz   the same with Lya/X-rays on (Zminsfr = 8), Vel_comp 1
+  halos_n64.npz     get_halos.c, 64^3, L=40 Mpc, z = 8, 7, 6, no subgrid
+  halos_n128_dense.npz  get_halos.c, 128^3 smoothed integer-hash field (nc up
+                    to 8), L=100 Mpc, z = 2, 1: tens of thousands of halos
+  halos_n64_sgrid.npz  get_halos.c, 64^3 integer-hash field, L=40 Mpc, z = 8, 7,
+                    subgrid on (halo_Mmin 1e9)
+The integer-hash boxes (synth.hash_field) are rebuilt bit for bit from their
+recipe on any machine and are not stored.
 
 Each holds the ini values, the input boxes per redshift, the xHII boxes the
 reference wrote, and its x_HI text output.  Needs the reference sources (only
 in the build container); the GPU tests read the committed .npz files.
-Usage: python tests/golden/make_golden.py
+Usage: python tests/golden/make_golden.py [case-prefix ...]   (default: all)
 """
 from __future__ import annotations
 
@@ -166,11 +173,71 @@ def case_t21(name: str, N: int, L: float, seed: int, vel_comp: int, lya: bool):
         shutil.rmtree(base)
 
 
+def case_halos(name: str, w, zmin: float, zmax: float, dz: float, keep_full: int = 20000):
+    """The reference's get_halos.c (built by ``make -C oracle ref``) on a
+    seeded z = 0 density box.  Stores the ini, the box, and per redshift the
+    halo count, the SHA-256 of the catalogue records, the per-mass counts the
+    reference prints (:281, :320) and the records themselves (all of them up
+    to keep_full, else the first 4096)."""
+    import hashlib
+    import re
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True)
+    base = tempfile.mkdtemp(prefix="sf21halo_")
+    try:
+        delta = synth.write_halo_base_dir(base, w, zmin, zmax, dz, nthreads=4)
+        r = subprocess.run([os.path.join(ROOT, "oracle", "_ref", "get_halos.x"), base], capture_output=True,
+                           text=True)
+        if r.returncode != 0:
+            raise RuntimeError(r.stdout + r.stderr)
+        zs = synth.halo_redshifts(zmin, zmax, dz)
+        ini = open(os.path.join(base, "simfast21.ini")).read()
+        out = {"ini": ini, "zs": np.array(zs), "stdout": r.stdout, "N": np.int64(w.N), "L_mpc": np.float64(w.L_mpc),
+               "sigma": np.float64(w.sigma), "seed": np.int64(w.seed), "smooth": np.int64(w.smooth),
+               "slope": np.float64(w.slope)}
+        if w.smooth == 0:  # a Gaussian field is stored; synth.hash_field boxes are rebuilt from the recipe
+            out["delta"] = delta
+        blocks = r.stdout.split("+++++++++++++++++++++++++++ z = ")[1:]
+        for i, z in enumerate(zs):
+            raw = open(os.path.join(base, synth.halo_catalogue_name(z, w.N, w.L_mpc)), "rb").read()
+            n = int(np.frombuffer(raw[:8], np.int64)[0])
+            recs = np.frombuffer(raw[8:], dtype=[("Mass", "<f4"), ("x", "<f4"), ("y", "<f4"), ("z", "<f4")])
+            assert len(recs) == n
+            out[f"count_{i}"] = np.int64(n)
+            out[f"sha_{i}"] = hashlib.sha256(raw[8:]).hexdigest()
+            mc = re.findall(r"Number of halos for M=([0-9.E+-]+): (\d+)", blocks[i])
+            out[f"masscounts_{i}"] = np.array([[float(m), float(c)] for m, c in mc])
+            cell = re.findall(r"Number of halos found in cell size cycle: (\d+)", blocks[i])
+            out[f"cellcount_{i}"] = np.int64(cell[0]) if cell else np.int64(-1)
+            out[f"cat_{i}"] = recs.copy() if n <= keep_full else recs[:4096].copy()
+            print(name, "z =", z, "halos", n)
+        np.savez_compressed(os.path.join(HERE, name), **out)
+    finally:
+        shutil.rmtree(base)
+
+
+CASES = {
+    "hii_n32_sfr": lambda: case_sfr("hii_n32_sfr.npz", 32, 25.0, 7.0, 8.0, seed=101),
+    "hii_n64_sfr": lambda: case_sfr("hii_n64_sfr.npz", 64, 50.0, 8.0, 8.0, seed=202),
+    "hii_n32_halo": lambda: case_halo("hii_n32_halo.npz", 32, 64, 25.0, 8.0, seed=303),
+    "pk_n32": lambda: case_pk("pk_n32.npz", 32, 0.75, seed=404),
+    "pk_n64": lambda: case_pk("pk_n64.npz", 64, 1.5, seed=505, flags=(1,)),
+    "t21_n32": lambda: case_t21("t21_n32.npz", 32, 25.0, seed=606, vel_comp=3, lya=False),
+    "t21_n32_lya": lambda: case_t21("t21_n32_lya.npz", 32, 25.0, seed=707, vel_comp=1, lya=True),
+    "halos_n64": lambda: case_halos("halos_n64.npz", synth.HaloWorkload(N=64, L_mpc=40.0, sigma=3.0, seed=808),
+                                    6.0, 8.0, 1.0),
+    "halos_n128_dense": lambda: case_halos("halos_n128_dense.npz",
+                                           synth.HaloWorkload(N=128, L_mpc=100.0, sigma=4.0, seed=7, smooth=3),
+                                           1.0, 2.0, 1.0),
+    "halos_n64_sgrid": lambda: case_halos("halos_n64_sgrid.npz",
+                                          synth.HaloWorkload(N=64, L_mpc=40.0, sigma=3.0, seed=1010, smooth=1,
+                                                             subgrid=True, Mmin=1e9),
+                                          7.0, 8.0, 1.0),
+}
+
+
 if __name__ == "__main__":
-    case_sfr("hii_n32_sfr.npz", 32, 25.0, 7.0, 8.0, seed=101)
-    case_sfr("hii_n64_sfr.npz", 64, 50.0, 8.0, 8.0, seed=202)
-    case_halo("hii_n32_halo.npz", 32, 64, 25.0, 8.0, seed=303)
-    case_pk("pk_n32.npz", 32, 0.75, seed=404)
-    case_pk("pk_n64.npz", 64, 1.5, seed=505, flags=(1,))
-    case_t21("t21_n32.npz", 32, 25.0, seed=606, vel_comp=3, lya=False)
-    case_t21("t21_n32_lya.npz", 32, 25.0, seed=707, vel_comp=1, lya=True)
+    want = sys.argv[1:]
+    for key, fn in CASES.items():
+        if not want or any(key.startswith(w) for w in want):
+            fn()
+
