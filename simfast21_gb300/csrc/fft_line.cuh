@@ -40,6 +40,26 @@ struct LineGeom {
   static_assert((N & (N - 1)) == 0 && N >= 16 && N <= 1024, "N must be a power of two in [16, 1024]");
 };
 
+// CTA shapes of the line passes: contiguous-axis rows (T threads per row,
+// ROWS rows per CTA) and strided-axis tiles (N rows x CW contiguous columns).
+template <int N>
+struct RowGeom {
+  static constexpr int T = N / 8;
+  static constexpr int ROWS = (256 / T) > 0 ? (256 / T) : 1;  // rows per CTA
+  static constexpr int THREADS = T * ROWS;
+};
+
+template <int N>
+struct ColGeom {
+  static constexpr int CW = (N <= 512) ? 16 : 8;  // columns (contiguous c) per tile
+  static constexpr int THREADS = CW * (N / 8);
+};
+
+template <int N>
+__device__ __forceinline__ void load_twiddles(float2* stw, const float2* __restrict__ gtw) {
+  for (int t = threadIdx.x; t < N; t += blockDim.x) stw[t] = gtw[t];
+}
+
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {

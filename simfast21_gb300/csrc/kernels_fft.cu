@@ -26,24 +26,6 @@
 
 namespace sf21 {
 
-template <int N>
-struct RowGeom {
-  static constexpr int T = N / 8;
-  static constexpr int ROWS = (256 / T) > 0 ? (256 / T) : 1;  // rows per CTA
-  static constexpr int THREADS = T * ROWS;
-};
-
-template <int N>
-struct ColGeom {
-  static constexpr int CW = (N <= 512) ? 16 : 8;  // columns (contiguous c) per tile
-  static constexpr int THREADS = CW * (N / 8);
-};
-
-template <int N>
-__device__ __forceinline__ void load_twiddles(float2* stw, const float2* __restrict__ gtw) {
-  for (int t = threadIdx.x; t < N; t += blockDim.x) stw[t] = gtw[t];
-}
-
 // ---------------------------------------------------------------------------
 // Forward c-axis pass of the packed prologue output: z = (rec0, ion * alpha).
 template <int N>

@@ -140,6 +140,44 @@ cudaError_t launch_t21_finish(long n3, const float2* inv, const float* delta, co
                               const float* xalpha, const float* tempx, const T21Args& ta, float* tb,
                               float* partials, cudaStream_t st);
 
+// Excursion-set halo finder (kernels_hf.cu).
+constexpr int HF_KMAX = 4;  // mass pairs per filter-bank pass
+struct HfPair {
+  float dkRa, dkRb;    // dk R of the two masses (b unused when bits_b is null)
+  float thr_a, thr_b;  // candidate <=> filtered value > thr (largest float <= deltaCMZ)
+  float2* work;        // N^3 complex work box
+  uint32_t* bits_a;    // candidate bit sets, N^3 / 32 words each
+  uint32_t* bits_b;
+};
+struct HfBatch {
+  int K;
+  float scale;  // dx^3 / L^3 * growth (get_halos.c:225)
+  HfPair p[HF_KMAX];
+};
+// candidate states of the overlap test
+constexpr uint8_t HF_UND = 0, HF_PEND_ACC = 1, HF_PEND_REJ = 2, HF_ACC = 3, HF_ACC_FLAGGED = 4, HF_REJ = 5;
+cudaError_t hf_setup(int N);
+cudaError_t launch_hf_rows_filter(int N, const float2* spec, const HfBatch& hb, const float2* tw, cudaStream_t st);
+cudaError_t launch_hf_cols_a_thresh(int N, const HfBatch& hb, const float2* tw, cudaStream_t st);
+long hf_compact_chunks(long nwords);
+cudaError_t launch_bits_count(const uint32_t* W, long nwords, uint32_t* cnt, cudaStream_t st);
+cudaError_t launch_scan_counts(uint32_t* cnt, long n, uint32_t* tot, cudaStream_t st);
+cudaError_t launch_bits_emit(const uint32_t* W, long nwords, const uint32_t* off, uint32_t* out, cudaStream_t st);
+// runs: {di, dj, m, 0}: the cells (i+di, j+dj, p-m .. p+m) of a sphere (or of D)
+cudaError_t launch_hf_prefilter(const uint32_t* list, const uint32_t* n_ptr, int logN, const int4* runs, int nruns,
+                                const uint32_t* FL, uint32_t* UND, uint8_t* status, uint32_t* n_und, cudaStream_t st);
+cudaError_t launch_hf_round(const uint32_t* list, const uint32_t* n_ptr, int logN, const int4* druns, int ndruns,
+                            uint32_t* UND, uint32_t* ACC, uint8_t* status, uint32_t* n_und, cudaStream_t st);
+cudaError_t launch_hf_flag_accepted(const uint32_t* list, const uint32_t* n_ptr, int logN, const int4* runs,
+                                    int nruns, uint32_t* FL, uint8_t* status, cudaStream_t st);
+cudaError_t launch_hf_finisher(const uint32_t* list, const uint32_t* n_ptr, int logN, const int4* runs, int nruns,
+                               uint32_t* FL, uint32_t* ACC, uint8_t* status, cudaStream_t st);
+cudaError_t launch_hf_clear(const uint32_t* list, const uint32_t* n_ptr, uint32_t* UND, uint32_t* ACC,
+                            cudaStream_t st);
+cudaError_t launch_hf_cell(long nwords, const float* delta, float tcell, uint32_t* FL, uint32_t* bits,
+                           cudaStream_t st);
+cudaError_t launch_hf_records(const uint32_t* idx, long n, int logN, float mass, float4* out, cudaStream_t st);
+
 // Plain form (kernels_plain.cu).
 cudaError_t launch_plain_centres(long n3, const float2* box, const float* alpha, float zmul, float* mask, int* flag,
                                  cudaStream_t st);

@@ -49,6 +49,15 @@ int sf21_read_params(const char *basedir, sf21_stage_params *p) {
       if (!strcmp(third, "T")) p->use_Lya_xrays = 1;
       if (!strcmp(third, "F")) p->use_Lya_xrays = 0;
     } else if (!strcmp(first, "Zminsfr")) p->Zminsfr = atof(third);
+    else if (!strcmp(first, "sigma8")) p->sigma8 = atof(third);
+    else if (!strcmp(first, "spectral_index")) p->n_index = atof(third);
+    else if (!strcmp(first, "critical_overdensity")) p->delta_c = atof(third);
+    else if (!strcmp(first, "STa")) p->STa = atof(third);
+    else if (!strcmp(first, "STb")) p->STb = atof(third);
+    else if (!strcmp(first, "STc")) p->STc = atof(third);
+    else if (!strcmp(first, "Use_subgrid")) p->use_sgrid = !strcmp(third, "T");
+    else if (!strcmp(first, "halo_Mmin")) p->halo_Mmin = atof(third);
+    else if (!strcmp(first, "halo_dlm")) p->halo_dlm = atof(third);
   }
   fclose(f);
   /* Input_variables.c:121-133 */

@@ -22,9 +22,14 @@ typedef struct {
   int vel_comp;                     /* Vel_comp */
   int use_Lya_xrays;                /* use_Lya_xrays (default F, Input_variables.c:35) */
   double Zminsfr;                   /* re-snapped as Input_variables.c:134-137 */
+  /* keys of the halo finder (get_halos.c) */
+  double sigma8, n_index;           /* sigma8, spectral_index */
+  double delta_c, STa, STb, STc;    /* critical_overdensity, STa, STb, STc */
+  int use_sgrid;                    /* Use_subgrid (T -> 1, anything else 0) */
+  double halo_Mmin, halo_dlm;       /* halo_Mmin, halo_dlm */
 } sf21_stage_params;
 
-/* Input_variables.c:16-141 restricted to the keys of the HII and 21-cm stages.
+/* Input_variables.c:16-141 restricted to the keys of the HII, 21-cm and halo stages.
  * Returns 0, or nonzero if the file is missing or malformed. */
 int sf21_read_params(const char *basedir, sf21_stage_params *p);
 

@@ -26,12 +26,12 @@ def lib():
 
 
 def test_exports_every_declared_symbol(lib):
-    from simfast21_gb300 import hii
+    from simfast21_gb300 import halos, hii
     syms = declared_symbols()
     assert len(syms) >= 12
     for s in syms:
         assert hasattr(lib, s), s
-    assert sorted(hii.EXPORTS) == syms
+    assert sorted(hii.EXPORTS + halos.EXPORTS) == syms
 
 
 def test_no_cpu_fallback_without_gpu(lib):
