@@ -426,6 +426,23 @@ struct sf21_halo_ctx {
   std::vector<long> counts;
   std::vector<sf21_halo_mass> sched;
   uint32_t rng[3] = {0, 0, 0};
+  // subgrid cycle (allocated / grown on use)
+  uint32_t *d_sg_pow2 = nullptr, *d_sg_local = nullptr;
+  uint8_t* d_sgL = nullptr;
+  long sgL_cap = 0;
+  uint8_t *d_sgX = nullptr, *d_sgGX = nullptr, *d_sg_gentry = nullptr, *d_sg_bentry = nullptr;
+  uint16_t* d_sgD = nullptr;
+  uint32_t *d_sgGD = nullptr, *d_sg_cnt = nullptr;
+  uint64_t *d_sg_gbase = nullptr, *d_sg_bbase = nullptr;
+  long sg_blocks_cap = 0;
+  uint64_t* d_sg_dn = nullptr;
+  uint8_t* d_sg_dk = nullptr;
+  uint32_t *d_sg_cell = nullptr, *d_sg_nn = nullptr;
+  long sg_draw_cap = 0;
+  uint32_t *d_sg_wpre = nullptr, *d_sg_chunk = nullptr;
+  long sg_chunk_cap = 0;
+  uint64_t* d_sg_u64 = nullptr;  // [0] positions consumed, [1] draws available
+  int* d_sg_err = nullptr;
   std::string err;
 };
 
@@ -466,11 +483,63 @@ static void taus_seed(uint32_t seed, uint32_t s[3]) {
   s[2] = c;
 }
 
+// The generator's step T is linear over GF(2) in each 32-bit component:
+// a jump by q steps is the matrix power T^q (column k = image of bit k).
+struct TausMat {
+  uint32_t col[3][32];
+};
+
+static uint32_t gf2_apply_h(const uint32_t* col, uint32_t v) {
+  uint32_t r = 0;
+  for (int k = 0; k < 32; ++k)
+    if ((v >> k) & 1u) r ^= col[k];
+  return r;
+}
+
+static TausMat taus_identity() {
+  TausMat m;
+  for (int c = 0; c < 3; ++c)
+    for (int k = 0; k < 32; ++k) m.col[c][k] = 1u << k;
+  return m;
+}
+
+static TausMat taus_one_step() {
+  TausMat m;
+  for (int k = 0; k < 32; ++k) {
+    const uint32_t e = 1u << k;
+    m.col[0][k] = ((e & 4294967294u) << 12) ^ (((e << 13) ^ e) >> 19);
+    m.col[1][k] = ((e & 4294967288u) << 4) ^ (((e << 2) ^ e) >> 25);
+    m.col[2][k] = ((e & 4294967280u) << 17) ^ (((e << 3) ^ e) >> 11);
+  }
+  return m;
+}
+
+static TausMat taus_mul(const TausMat& a, const TausMat& b) {  // a b
+  TausMat r;
+  for (int c = 0; c < 3; ++c)
+    for (int k = 0; k < 32; ++k) r.col[c][k] = gf2_apply_h(a.col[c], b.col[c][k]);
+  return r;
+}
+
+static void taus_jump(uint32_t s[3], uint64_t q) {
+  TausMat p = taus_one_step();
+  while (q) {
+    if (q & 1)
+      for (int c = 0; c < 3; ++c) s[c] = gf2_apply_h(p.col[c], s[c]);
+    q >>= 1;
+    if (q) p = taus_mul(p, p);
+  }
+}
+
 static void free_hctx(sf21_halo_ctx* c) {
   if (!c) return;
   if (c->device >= 0) cudaSetDevice(c->device);
-  void* ptrs[] = {c->d_tw, c->d_spec, c->d_work, c->d_delta, c->d_FL, c->d_UND, c->d_ACC, c->d_bits,
-                  c->d_list, c->d_list2, c->d_status, c->d_chunk, c->d_cnt, c->d_cat, c->d_runs};
+  void* ptrs[] = {c->d_tw,        c->d_spec,      c->d_work,      c->d_delta,     c->d_FL,        c->d_UND,
+                  c->d_ACC,       c->d_bits,      c->d_list,      c->d_list2,     c->d_status,    c->d_chunk,
+                  c->d_cnt,       c->d_cat,       c->d_runs,      c->d_sg_pow2,   c->d_sg_local,  c->d_sgL,
+                  c->d_sgX,       c->d_sgGX,      c->d_sg_gentry, c->d_sg_bentry, c->d_sgD,       c->d_sgGD,
+                  c->d_sg_cnt,    c->d_sg_gbase,  c->d_sg_bbase,  c->d_sg_dn,     c->d_sg_dk,     c->d_sg_cell,
+                  c->d_sg_nn,     c->d_sg_wpre,   c->d_sg_chunk,  c->d_sg_u64,    c->d_sg_err};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (uint32_t* p : c->d_masks)
@@ -706,6 +775,175 @@ static int greedy_mass(sf21_halo_ctx* c, const MassPlan& mp, const uint32_t* can
   return SF21_OK;
 }
 
+template <class T>
+static int grow(sf21_halo_ctx* c, T** p, long n, long* cap, bool keep_cap_var = false) {
+  (void)keep_cap_var;
+  if (n <= *cap && *p) return SF21_OK;
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  HCTX_CUDA(c, cudaMalloc(p, sizeof(T) * (size_t)std::max(n, 1L)));
+  *cap = std::max(n, 1L);
+  return SF21_OK;
+}
+
+static int sg_tables(sf21_halo_ctx* c) {
+  if (c->d_sg_pow2) return SF21_OK;
+  std::vector<uint32_t> p2((size_t)SG_POW2 * 96), loc((size_t)SG_LOCAL * 96);
+  TausMat m = taus_one_step();
+  for (int k = 0; k < SG_POW2; ++k) {
+    for (int cc = 0; cc < 3; ++cc) memcpy(&p2[((size_t)k * 3 + cc) * 32], m.col[cc], 128);
+    m = taus_mul(m, m);
+  }
+  const TausMat t1 = taus_one_step();
+  const TausMat t4 = taus_mul(taus_mul(t1, t1), taus_mul(t1, t1));
+  TausMat acc = taus_identity();
+  for (int i = 0; i < SG_LOCAL; ++i) {
+    for (int cc = 0; cc < 3; ++cc) memcpy(&loc[((size_t)i * 3 + cc) * 32], acc.col[cc], 128);
+    acc = taus_mul(t4, acc);
+  }
+  HCTX_CUDA(c, cudaMalloc(&c->d_sg_pow2, sizeof(uint32_t) * p2.size()));
+  HCTX_CUDA(c, cudaMalloc(&c->d_sg_local, sizeof(uint32_t) * loc.size()));
+  HCTX_CUDA(c, cudaMemcpy(c->d_sg_pow2, p2.data(), sizeof(uint32_t) * p2.size(), cudaMemcpyHostToDevice));
+  HCTX_CUDA(c, cudaMemcpy(c->d_sg_local, loc.data(), sizeof(uint32_t) * loc.size(), cudaMemcpyHostToDevice));
+  HCTX_CUDA(c, cudaMalloc(&c->d_sg_u64, sizeof(uint64_t) * 4));
+  HCTX_CUDA(c, cudaMalloc(&c->d_sg_err, sizeof(int) * 3));
+  return SF21_OK;
+}
+
+static int sg_chunk(sf21_halo_ctx* c, long n) { return grow(c, &c->d_sg_chunk, scan_chunks(n), &c->sg_chunk_cap); }
+
+// Subgrid cycle (get_halos.c:326-371) from the mass below the cell mass down
+// to halo_Mmin; the context's generator continues across masses and calls.
+static int subgrid_cycle(sf21_halo_ctx* c, const Cosmo& cs, double z, double growth, double M, long* total_out) {
+  const sf21_halo_config& cf = c->cfg;
+  cudaStream_t st = c->stream;
+  *total_out = 0;
+  if (!(M >= cf.halo_Mmin)) return SF21_OK;
+  int rc = sg_tables(c);
+  if (rc) return rc;
+  const double rhom = cs.rho_m();
+  double R = pow(3 / 4.0 / kPI / rhom * M, 1.0 / 3);
+  // unflagged cells: per-word counts -> exclusive prefix (select by binary search)
+  long wcap = c->nwords;
+  if (!c->d_sg_wpre) HCTX_CUDA(c, cudaMalloc(&c->d_sg_wpre, sizeof(uint32_t) * c->nwords));
+  (void)wcap;
+  if ((rc = sg_chunk(c, c->nwords))) return rc;
+  HCTX_CUDA(c, launch_sg_free_count(c->d_FL, c->nwords, c->d_sg_wpre, st));
+  HCTX_CUDA(c, launch_scan_u32(c->d_sg_wpre, c->nwords, c->d_sg_wpre, c->d_sg_chunk, c->d_cnt + 3, st));
+  if ((rc = read_counts(c))) return rc;
+  const uint64_t U = c->h_cnt[3];
+  long total = 0;
+  while (M >= cf.halo_Mmin) {  // :329
+    const double sigma_aux = cs.sigma(R);
+    const double dndm = cs.mass_function(z, M, growth) * M * (pow(10.0, cf.halo_dlm) - 1) * pow(c->dx, 3);
+    const double hbias = cs.bias(sigma_aux, growth);
+    if (!(dndm <= 10.0))
+      HCTX_FAIL(c, SF21_E_UNSUPPORTED, "subgrid: Poisson mean %g per cell above 10 (M = %E)", dndm, M);
+    if (U > 0) {
+      SgArgs a;
+      memcpy(a.s0, c->rng, sizeof(a.s0));
+      const double emu = exp(-dndm);
+      const double xt = floor(ldexp(emu, 32));
+      a.x1 = xt >= 4294967295.0 ? 0xffffffffu : (uint32_t)xt;
+      memcpy(&a.emu, &emu, 8);
+      // positions to generate: the mean consumption (1 + mu) per draw plus a margin
+      const double need = (double)U * (1.0 + dndm) + 12.0 * sqrt((double)U * (1.0 + dndm) * (1.0 + dndm)) + 8 * SG_B;
+      long nblocks = (long)ceil(need / SG_B);
+      for (int attempt = 0;; ++attempt) {
+        const long Q = nblocks * SG_B;
+        const long ngroups = (nblocks + SG_G - 1) / SG_G;
+        if ((rc = grow(c, &c->d_sgL, Q, &c->sgL_cap))) return rc;
+        if (nblocks > c->sg_blocks_cap || !c->d_sgX) {
+          const long nb = nblocks, ng = ngroups;
+          uint8_t** b8[] = {&c->d_sgX, &c->d_sgGX, &c->d_sg_gentry, &c->d_sg_bentry};
+          for (uint8_t** q : b8)
+            if (*q) cudaFree(*q), *q = nullptr;
+          if (c->d_sgD) cudaFree(c->d_sgD), c->d_sgD = nullptr;
+          if (c->d_sgGD) cudaFree(c->d_sgGD), c->d_sgGD = nullptr;
+          if (c->d_sg_cnt) cudaFree(c->d_sg_cnt), c->d_sg_cnt = nullptr;
+          if (c->d_sg_gbase) cudaFree(c->d_sg_gbase), c->d_sg_gbase = nullptr;
+          if (c->d_sg_bbase) cudaFree(c->d_sg_bbase), c->d_sg_bbase = nullptr;
+          c->sg_blocks_cap = 0;
+          HCTX_CUDA(c, cudaMalloc(&c->d_sgX, (size_t)nb * SG_LMAX));
+          HCTX_CUDA(c, cudaMalloc(&c->d_sgD, sizeof(uint16_t) * (size_t)nb * SG_LMAX));
+          HCTX_CUDA(c, cudaMalloc(&c->d_sgGX, (size_t)ng * SG_LMAX));
+          HCTX_CUDA(c, cudaMalloc(&c->d_sgGD, sizeof(uint32_t) * (size_t)ng * SG_LMAX));
+          HCTX_CUDA(c, cudaMalloc(&c->d_sg_gentry, (size_t)ng));
+          HCTX_CUDA(c, cudaMalloc(&c->d_sg_gbase, sizeof(uint64_t) * (size_t)(ng + 1)));
+          HCTX_CUDA(c, cudaMalloc(&c->d_sg_bentry, (size_t)nb));
+          HCTX_CUDA(c, cudaMalloc(&c->d_sg_bbase, sizeof(uint64_t) * (size_t)nb));
+          HCTX_CUDA(c, cudaMalloc(&c->d_sg_cnt, sizeof(uint32_t) * (size_t)nb));
+          c->sg_blocks_cap = nb;
+        }
+        HCTX_CUDA(c, cudaMemsetAsync(c->d_sg_err, 0, sizeof(int) * 3, st));
+        HCTX_CUDA(c, launch_sg_len(nblocks, a, c->d_sg_pow2, c->d_sg_local, c->d_sgL, c->d_sgX, c->d_sgD,
+                                   c->d_sg_err, st));
+        HCTX_CUDA(c, launch_sg_entries(c->d_sgX, c->d_sgD, nblocks, c->d_sgGX, c->d_sgGD, c->d_sg_gentry,
+                                       c->d_sg_gbase, c->d_sg_bentry, c->d_sg_bbase, st));
+        uint64_t avail = 0;
+        int errf = 0;
+        HCTX_CUDA(c, cudaMemcpyAsync(&avail, c->d_sg_gbase + ngroups, sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+        HCTX_CUDA(c, cudaMemcpyAsync(&errf, c->d_sg_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+        HCTX_CUDA(c, cudaStreamSynchronize(st));
+        if (errf) HCTX_FAIL(c, SF21_E_UNSUPPORTED, "subgrid: a Poisson draw needed more than %d uniforms", SG_LMAX);
+        if (avail >= U) break;
+        if (attempt >= 3) HCTX_FAIL(c, SF21_E_ARG, "subgrid: stream positions short of the %llu draws",
+                                    (unsigned long long)U);
+        nblocks *= 2;
+      }
+      // draws with k >= 1: count per block, offsets, list
+      HCTX_CUDA(c, launch_sg_walk(0, c->d_sgL, nblocks, c->d_sg_bentry, c->d_sg_bbase, U, c->d_sg_cnt, c->d_sg_u64,
+                                  nullptr, nullptr, 0, c->d_sg_err, st));
+      if ((rc = sg_chunk(c, nblocks))) return rc;
+      HCTX_CUDA(c, launch_scan_u32(c->d_sg_cnt, nblocks, c->d_sg_cnt, c->d_sg_chunk, c->d_cnt + 3, st));
+      uint64_t consumed = 0;
+      HCTX_CUDA(c, cudaMemcpyAsync(&consumed, c->d_sg_u64, sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+      if ((rc = read_counts(c))) return rc;
+      const long nd = c->h_cnt[3];
+      long dcap = c->sg_draw_cap;
+      if ((rc = grow(c, &c->d_sg_dn, nd, &dcap))) return rc;
+      dcap = c->sg_draw_cap;
+      if ((rc = grow(c, &c->d_sg_dk, nd, &dcap))) return rc;
+      dcap = c->sg_draw_cap;
+      if ((rc = grow(c, &c->d_sg_cell, nd, &dcap))) return rc;
+      dcap = c->sg_draw_cap;
+      if ((rc = grow(c, &c->d_sg_nn, nd, &dcap))) return rc;
+      c->sg_draw_cap = std::max(c->sg_draw_cap, std::max(nd, 1L));
+      long recs = 0;
+      if (nd > 0) {
+        HCTX_CUDA(c, launch_sg_walk(1, c->d_sgL, nblocks, c->d_sg_bentry, c->d_sg_bbase, U, c->d_sg_cnt, nullptr,
+                                    c->d_sg_dn, c->d_sg_dk, (uint64_t)c->sg_draw_cap, c->d_sg_err, st));
+        uint64_t gb, hb;
+        memcpy(&gb, &growth, 8);
+        memcpy(&hb, &hbias, 8);
+        HCTX_CUDA(c, launch_sg_nn(c->d_sg_dn, c->d_sg_dk, nd, c->d_FL, c->d_sg_wpre, c->nwords, c->d_delta, gb, hb,
+                                  c->d_sg_cell, c->d_sg_nn, c->d_sg_err, st));
+        if ((rc = sg_chunk(c, nd))) return rc;
+        // offsets of the records in place of the per-draw indices (dn is no longer needed)
+        uint32_t* off = reinterpret_cast<uint32_t*>(c->d_sg_dn);
+        HCTX_CUDA(c, launch_scan_u32(c->d_sg_nn, nd, off, c->d_sg_chunk, c->d_cnt + 3, st));
+        if ((rc = read_counts(c))) return rc;
+        recs = c->h_cnt[3];
+        if ((rc = ensure_cat(c, c->cat_n + recs))) return rc;
+        HCTX_CUDA(c, launch_sg_records(c->d_sg_cell, c->d_sg_nn, off, nd, c->logN, (float)M, c->d_cat + c->cat_n,
+                                       (uint64_t)(c->cat_cap - c->cat_n), c->d_sg_err, st));
+        c->cat_n += recs;
+      }
+      int chk[3] = {0, 0, 0};
+      HCTX_CUDA(c, cudaMemcpyAsync(chk, c->d_sg_err, sizeof(chk), cudaMemcpyDeviceToHost, st));
+      HCTX_CUDA(c, cudaStreamSynchronize(st));
+      if (chk[1])
+        HCTX_FAIL(c, SF21_E_CUDA, "subgrid: access outside its buffer at site %d, index %d (skipped)", chk[1], chk[2]);
+      taus_jump(c->rng, consumed);
+      total += recs;
+    }
+    M = M / pow(10.0, cf.halo_dlm);  // :366-367
+    R = pow(3 / 4.0 / kPI / rhom * M, 1.0 / 3);
+  }
+  *total_out = total;
+  return SF21_OK;
+}
+
 static int run_filter_bank(sf21_halo_ctx* c, const std::vector<MassPlan>& plan, double growth) {
   const int N = (int)c->N;
   cudaStream_t st = c->stream;
@@ -816,9 +1054,10 @@ extern "C" int sf21_halo_find_z(sf21_halo_ctx* c, double z, long* nhalos) {
     if ((rc = append_records(c, c->d_list2, nc, M))) return rc;
     c->counts[ms.size()] = nc;
   }
-  if (cf.use_subgrid == 1) {
-    M = M / pow(10.0, cf.halo_dlm);
-    if (M >= cf.halo_Mmin) HCTX_FAIL(c, SF21_E_UNSUPPORTED, "subgrid cycle not available yet");
+  if (cf.use_subgrid == 1) {  // :323-371
+    long nsg = 0;
+    if ((rc = subgrid_cycle(c, cs, z, growth, M / pow(10.0, cf.halo_dlm), &nsg))) return rc;
+    c->counts[ms.size() + 1] = nsg;
   }
   HCTX_CUDA(c, cudaStreamSynchronize(st));
   if (nhalos) *nhalos = c->cat_n;

@@ -1,0 +1,423 @@
+// Subgrid Poisson cycle of the halo finder on the GPU (get_halos.c:326-371).
+//
+// The reference walks the unflagged cells in index order and draws one
+// Poisson deviate per cell from a single taus generator (gsl_ran_poisson,
+// the product-of-uniforms method for means <= 10): a draw that starts at
+// stream position s consumes L(s) uniforms, L(s) = the first L with
+// u_s u_{s+1} ... u_{s+L-1} <= exp(-mu) (products in double), and returns
+// k = L(s) - 1.  Draw n starts at s_n, s_{n+1} = s_n + L(s_n).  The GPU form
+// reproduces that stream exactly:
+//   A  per block of SG_B positions: the generator's state is jumped to the
+//      block (the generator is linear over GF(2): 32x32 bit matrices of its
+//      powers), each thread steps 4 consecutive positions, L(s) is computed
+//      for every position (one integer compare decides L = 1; longer chains
+//      multiply in soft-double), and pointer jumping gives, for every entry
+//      offset e < SG_LMAX, the block's exit offset and draw count;
+//   B  the entries of all blocks follow by composing those tables (groups of
+//      SG_G blocks in parallel, then the groups in order, then the blocks of
+//      each group);
+//   C  each block replays its chain from its entry and lists the draws with
+//      k >= 1 (k = 0 writes nothing) with their draw index;
+//   D  draw n belongs to the n-th unflagged cell (binary search in the
+//      per-word prefix counts of the unflagged bit set); nn = (int)
+//      round(k (1 + delta growth hbias)) in soft-double; the records follow
+//      from a prefix sum over nn.
+// No FP64 unit is used: soft-double (softdouble.h) gives the IEEE results.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "sf21_kernels.h"
+#include "softdouble.h"
+
+namespace sf21 {
+
+__device__ __forceinline__ uint32_t gf2_apply(const uint32_t* __restrict__ col, uint32_t v) {
+  uint32_t r = 0;
+#pragma unroll
+  for (int k = 0; k < 32; ++k) r ^= (0u - ((v >> k) & 1u)) & __ldg(col + k);
+  return r;
+}
+
+__device__ __forceinline__ void taus_step(uint32_t& a, uint32_t& b, uint32_t& c) {
+  a = ((a & 4294967294u) << 12) ^ (((a << 13) ^ a) >> 19);
+  b = ((b & 4294967288u) << 4) ^ (((b << 2) ^ b) >> 25);
+  c = ((c & 4294967280u) << 17) ^ (((c << 3) ^ c) >> 11);
+}
+
+// Access checks of the draw and record kernels: an index outside its buffer
+// is recorded (err[1] = site, err[2] = low 31 bits of the index) and the
+// access skipped; the host turns a record into an error return.
+__device__ __forceinline__ void sg_bad(int* err, int site, uint64_t idx) {
+  if (atomicCAS(err + 1, 0, site) == 0) err[2] = (int)(idx & 0x7fffffff);
+}
+
+// A ------------------------------------------------------------------------
+// jumps: pow2[k] = T^(2^k) (k < SG_POW2), local[i] = T^(4 i) (i <= (SG_B + SG_LMAX) / 4),
+// each 3 x 32 columns.  S0: the state whose next step gives position 0.
+__global__ void __launch_bounds__(SG_THREADS)
+k_sg_len(SgArgs a, const uint32_t* __restrict__ pow2, const uint32_t* __restrict__ local, uint8_t* __restrict__ Lout,
+         uint8_t* __restrict__ X, uint16_t* __restrict__ D, int* __restrict__ err) {
+  __shared__ uint32_t sx[SG_B + SG_LMAX];
+  __shared__ uint32_t sS[3];
+  __shared__ uint16_t nxt[SG_B], cnt[SG_B];
+  const long b = blockIdx.x;
+  const uint64_t base = (uint64_t)b * SG_B;
+  if (threadIdx.x < 3) {
+    const int c = threadIdx.x;
+    uint32_t v = a.s0[c];
+    for (int k = 0; k < SG_POW2; ++k)
+      if ((base >> k) & 1u) v = gf2_apply(pow2 + ((size_t)k * 3 + c) * 32, v);
+    sS[c] = v;
+  }
+  __syncthreads();
+  for (int pass = 0; pass < 2; ++pass) {
+    const int i0 = pass ? SG_B + 4 * threadIdx.x : 4 * threadIdx.x;
+    if (pass && 4 * (int)threadIdx.x >= SG_LMAX) break;
+    const uint32_t* J = local + (size_t)(i0 / 4) * 96;
+    uint32_t x = gf2_apply(J, sS[0]), y = gf2_apply(J + 32, sS[1]), z = gf2_apply(J + 64, sS[2]);
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      taus_step(x, y, z);
+      sx[i0 + r] = x ^ y ^ z;
+    }
+  }
+  __syncthreads();
+  // L(s): x <= X1 <=> u = x 2^-32 <= exp(-mu) <=> one uniform
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int i = 4 * threadIdx.x + r;
+    int L = 1;
+    uint32_t xv = sx[i];
+    if (xv > a.x1) {
+      sd_t prod = sd_ldexp(sd_from_int((int64_t)xv), -32);
+      for (L = 2; L <= SG_LMAX; ++L) {
+        const uint32_t xn = sx[i + L - 1];
+        prod = sd_mul(prod, xn ? sd_ldexp(sd_from_int((int64_t)xn), -32) : (sd_t)0);
+        if (!sd_gt(prod, a.emu)) break;
+      }
+      if (L > SG_LMAX) {
+        atomicOr(err, 1);
+        L = SG_LMAX;
+      }
+    }
+    Lout[base + i] = (uint8_t)L;
+    nxt[i] = (uint16_t)(i + L);
+    cnt[i] = 1;
+  }
+  __syncthreads();
+  // pointer jumping: after log2(SG_B) rounds every chain has left the block
+  for (int round = 0; (1 << round) < SG_B; ++round) {
+    uint16_t nn[4], cc[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int i = 4 * threadIdx.x + r;
+      const int n = nxt[i];
+      if (n < SG_B) {
+        nn[r] = nxt[n];
+        cc[r] = (uint16_t)(cnt[i] + cnt[n]);
+      } else {
+        nn[r] = (uint16_t)n;
+        cc[r] = cnt[i];
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      nxt[4 * threadIdx.x + r] = nn[r];
+      cnt[4 * threadIdx.x + r] = cc[r];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x < SG_LMAX) {
+    X[(size_t)b * SG_LMAX + threadIdx.x] = (uint8_t)(nxt[threadIdx.x] - SG_B);
+    D[(size_t)b * SG_LMAX + threadIdx.x] = cnt[threadIdx.x];
+  }
+}
+
+// B ------------------------------------------------------------------------
+__global__ void k_sg_group(const uint8_t* __restrict__ X, const uint16_t* __restrict__ D, long nblocks,
+                           uint8_t* __restrict__ GX, uint32_t* __restrict__ GD) {
+  const long g = blockIdx.x;
+  const int e0 = threadIdx.x;  // SG_LMAX threads
+  int e = e0;
+  uint32_t tot = 0;
+  const long b1 = (g + 1) * SG_G < nblocks ? (g + 1) * SG_G : nblocks;
+  for (long b = g * SG_G; b < b1; ++b) {
+    tot += D[(size_t)b * SG_LMAX + e];
+    e = X[(size_t)b * SG_LMAX + e];
+  }
+  GX[(size_t)g * SG_LMAX + e0] = (uint8_t)e;
+  GD[(size_t)g * SG_LMAX + e0] = tot;
+}
+
+__global__ void k_sg_top(const uint8_t* __restrict__ GX, const uint32_t* __restrict__ GD, long ngroups,
+                         uint8_t* __restrict__ gentry, uint64_t* __restrict__ gbase) {
+  if (threadIdx.x || blockIdx.x) return;
+  int e = 0;
+  uint64_t base = 0;
+  for (long g = 0; g < ngroups; ++g) {
+    gentry[g] = (uint8_t)e;
+    gbase[g] = base;
+    base += GD[(size_t)g * SG_LMAX + e];
+    e = GX[(size_t)g * SG_LMAX + e];
+  }
+  gbase[ngroups] = base;  // draws available in all generated positions
+}
+
+__global__ void k_sg_blocks(const uint8_t* __restrict__ X, const uint16_t* __restrict__ D, long nblocks,
+                            long ngroups, const uint8_t* __restrict__ gentry, const uint64_t* __restrict__ gbase,
+                            uint8_t* __restrict__ bentry, uint64_t* __restrict__ bbase) {
+  const long g = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= ngroups) return;
+  int e = gentry[g];
+  uint64_t base = gbase[g];
+  const long b1 = (g + 1) * SG_G < nblocks ? (g + 1) * SG_G : nblocks;
+  for (long b = g * SG_G; b < b1; ++b) {
+    bentry[b] = (uint8_t)e;
+    bbase[b] = base;
+    base += D[(size_t)b * SG_LMAX + e];
+    e = X[(size_t)b * SG_LMAX + e];
+  }
+}
+
+// C ------------------------------------------------------------------------
+// mode 0: count the draws with k >= 1 among draws < U per block, and record
+// the position after draw U - 1; mode 1: write them (draw index, k).
+__global__ void k_sg_walk(int mode, const uint8_t* __restrict__ Lb, long nblocks, const uint8_t* __restrict__ bentry,
+                          const uint64_t* __restrict__ bbase, uint64_t U, uint32_t* __restrict__ cnt,
+                          uint64_t* __restrict__ consumed, uint64_t* __restrict__ dn, uint8_t* __restrict__ dk,
+                          uint64_t cap, int* __restrict__ err) {
+  const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nblocks) return;
+  uint64_t n = bbase[b];
+  if (n >= U) {
+    if (mode == 0) cnt[b] = 0;
+    return;
+  }
+  const uint64_t base = (uint64_t)b * SG_B;
+  int s = bentry[b];
+  uint32_t c = 0;
+  const uint32_t off = mode ? cnt[b] : 0;
+  while (s < SG_B && n < U) {
+    const int L = Lb[base + s];
+    if (L >= 2) {
+      if (mode) {
+        if ((uint64_t)off + c < cap) {
+          dn[off + c] = n;
+          dk[off + c] = (uint8_t)(L - 1);
+        } else {
+          sg_bad(err, 1, (uint64_t)off + c);
+        }
+      }
+      ++c;
+    }
+    if (mode == 0 && n == U - 1) *consumed = base + s + L;
+    s += L;
+    ++n;
+  }
+  if (mode == 0) cnt[b] = c;
+}
+
+// D ------------------------------------------------------------------------
+__device__ __forceinline__ int64_t sd_round_half_away(sd_t x) {
+  if (sd_is_zero(x)) return 0;
+  const int e = (int)((x >> 52) & 0x7FF) - 1023;
+  const uint64_t m = (x & 0xFFFFFFFFFFFFFULL) | (1ULL << 52);  // value = m 2^(e-52)
+  int64_t q;
+  if (e < -1) {
+    q = 0;
+  } else if (e >= 52) {
+    q = (int64_t)(m << (e - 52 < 11 ? e - 52 : 10));
+  } else {
+    const int sh = 52 - e;  // 1..53
+    const uint64_t r = m & ((1ULL << sh) - 1);
+    q = (int64_t)(m >> sh) + (r >= (1ULL << (sh - 1)) ? 1 : 0);
+  }
+  return (x >> 63) ? -q : q;
+}
+
+// cell of draw n: the n-th zero bit of FL; wpre[w] = zero bits of words < w
+__device__ __forceinline__ uint32_t select_unflagged(const uint32_t* __restrict__ FL,
+                                                     const uint32_t* __restrict__ wpre, long nwords, uint64_t n) {
+  long lo = 0, hi = nwords - 1;  // last w with wpre[w] <= n
+  while (lo < hi) {
+    const long mid = (lo + hi + 1) >> 1;
+    if (wpre[mid] <= n) lo = mid; else hi = mid - 1;
+  }
+  uint32_t free_bits = ~FL[lo];
+  uint32_t r = (uint32_t)(n - wpre[lo]);
+  while (r-- && free_bits) free_bits &= free_bits - 1;
+  return (uint32_t)(lo * 32 + (free_bits ? __ffs(free_bits) - 1 : 0));  // n < free cells: never the 0 case
+}
+
+__global__ void k_sg_nn(const uint64_t* __restrict__ dn, const uint8_t* __restrict__ dk, long nd,
+                        const uint32_t* __restrict__ FL, const uint32_t* __restrict__ wpre, long nwords,
+                        const float* __restrict__ delta, uint64_t growth, uint64_t hbias, uint32_t* __restrict__ cell,
+                        uint32_t* __restrict__ nn, int* __restrict__ err) {
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nd; i += (long)gridDim.x * blockDim.x) {
+    const uint32_t t = select_unflagged(FL, wpre, nwords, dn[i]);
+    if ((long)t >= nwords * 32) {
+      sg_bad(err, 2, t);
+      cell[i] = 0;
+      nn[i] = 0;
+      continue;
+    }
+    // tempv = map_in_f[index] * growth * hbias; nn = (int) round(Pn (1 + tempv))  (:351-354)
+    const sd_t tempv = sd_mul(sd_mul(sd_from_float(delta[t]), growth), hbias);
+    const sd_t v = sd_mul(sd_from_int(dk[i]), sd_add(0x3FF0000000000000ULL, tempv));
+    int64_t q = sd_round_half_away(v);
+    if (q > (1 << 24)) {  // a finite density and k <= 63 stay far below
+      sg_bad(err, 3, (uint64_t)i);
+      q = 0;
+    }
+    cell[i] = t;
+    nn[i] = q > 0 ? (uint32_t)q : 0u;
+  }
+}
+
+__global__ void k_sg_records(const uint32_t* __restrict__ cell, const uint32_t* __restrict__ nn,
+                             const uint32_t* __restrict__ off, long nd, int logN, float mass,
+                             float4* __restrict__ out, uint64_t cap, int* __restrict__ err) {
+  const int N = 1 << logN;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nd; i += (long)gridDim.x * blockDim.x) {
+    const uint32_t t = cell[i];
+    const float4 rec = make_float4(mass, (float)(t >> (2 * logN)), (float)((t >> logN) & (N - 1)),
+                                   (float)(t & (N - 1)));
+    const uint32_t o = off[i];
+    for (uint32_t r = 0; r < nn[i]; ++r) {
+      if ((uint64_t)o + r < cap)
+        out[o + r] = rec;
+      else
+        sg_bad(err, 4, (uint64_t)o + r);
+    }
+  }
+}
+
+// zero bits per word of FL
+__global__ void k_sg_free_count(const uint32_t* __restrict__ FL, long nwords, uint32_t* __restrict__ c) {
+  for (long w = (long)blockIdx.x * blockDim.x + threadIdx.x; w < nwords; w += (long)gridDim.x * blockDim.x)
+    c[w] = 32u - (uint32_t)__popc(FL[w]);
+}
+
+// ---------------------------------------------------------------------------
+// Exclusive prefix sums of a uint32 array (chunk sums, one CTA over the
+// chunk sums, per-chunk scans with the chunk's offset).  Totals < 2^32.
+constexpr int SC_THREADS = 256;
+constexpr long SC_CHUNK = 8192;
+
+__global__ void __launch_bounds__(SC_THREADS) k_chunk_sum(const uint32_t* __restrict__ a, long n,
+                                                          uint32_t* __restrict__ sums) {
+  const long c0 = blockIdx.x * SC_CHUNK;
+  uint32_t s = 0;
+  for (long i = c0 + threadIdx.x; i < c0 + SC_CHUNK && i < n; i += SC_THREADS) s += a[i];
+  s = __reduce_add_sync(0xffffffffu, s);
+  __shared__ uint32_t red[SC_THREADS / 32];
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t t = 0;
+    for (int k = 0; k < SC_THREADS / 32; ++k) t += red[k];
+    sums[blockIdx.x] = t;
+  }
+}
+
+// a and out may be the same array (in-place scans): no __restrict__ on
+// them, so every element is loaded before its slot is overwritten.
+__global__ void __launch_bounds__(SC_THREADS) k_chunk_scan(const uint32_t* a, long n,
+                                                           const uint32_t* __restrict__ off, uint32_t* out) {
+  // each thread scans SC_CHUNK / SC_THREADS consecutive elements
+  constexpr int PER = (int)(SC_CHUNK / SC_THREADS);
+  const long i0 = blockIdx.x * SC_CHUNK + (long)threadIdx.x * PER;
+  uint32_t s = 0;
+  for (int k = 0; k < PER; ++k)
+    if (i0 + k < n) s += a[i0 + k];
+  __shared__ uint32_t wsum[SC_THREADS / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  uint32_t x = s;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) wsum[w] = x;
+  __syncthreads();
+  uint32_t before = 0;
+  for (int k = 0; k < w; ++k) before += wsum[k];
+  uint32_t run = off[blockIdx.x] + before + x - s;
+  for (int k = 0; k < PER; ++k) {
+    if (i0 + k >= n) break;
+    const uint32_t v = a[i0 + k];
+    out[i0 + k] = run;
+    run += v;
+  }
+}
+
+long scan_chunks(long n) { return (n + SC_CHUNK - 1) / SC_CHUNK; }
+
+cudaError_t launch_scan_u32(const uint32_t* a, long n, uint32_t* out, uint32_t* chunk, uint32_t* total,
+                            cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  const long nc = scan_chunks(n);
+  k_chunk_sum<<<(unsigned)nc, SC_THREADS, 0, st>>>(a, n, chunk);
+  cudaError_t e = cudaGetLastError();
+  if (e) return e;
+  if ((e = launch_scan_counts(chunk, nc, total, st))) return e;
+  k_chunk_scan<<<(unsigned)nc, SC_THREADS, 0, st>>>(a, n, chunk, out);
+  return cudaGetLastError();
+}
+
+static unsigned grid_for(long n, int threads) {
+  long b = (n + threads - 1) / threads;
+  if (b < 1) b = 1;
+  if (b > 152 * 32) b = 152 * 32;
+  return (unsigned)b;
+}
+
+cudaError_t launch_sg_len(long nblocks, const SgArgs& a, const uint32_t* pow2, const uint32_t* local, uint8_t* L,
+                          uint8_t* X, uint16_t* D, int* err, cudaStream_t st) {
+  k_sg_len<<<(unsigned)nblocks, SG_THREADS, 0, st>>>(a, pow2, local, L, X, D, err);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sg_entries(const uint8_t* X, const uint16_t* D, long nblocks, uint8_t* GX, uint32_t* GD,
+                              uint8_t* gentry, uint64_t* gbase, uint8_t* bentry, uint64_t* bbase, cudaStream_t st) {
+  const long ngroups = (nblocks + SG_G - 1) / SG_G;
+  k_sg_group<<<(unsigned)ngroups, SG_LMAX, 0, st>>>(X, D, nblocks, GX, GD);
+  cudaError_t e = cudaGetLastError();
+  if (e) return e;
+  k_sg_top<<<1, 32, 0, st>>>(GX, GD, ngroups, gentry, gbase);
+  if ((e = cudaGetLastError())) return e;
+  k_sg_blocks<<<(unsigned)((ngroups + 127) / 128), 128, 0, st>>>(X, D, nblocks, ngroups, gentry, gbase, bentry,
+                                                                  bbase);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sg_walk(int mode, const uint8_t* L, long nblocks, const uint8_t* bentry, const uint64_t* bbase,
+                           uint64_t U, uint32_t* cnt, uint64_t* consumed, uint64_t* dn, uint8_t* dk, uint64_t cap,
+                           int* err, cudaStream_t st) {
+  k_sg_walk<<<(unsigned)((nblocks + 127) / 128), 128, 0, st>>>(mode, L, nblocks, bentry, bbase, U, cnt, consumed,
+                                                                dn, dk, cap, err);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sg_free_count(const uint32_t* FL, long nwords, uint32_t* c, cudaStream_t st) {
+  k_sg_free_count<<<grid_for(nwords, 256), 256, 0, st>>>(FL, nwords, c);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sg_nn(const uint64_t* dn, const uint8_t* dk, long nd, const uint32_t* FL, const uint32_t* wpre,
+                         long nwords, const float* delta, uint64_t growth, uint64_t hbias, uint32_t* cell,
+                         uint32_t* nn, int* err, cudaStream_t st) {
+  if (nd <= 0) return cudaSuccess;
+  k_sg_nn<<<grid_for(nd, 256), 256, 0, st>>>(dn, dk, nd, FL, wpre, nwords, delta, growth, hbias, cell, nn, err);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sg_records(const uint32_t* cell, const uint32_t* nn, const uint32_t* off, long nd, int logN,
+                              float mass, float4* out, uint64_t cap, int* err, cudaStream_t st) {
+  if (nd <= 0) return cudaSuccess;
+  k_sg_records<<<grid_for(nd, 256), 256, 0, st>>>(cell, nn, off, nd, logN, mass, out, cap, err);
+  return cudaGetLastError();
+}
+
+}  // namespace sf21

@@ -178,6 +178,39 @@ cudaError_t launch_hf_cell(long nwords, const float* delta, float tcell, uint32_
                            cudaStream_t st);
 cudaError_t launch_hf_records(const uint32_t* idx, long n, int logN, float mass, float4* out, cudaStream_t st);
 
+// Subgrid Poisson cycle of the halo finder (kernels_sg.cu).
+constexpr int SG_B = 1024;               // stream positions per block
+constexpr int SG_THREADS = SG_B / 4;     // 4 consecutive positions per thread
+constexpr int SG_LMAX = 64;              // uniforms one draw may consume at most
+constexpr int SG_G = 1024;               // blocks per group of the entry composition
+constexpr int SG_POW2 = 40;              // jump matrices T^(2^k), k < SG_POW2
+constexpr int SG_LOCAL = (SG_B + SG_LMAX) / 4;  // jump matrices T^(4 i), i < SG_LOCAL
+struct SgArgs {
+  uint32_t s0[3];  // taus state before position 0
+  uint32_t x1;     // one uniform suffices <=> its 32-bit draw <= x1 (= floor(exp(-mu) 2^32))
+  uint64_t emu;    // exp(-mu), double bits
+};
+cudaError_t launch_sg_len(long nblocks, const SgArgs& a, const uint32_t* pow2, const uint32_t* local, uint8_t* L,
+                          uint8_t* X, uint16_t* D, int* err, cudaStream_t st);
+cudaError_t launch_sg_entries(const uint8_t* X, const uint16_t* D, long nblocks, uint8_t* GX, uint32_t* GD,
+                              uint8_t* gentry, uint64_t* gbase, uint8_t* bentry, uint64_t* bbase, cudaStream_t st);
+// err: int[3], [0] a draw longer than SG_LMAX, [1] site of an access outside
+// its buffer (skipped), [2] its index
+cudaError_t launch_sg_walk(int mode, const uint8_t* L, long nblocks, const uint8_t* bentry, const uint64_t* bbase,
+                           uint64_t U, uint32_t* cnt, uint64_t* consumed, uint64_t* dn, uint8_t* dk, uint64_t cap,
+                           int* err, cudaStream_t st);
+cudaError_t launch_sg_free_count(const uint32_t* FL, long nwords, uint32_t* c, cudaStream_t st);
+cudaError_t launch_sg_nn(const uint64_t* dn, const uint8_t* dk, long nd, const uint32_t* FL, const uint32_t* wpre,
+                         long nwords, const float* delta, uint64_t growth, uint64_t hbias, uint32_t* cell,
+                         uint32_t* nn, int* err, cudaStream_t st);
+cudaError_t launch_sg_records(const uint32_t* cell, const uint32_t* nn, const uint32_t* off, long nd, int logN,
+                              float mass, float4* out, uint64_t cap, int* err, cudaStream_t st);
+// exclusive prefix sums of n uint32 (out may equal a); chunk: scan_chunks(n)
+// words of scratch; *total (device) receives the sum
+long scan_chunks(long n);
+cudaError_t launch_scan_u32(const uint32_t* a, long n, uint32_t* out, uint32_t* chunk, uint32_t* total,
+                            cudaStream_t st);
+
 // Plain form (kernels_plain.cu).
 cudaError_t launch_plain_centres(long n3, const float2* box, const float* alpha, float zmul, float* mask, int* flag,
                                  cudaStream_t st);

@@ -89,6 +89,8 @@ def _check_case(H, name, zs_limit=None):
         assert len(cat) == len(ocat), (name, z, len(cat), len(ocat))
         assert cat.tobytes() == ocat.tobytes(), (name, z)
         np.testing.assert_array_equal(hf.counts()[: len(sch) + 1], ocounts[: len(sch) + 1])
+        # the subgrid generator continues identically
+        np.testing.assert_array_equal(hf.rng().astype(np.uint64), rng)
         if flips == 0:
             assert hashlib.sha256(cat.tobytes()).hexdigest() == str(g[f"sha_{i}"]), (name, z)
         report.append((z, len(cat), band, flips))
@@ -104,6 +106,13 @@ def test_catalogue_n64(H):
 def test_catalogue_n128_dense(H):
     rep = _check_case(H, "halos_n128_dense.npz")
     print("halos_n128_dense (z, halos, band cells, flipped cells):", rep)
+
+
+def test_catalogue_n64_subgrid(H):
+    """Subgrid Poisson cycle: the taus stream, the Poisson draws and the
+    halo counts per cell reproduce the reference's serial loop."""
+    rep = _check_case(H, "halos_n64_sgrid.npz")
+    print("halos_n64_sgrid (z, halos, band cells, flipped cells):", rep)
 
 
 def test_driver_writes_library_catalogues(tmp_path):
