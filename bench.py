@@ -270,6 +270,59 @@ def grad_metrics(N, L, z, zeta, rmax, factor, seed, stream, dev, kmax=0):
             "checkpoint": "uint8 argmax radius per voxel; filtered fields recomputed"}
 
 
+def halo_metrics(rank: int, with_cpu: bool, N: int = 512, z: float = 7.0, reps: int = 3):
+    """Halo finder of get_halos.c on a seeded Gaussian z = 0 density box
+    (P(k) ~ k^-2, rms 4 per cell), L = 100 Mpc, default halo keys with the
+    subgrid cycle on: device time per redshift, end to end with the catalogue
+    copied to host memory, and the CPU restatement at 256^3."""
+    import ctypes
+
+    from simfast21_gb300 import halos
+    w = synth.HaloWorkload(N=N, L_mpc=100.0, sigma=4.0, seed=11, subgrid=True)
+    ini = synth.halo_ini_text(w, z, z, 1.0)
+    d = w.density()
+    hf = halos.HaloFinder(halos.config_from_ini(halos.parse_ini(ini)))
+    t0 = time.perf_counter()
+    hf.set_density(d)
+    dens_ms = (time.perf_counter() - t0) * 1e3
+    n = ctypes.c_long(0)
+    L = hf._L
+    dev, e2e = [], []
+    for r in range(reps + 1):
+        hf.set_rng(None)
+        t0 = time.perf_counter()
+        hf._check(L.sf21_halo_find_z(hf._h, z, ctypes.byref(n)))
+        t1 = time.perf_counter()
+        out = np.empty(n.value, halos.HALO_DTYPE)
+        hf._check(L.sf21_halo_fetch(hf._h, out.ctypes.data, 0, n.value))
+        t2 = time.perf_counter()
+        if r:  # first call: warm-up (allocations)
+            dev.append((t1 - t0) * 1e3)
+            e2e.append((t2 - t0) * 1e3)
+    counts = hf.counts()
+    hf.close()
+    ms, ms_e2e = float(np.median(dev)), float(np.median(e2e))
+    res = {"N": N, "L_mpc": 100.0, "z": z, "subgrid": True, "halos": int(n.value),
+           "excursion_set_halos": int(counts[:-2].sum()), "cell_cycle_halos": int(counts[-2]),
+           "subgrid_halos": int(counts[-1]), "set_density_ms": dens_ms, "ms_per_redshift": ms,
+           "cells_per_s": N ** 3 / (ms / 1e3), "e2e_ms_per_redshift": ms_e2e,
+           "e2e_cells_per_s": N ** 3 / (ms_e2e / 1e3), "d2h_bytes": int(n.value) * 16}
+    if rank == 0 and with_cpu:
+        from oracle import halo as OH
+        Nc = 256
+        wc = synth.HaloWorkload(N=Nc, L_mpc=100.0 * Nc / N, sigma=4.0, seed=11, subgrid=True)
+        pc = OH.params_from_ini(OH.parse_ini(synth.halo_ini_text(wc, z, z, 1.0)))
+        dc = wc.density()
+        t0 = time.perf_counter()
+        OH.find_z(pc, z, dc, OH.taus_seed(0))
+        cpu_s = time.perf_counter() - t0
+        res["cpu_baseline"] = {"value": Nc ** 3 / cpu_s, "unit": "cells/s", "cores": os.cpu_count() or 1,
+                               "kind": "port", "sample": f"restatement of get_halos.c (FFTW-API shim, OpenMP "
+                                                         f"filter loop, serial overlap and subgrid loops) at "
+                                                         f"{Nc}^3, same cell size and parameters, {cpu_s:.1f} s"}
+    return res
+
+
 def run_ours(args, w, rank, world):
     import torch
     from simfast21_gb300 import build as B
@@ -433,6 +486,14 @@ def run_ours(args, w, rank, world):
             t21["cpu_baseline"] = {"ms": (time.perf_counter() - t0) * 1e3, "cores": os.cpu_count() or 1,
                                    "kind": "port", "sample": "restatement of t21.c (numpy, double), same boxes"}
 
+    # excursion-set halo finder (get_halos.c) through the C-ABI: one redshift
+    # of a 512^3 box per call, the catalogue left on the device (value) or
+    # fetched to host memory (e2e); the restatement of get_halos.c on the host
+    # cores at 256^3 (the same generator and parameters) as its baseline
+    halo = None
+    if not args.no_halos:
+        halo = halo_metrics(rank, not args.no_cpu_baseline)
+
     # CPU baseline (rank 0 only)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -470,6 +531,7 @@ def run_ours(args, w, rank, world):
             "differentiation": grad,
             "power_spectrum": pk,
             "t21": t21,
+            "halo_finder": halo,
             "cpu_baseline": cpu,
         }
         print(json.dumps(out))
@@ -486,12 +548,20 @@ def main():
     ap.add_argument("--kmax", type=int, default=0, help="radii per spectrum read (0 = library default)")
     ap.add_argument("--no-grad", action="store_true", help="skip the bwd/fwd measurement")
     ap.add_argument("--no-pk", action="store_true", help="skip the power-spectrum and 21-cm measurements")
+    ap.add_argument("--no-halos", action="store_true", help="skip the halo-finder measurement")
+    ap.add_argument("--halos-only", type=int, default=0, metavar="N",
+                    help="run only the halo-finder measurement at N^3 and print it (profiling entry point)")
     ap.add_argument("--grad-large", action="store_true", help="also time fwd+bwd at 1024^3 (peak HBM)")
     ap.add_argument("--path", type=int, default=0,
                     help="radius pipeline: 0 = tuned, else one of PIPELINES")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
+    if args.halos_only:
+        from simfast21_gb300 import build as B
+        B.build()
+        print(json.dumps({"halo_finder": halo_metrics(rank, not args.no_cpu_baseline, N=args.halos_only)}))
+        return
     w = workload(args.workload, rank)
     if args.impl == "reference":
         run_reference(args, w, rank)

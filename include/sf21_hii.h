@@ -59,12 +59,16 @@ typedef struct {
   const sf21_hii_set *sets;
   int kmax;          /* radii per spectrum read (0 = automatic, <= 8)       */
   int path;          /* radius pipeline: 0 = tuned at create (times one batch
-                        of each available one and keeps the fastest),
+                        of each available one and keeps the fastest; the
+                        timings are cached per device, N and kmax in
+                        $SF21_TUNE_CACHE or ~/.cache/simfast21_gb300/
+                        tune.jsonl and reused, SF21_RETUNE=1 times again),
                         1 = three axis passes, 2 = plane passes on
                         thread-block clusters (N 64..512), 3 = three axis
                         passes with the ky pass TMA-pipelined and
                         persistent, 4 = ky and kx passes TMA-pipelined
-                        (3 and 4: N 64..1024) */
+                        (3 and 4: N 64..1024), 5-7 = the same over
+                        column-block-major work boxes */
   int graph;         /* 0 = sf21_hii_run_z_device captures its per-redshift
                         schedule as a CUDA graph and replays it while z, the
                         kind, the buffers and the stream stay the same;

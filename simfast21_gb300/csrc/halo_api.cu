@@ -24,6 +24,7 @@
 
 #include <algorithm>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/sf21_halos.h"
@@ -359,21 +360,37 @@ void sum_runs(const std::vector<int4>& S, long nc, std::vector<int4>& out) {
 constexpr long kRoundsMaxNc = 24;  // D tables for spheres up to this half-width
 constexpr int kMaxRounds = 96;
 
-int plan_masses(const sf21_halo_config& c, double z, std::vector<sf21_halo_mass>& out) {
-  const Cosmo cs(c);
+// f(0), ..., f(n - 1) on the host's cores (the scalar work of a schedule is
+// about a hundred independent adaptive integrations); each f(i) is the same
+// arithmetic as a serial call, so the results do not depend on the split.
+template <class F>
+void host_parallel_for(int n, const F& f) {
+  const unsigned hw = std::thread::hardware_concurrency();
+  const int nt = std::max(1, std::min(n, (int)(hw ? hw : 1)));
+  if (nt <= 1) {
+    for (int i = 0; i < n; ++i) f(i);
+    return;
+  }
+  std::vector<std::thread> th;
+  for (int t = 0; t < nt; ++t)
+    th.emplace_back([&, t] {
+      for (int i = t; i < n; i += nt) f(i);
+    });
+  for (std::thread& x : th) x.join();
+}
+
+int plan_masses(const Cosmo& cs, double z, double growth, std::vector<sf21_halo_mass>& out) {
+  const sf21_halo_config& c = cs.c;
   const double rhom = cs.rho_m(), dx = c.L / c.N_halo, L3 = c.L * c.L * c.L;
   const double mass_dx = rhom * pow(dx, 3) * pow(10.0, c.halo_dlm);  // get_halos.c:159
-  const double growth = cs.growth(z);
   double R = c.L / 2.0;  // global_halo_Rmax (Input_variables.c:122)
   double M = (4.0 / 3.0) * kPI * rhom * pow(R, 3);
   out.clear();
   while (M > mass_dx && M >= c.halo_Mmin) {  // :197
     sf21_halo_mass h;
+    memset(&h, 0, sizeof h);
     h.M = M;
     h.R = R;
-    h.dndm = cs.mass_function(z, M, growth) * M * (pow(10.0, c.halo_dlm) - 1) * L3;
-    h.active = h.dndm > -log(1 - 0.1);
-    h.dcmz = h.active ? growth * cs.delta_filter(cs.sigma(R), growth) : 0.0;
     long nc = (long)(R / dx);
     if (nc == 0) nc = 1;
     h.nc = (int)nc;
@@ -382,6 +399,13 @@ int plan_masses(const sf21_halo_config& c, double z, std::vector<sf21_halo_mass>
     M = M / pow(10.0, c.halo_dlm);  // :285-286
     R = pow(3 / 4.0 / kPI / rhom * M, 1.0 / 3);
   }
+  // expected counts (:201) and, for the masses that pass the gate, the barrier (:204-205)
+  host_parallel_for((int)out.size(), [&](int i) {
+    sf21_halo_mass& h = out[i];
+    h.dndm = cs.mass_function(z, h.M, growth) * h.M * (pow(10.0, c.halo_dlm) - 1) * L3;
+    h.active = h.dndm > -log(1 - 0.1);
+    h.dcmz = h.active ? growth * cs.delta_filter(cs.sigma(h.R), growth) : 0.0;
+  });
   return SF21_OK;
 }
 
@@ -430,10 +454,10 @@ struct sf21_halo_ctx {
   uint32_t *d_sg_pow2 = nullptr, *d_sg_local = nullptr;
   uint8_t* d_sgL = nullptr;
   long sgL_cap = 0;
-  uint8_t *d_sgX = nullptr, *d_sgGX = nullptr, *d_sg_gentry = nullptr, *d_sg_bentry = nullptr;
+  uint8_t* d_sgX = nullptr;
   uint16_t* d_sgD = nullptr;
-  uint32_t *d_sgGD = nullptr, *d_sg_cnt = nullptr;
-  uint64_t *d_sg_gbase = nullptr, *d_sg_bbase = nullptr;
+  uint32_t* d_sg_cnt = nullptr;
+  SgEntryBufs sg_eb = {};
   long sg_blocks_cap = 0;
   uint64_t* d_sg_dn = nullptr;
   uint8_t* d_sg_dk = nullptr;
@@ -537,9 +561,10 @@ static void free_hctx(sf21_halo_ctx* c) {
   void* ptrs[] = {c->d_tw,        c->d_spec,      c->d_work,      c->d_delta,     c->d_FL,        c->d_UND,
                   c->d_ACC,       c->d_bits,      c->d_list,      c->d_list2,     c->d_status,    c->d_chunk,
                   c->d_cnt,       c->d_cat,       c->d_runs,      c->d_sg_pow2,   c->d_sg_local,  c->d_sgL,
-                  c->d_sgX,       c->d_sgGX,      c->d_sg_gentry, c->d_sg_bentry, c->d_sgD,       c->d_sgGD,
-                  c->d_sg_cnt,    c->d_sg_gbase,  c->d_sg_bbase,  c->d_sg_dn,     c->d_sg_dk,     c->d_sg_cell,
-                  c->d_sg_nn,     c->d_sg_wpre,   c->d_sg_chunk,  c->d_sg_u64,    c->d_sg_err};
+                  c->d_sgX,       c->d_sgD,       c->d_sg_cnt,    c->sg_eb.gx,    c->sg_eb.sx,    c->sg_eb.gentry,
+                  c->sg_eb.sentry, c->sg_eb.bentry, c->sg_eb.gd,  c->sg_eb.sd,    c->sg_eb.gbase, c->sg_eb.sbase,
+                  c->sg_eb.bbase, c->d_sg_dn,     c->d_sg_dk,     c->d_sg_cell,   c->d_sg_nn,     c->d_sg_wpre,
+                  c->d_sg_chunk,  c->d_sg_u64,    c->d_sg_err};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (uint32_t* p : c->d_masks)
@@ -556,7 +581,8 @@ extern "C" int sf21_halo_schedule(const sf21_halo_config* cfg, double z, sf21_ha
     return -SF21_E_ARG;
   }
   std::vector<sf21_halo_mass> v;
-  if (plan_masses(*cfg, z, v) != SF21_OK) {
+  const Cosmo cs(*cfg);
+  if (plan_masses(cs, z, cs.growth(z), v) != SF21_OK) {
     g_halo_err = "mass schedule longer than 4096 entries";
     return -SF21_E_ARG;
   }
@@ -596,6 +622,7 @@ extern "C" int sf21_halo_create(const sf21_halo_config* cfg, sf21_halo_ctx** out
   HCREATE(cudaSetDevice(c->device));
   HCREATE(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
   HCREATE(fft_setup(N));
+  HCREATE(cb_setup(N));
   HCREATE(hf_setup(N));
   const size_t box_c = sizeof(float2) * c->n3, bits = sizeof(uint32_t) * c->nwords;
   HCREATE(cudaMalloc(&c->d_spec, box_c));
@@ -797,8 +824,9 @@ static int sg_tables(sf21_halo_ctx* c) {
   const TausMat t1 = taus_one_step();
   const TausMat t4 = taus_mul(taus_mul(t1, t1), taus_mul(t1, t1));
   TausMat acc = taus_identity();
-  for (int i = 0; i < SG_LOCAL; ++i) {
-    for (int cc = 0; cc < 3; ++cc) memcpy(&loc[((size_t)i * 3 + cc) * 32], acc.col[cc], 128);
+  for (int i = 0; i < SG_LOCAL; ++i) {  // column-major over i (see kernels_sg.cu)
+    for (int cc = 0; cc < 3; ++cc)
+      for (int k = 0; k < 32; ++k) loc[((size_t)cc * 32 + k) * SG_LOCAL + i] = acc.col[cc][k];
     acc = taus_mul(t4, acc);
   }
   HCTX_CUDA(c, cudaMalloc(&c->d_sg_pow2, sizeof(uint32_t) * p2.size()));
@@ -832,11 +860,27 @@ static int subgrid_cycle(sf21_halo_ctx* c, const Cosmo& cs, double z, double gro
   HCTX_CUDA(c, launch_scan_u32(c->d_sg_wpre, c->nwords, c->d_sg_wpre, c->d_sg_chunk, c->d_cnt + 3, st));
   if ((rc = read_counts(c))) return rc;
   const uint64_t U = c->h_cnt[3];
+  // the masses of the cycle (:329, :366-367) and their scalars (:332-334),
+  // evaluated on the host cores in parallel
+  struct SgMass {
+    double M, dndm, hbias;
+  };
+  std::vector<SgMass> sm;
+  for (double m = M, r = R; m >= cf.halo_Mmin;) {
+    sm.push_back({m, r, 0.0});  // R parked in dndm until evaluated
+    m = m / pow(10.0, cf.halo_dlm);
+    r = pow(3 / 4.0 / kPI / rhom * m, 1.0 / 3);
+  }
+  host_parallel_for((int)sm.size(), [&](int i) {
+    const double r = sm[i].dndm;
+    const double sigma_aux = cs.sigma(r);
+    sm[i].dndm = cs.mass_function(z, sm[i].M, growth) * sm[i].M * (pow(10.0, cf.halo_dlm) - 1) * pow(c->dx, 3);
+    sm[i].hbias = cs.bias(sigma_aux, growth);
+  });
   long total = 0;
-  while (M >= cf.halo_Mmin) {  // :329
-    const double sigma_aux = cs.sigma(R);
-    const double dndm = cs.mass_function(z, M, growth) * M * (pow(10.0, cf.halo_dlm) - 1) * pow(c->dx, 3);
-    const double hbias = cs.bias(sigma_aux, growth);
+  for (const SgMass& sgm : sm) {
+    M = sgm.M;
+    const double dndm = sgm.dndm, hbias = sgm.hbias;
     if (!(dndm <= 10.0))
       HCTX_FAIL(c, SF21_E_UNSUPPORTED, "subgrid: Poisson mean %g per cell above 10 (M = %E)", dndm, M);
     if (U > 0) {
@@ -851,38 +895,42 @@ static int subgrid_cycle(sf21_halo_ctx* c, const Cosmo& cs, double z, double gro
       long nblocks = (long)ceil(need / SG_B);
       for (int attempt = 0;; ++attempt) {
         const long Q = nblocks * SG_B;
-        const long ngroups = (nblocks + SG_G - 1) / SG_G;
         if ((rc = grow(c, &c->d_sgL, Q, &c->sgL_cap))) return rc;
         if (nblocks > c->sg_blocks_cap || !c->d_sgX) {
-          const long nb = nblocks, ng = ngroups;
-          uint8_t** b8[] = {&c->d_sgX, &c->d_sgGX, &c->d_sg_gentry, &c->d_sg_bentry};
-          for (uint8_t** q : b8)
-            if (*q) cudaFree(*q), *q = nullptr;
-          if (c->d_sgD) cudaFree(c->d_sgD), c->d_sgD = nullptr;
-          if (c->d_sgGD) cudaFree(c->d_sgGD), c->d_sgGD = nullptr;
-          if (c->d_sg_cnt) cudaFree(c->d_sg_cnt), c->d_sg_cnt = nullptr;
-          if (c->d_sg_gbase) cudaFree(c->d_sg_gbase), c->d_sg_gbase = nullptr;
-          if (c->d_sg_bbase) cudaFree(c->d_sg_bbase), c->d_sg_bbase = nullptr;
+          const long nb = nblocks, ng = sg_groups(nb), ns = sg_groups(ng);
+          void* old[] = {c->d_sgX,        c->d_sgD,        c->d_sg_cnt,     c->sg_eb.gx,    c->sg_eb.sx,
+                         c->sg_eb.gentry, c->sg_eb.sentry, c->sg_eb.bentry, c->sg_eb.gd,    c->sg_eb.sd,
+                         c->sg_eb.gbase,  c->sg_eb.sbase,  c->sg_eb.bbase};
+          for (void* q : old)
+            if (q) cudaFree(q);
+          c->d_sgX = nullptr;
+          c->d_sgD = nullptr;
+          c->d_sg_cnt = nullptr;
+          c->sg_eb = SgEntryBufs{};
           c->sg_blocks_cap = 0;
           HCTX_CUDA(c, cudaMalloc(&c->d_sgX, (size_t)nb * SG_LMAX));
           HCTX_CUDA(c, cudaMalloc(&c->d_sgD, sizeof(uint16_t) * (size_t)nb * SG_LMAX));
-          HCTX_CUDA(c, cudaMalloc(&c->d_sgGX, (size_t)ng * SG_LMAX));
-          HCTX_CUDA(c, cudaMalloc(&c->d_sgGD, sizeof(uint32_t) * (size_t)ng * SG_LMAX));
-          HCTX_CUDA(c, cudaMalloc(&c->d_sg_gentry, (size_t)ng));
-          HCTX_CUDA(c, cudaMalloc(&c->d_sg_gbase, sizeof(uint64_t) * (size_t)(ng + 1)));
-          HCTX_CUDA(c, cudaMalloc(&c->d_sg_bentry, (size_t)nb));
-          HCTX_CUDA(c, cudaMalloc(&c->d_sg_bbase, sizeof(uint64_t) * (size_t)nb));
           HCTX_CUDA(c, cudaMalloc(&c->d_sg_cnt, sizeof(uint32_t) * (size_t)nb));
+          HCTX_CUDA(c, cudaMalloc(&c->sg_eb.gx, (size_t)ng * SG_LMAX));
+          HCTX_CUDA(c, cudaMalloc(&c->sg_eb.gd, sizeof(uint32_t) * (size_t)ng * SG_LMAX));
+          HCTX_CUDA(c, cudaMalloc(&c->sg_eb.sx, (size_t)ns * SG_LMAX));
+          HCTX_CUDA(c, cudaMalloc(&c->sg_eb.sd, sizeof(uint32_t) * (size_t)ns * SG_LMAX));
+          HCTX_CUDA(c, cudaMalloc(&c->sg_eb.sentry, (size_t)ns));
+          HCTX_CUDA(c, cudaMalloc(&c->sg_eb.sbase, sizeof(uint64_t) * (size_t)(ns + 1)));
+          HCTX_CUDA(c, cudaMalloc(&c->sg_eb.gentry, (size_t)ng));
+          HCTX_CUDA(c, cudaMalloc(&c->sg_eb.gbase, sizeof(uint64_t) * (size_t)ng));
+          HCTX_CUDA(c, cudaMalloc(&c->sg_eb.bentry, (size_t)nb));
+          HCTX_CUDA(c, cudaMalloc(&c->sg_eb.bbase, sizeof(uint64_t) * (size_t)nb));
           c->sg_blocks_cap = nb;
         }
         HCTX_CUDA(c, cudaMemsetAsync(c->d_sg_err, 0, sizeof(int) * 3, st));
         HCTX_CUDA(c, launch_sg_len(nblocks, a, c->d_sg_pow2, c->d_sg_local, c->d_sgL, c->d_sgX, c->d_sgD,
                                    c->d_sg_err, st));
-        HCTX_CUDA(c, launch_sg_entries(c->d_sgX, c->d_sgD, nblocks, c->d_sgGX, c->d_sgGD, c->d_sg_gentry,
-                                       c->d_sg_gbase, c->d_sg_bentry, c->d_sg_bbase, st));
+        HCTX_CUDA(c, launch_sg_entries(c->d_sgX, c->d_sgD, nblocks, c->sg_eb, st));
         uint64_t avail = 0;
         int errf = 0;
-        HCTX_CUDA(c, cudaMemcpyAsync(&avail, c->d_sg_gbase + ngroups, sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+        const long nsuper = sg_groups(sg_groups(nblocks));
+        HCTX_CUDA(c, cudaMemcpyAsync(&avail, c->sg_eb.sbase + nsuper, sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
         HCTX_CUDA(c, cudaMemcpyAsync(&errf, c->d_sg_err, sizeof(int), cudaMemcpyDeviceToHost, st));
         HCTX_CUDA(c, cudaStreamSynchronize(st));
         if (errf) HCTX_FAIL(c, SF21_E_UNSUPPORTED, "subgrid: a Poisson draw needed more than %d uniforms", SG_LMAX);
@@ -892,7 +940,7 @@ static int subgrid_cycle(sf21_halo_ctx* c, const Cosmo& cs, double z, double gro
         nblocks *= 2;
       }
       // draws with k >= 1: count per block, offsets, list
-      HCTX_CUDA(c, launch_sg_walk(0, c->d_sgL, nblocks, c->d_sg_bentry, c->d_sg_bbase, U, c->d_sg_cnt, c->d_sg_u64,
+      HCTX_CUDA(c, launch_sg_walk(0, c->d_sgL, nblocks, c->sg_eb.bentry, c->sg_eb.bbase, U, c->d_sg_cnt, c->d_sg_u64,
                                   nullptr, nullptr, 0, c->d_sg_err, st));
       if ((rc = sg_chunk(c, nblocks))) return rc;
       HCTX_CUDA(c, launch_scan_u32(c->d_sg_cnt, nblocks, c->d_sg_cnt, c->d_sg_chunk, c->d_cnt + 3, st));
@@ -911,7 +959,7 @@ static int subgrid_cycle(sf21_halo_ctx* c, const Cosmo& cs, double z, double gro
       c->sg_draw_cap = std::max(c->sg_draw_cap, std::max(nd, 1L));
       long recs = 0;
       if (nd > 0) {
-        HCTX_CUDA(c, launch_sg_walk(1, c->d_sgL, nblocks, c->d_sg_bentry, c->d_sg_bbase, U, c->d_sg_cnt, nullptr,
+        HCTX_CUDA(c, launch_sg_walk(1, c->d_sgL, nblocks, c->sg_eb.bentry, c->sg_eb.bbase, U, c->d_sg_cnt, nullptr,
                                     c->d_sg_dn, c->d_sg_dk, (uint64_t)c->sg_draw_cap, c->d_sg_err, st));
         uint64_t gb, hb;
         memcpy(&gb, &growth, 8);
@@ -937,8 +985,6 @@ static int subgrid_cycle(sf21_halo_ctx* c, const Cosmo& cs, double z, double gro
       taus_jump(c->rng, consumed);
       total += recs;
     }
-    M = M / pow(10.0, cf.halo_dlm);  // :366-367
-    R = pow(3 / 4.0 / kPI / rhom * M, 1.0 / 3);
   }
   *total_out = total;
   return SF21_OK;
@@ -976,9 +1022,9 @@ static int run_filter_bank(sf21_halo_ctx* c, const std::vector<MassPlan>& plan, 
       ++hb.K;
     }
     bt.K = hb.K;
-    HCTX_CUDA(c, launch_hf_rows_filter(N, c->d_spec, hb, c->d_tw, st));
-    HCTX_CUDA(c, launch_cols(N, nullptr, bt, bt.K, 1, true, c->d_tw, st));
-    HCTX_CUDA(c, launch_hf_cols_a_thresh(N, hb, c->d_tw, st));
+    HCTX_CUDA(c, launch_hf_rows_filter_cb(N, c->d_spec, hb, c->d_tw, st));
+    HCTX_CUDA(c, launch_cols_b_cb(N, bt, c->d_tw, st));
+    HCTX_CUDA(c, launch_hf_cols_a_thresh_cb(N, hb, c->d_tw, st));
   }
   return SF21_OK;
 }
@@ -991,9 +1037,9 @@ extern "C" int sf21_halo_find_z(sf21_halo_ctx* c, double z, long* nhalos) {
   const sf21_halo_config& cf = c->cfg;
   // schedule
   std::vector<sf21_halo_mass> ms;
-  if (plan_masses(cf, z, ms) != SF21_OK) HCTX_FAIL(c, SF21_E_ARG, "mass schedule longer than 4096 entries");
   const Cosmo cs(cf);
   const double growth = cs.growth(z);
+  if (plan_masses(cs, z, growth, ms) != SF21_OK) HCTX_FAIL(c, SF21_E_ARG, "mass schedule longer than 4096 entries");
   std::vector<MassPlan> plan(ms.size());
   std::vector<int4> table;
   c->mask_of.assign(ms.size(), -1);
@@ -1117,7 +1163,8 @@ extern "C" int sf21_halo_field(sf21_halo_ctx* c, double z, int m, float* out) {
   if (!out) HCTX_FAIL(c, SF21_E_ARG, "null output");
   if (!c->have_density) HCTX_FAIL(c, SF21_E_ARG, "no density box (sf21_halo_set_density first)");
   std::vector<sf21_halo_mass> ms;
-  if (plan_masses(c->cfg, z, ms) != SF21_OK || m < 0 || m >= (int)ms.size())
+  const Cosmo cs0(c->cfg);
+  if (plan_masses(cs0, z, cs0.growth(z), ms) != SF21_OK || m < 0 || m >= (int)ms.size())
     HCTX_FAIL(c, SF21_E_ARG, "mass %d not in the schedule", m);
   HCTX_CUDA(c, cudaSetDevice(c->device));
   const int N = (int)c->N;

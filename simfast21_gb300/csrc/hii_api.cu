@@ -17,6 +17,8 @@
 #include <stdint.h>
 #include <stdio.h>
 #include <string.h>
+#include <sys/stat.h>
+#include <stdlib.h>
 
 #include <string>
 #include <thread>
@@ -166,6 +168,83 @@ static void span(sf21_hii_ctx* c, int kind, int a, int b) {
 }
 
 static std::string g_create_err;
+
+// ---- autotuner cache --------------------------------------------------------
+// One JSON object per line, {"key": "<device>|N=<N>|K=<K>", "ms": [t1, ..., t7]}
+// (milliseconds of one batch per radius pipeline, 0 = not available), in
+// $SF21_TUNE_CACHE, else $XDG_CACHE_HOME/simfast21_gb300/tune.jsonl, else
+// ~/.cache/simfast21_gb300/tune.jsonl.  SF21_RETUNE=1 ignores the cache (and
+// rewrites the entry).  A missing or unreadable cache only means tuning again.
+static std::string tune_cache_path() {
+  if (const char* p = getenv("SF21_TUNE_CACHE")) return p;
+  std::string dir;
+  if (const char* x = getenv("XDG_CACHE_HOME")) dir = x;
+  else if (const char* h = getenv("HOME")) dir = std::string(h) + "/.cache";
+  else return "";
+  return dir + "/simfast21_gb300/tune.jsonl";
+}
+
+static std::string tune_key(int device, long N, int K) {
+  cudaDeviceProp pr;
+  char b[512];
+  if (cudaGetDeviceProperties(&pr, device) != cudaSuccess) return "";
+  snprintf(b, sizeof b, "%s sm_%d%d x%d|N=%ld|K=%d", pr.name, pr.major, pr.minor, pr.multiProcessorCount, N, K);
+  for (char* q = b; *q; ++q)
+    if (*q == '"' || *q == '\\') *q = '_';
+  return b;
+}
+
+static bool tune_cache_lookup(const std::string& key, double* ms, int npath) {
+  const char* re = getenv("SF21_RETUNE");
+  if (key.empty() || (re && re[0] == '1')) return false;
+  const std::string path = tune_cache_path();
+  FILE* f = path.empty() ? nullptr : fopen(path.c_str(), "r");
+  if (!f) return false;
+  char line[2048];
+  bool found = false;
+  const std::string want = "{\"key\": \"" + key + "\", \"ms\": [";
+  while (fgets(line, sizeof line, f)) {
+    if (strncmp(line, want.c_str(), want.size()) != 0) continue;
+    double v[16];
+    const char* q = line + want.size();
+    int n = 0;
+    while (n < npath) {
+      char* end = nullptr;
+      v[n] = strtod(q, &end);
+      if (end == q) break;
+      ++n;
+      q = end;
+      while (*q == ',' || *q == ' ') ++q;
+    }
+    if (n != npath) continue;
+    bool any = false;
+    for (int p = 1; p <= npath; ++p) {
+      ms[p] = v[p - 1] > 0 ? v[p - 1] : 1e30;
+      any |= v[p - 1] > 0;
+    }
+    found = any;  // the last matching line wins
+  }
+  fclose(f);
+  return found;
+}
+
+static void tune_cache_store(const std::string& key, const double* ms, int npath) {
+  const std::string path = tune_cache_path();
+  if (key.empty() || path.empty()) return;
+  const size_t slash = path.rfind('/');
+  if (slash != std::string::npos) {  // create the directory (and its parent) if needed
+    const std::string dir = path.substr(0, slash);
+    const size_t up = dir.rfind('/');
+    if (up != std::string::npos) mkdir(dir.substr(0, up).c_str(), 0755);
+    mkdir(dir.c_str(), 0755);
+  }
+  FILE* f = fopen(path.c_str(), "a");
+  if (!f) return;
+  fprintf(f, "{\"key\": \"%s\", \"ms\": [", key.c_str());
+  for (int p = 1; p <= npath; ++p) fprintf(f, "%s%.6g", p > 1 ? ", " : "", ms[p] < 1e29 ? ms[p] : 0.0);
+  fprintf(f, "]}\n");
+  fclose(f);
+}
 
 #define CTX_FAIL(ctx, code, ...)                                  \
   do {                                                            \
@@ -378,7 +457,14 @@ extern "C" int sf21_hii_create(const sf21_hii_config* cfg, sf21_hii_ctx** out) {
     return SF21_E_UNSUPPORTED;
   }
   c->path = want ? want : 1;
-  if (want == 0 && (can_plane || can_pipe)) {
+  // a tuning result cached for this device, box size and batch size skips the timing
+  const std::string tkey = tune_key(c->device, N, K);
+  if (want == 0 && (can_plane || can_pipe) && tune_cache_lookup(tkey, c->tune_ms, NPATH)) {
+    for (int p = 2; p <= NPATH; ++p)
+      if (c->tune_ms[p] < c->tune_ms[c->path]) c->path = p;
+    if ((c->path == 2 && !can_plane) || ((c->path == 3 || c->path == 4 || c->path == 6 || c->path == 7) && !can_pipe))
+      c->path = 1;
+  } else if (want == 0 && (can_plane || can_pipe)) {
     CREATE_CUDA(cudaMemsetAsync(c->d_spec, 0, box_c, c->stream));
     CREATE_CUDA(cudaMemsetAsync(c->d_alpha, 0, sizeof(float), c->stream));
     Batch bt;
@@ -425,6 +511,7 @@ extern "C" int sf21_hii_create(const sf21_hii_config* cfg, sf21_hii_ctx** out) {
     c->path = 1;
     for (int p = 2; p <= NPATH; ++p)
       if (best[p] < best[c->path]) c->path = p;
+    tune_cache_store(tkey, c->tune_ms, NPATH);
   }
 #undef CREATE_CUDA
   *out = c;

@@ -16,25 +16,11 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "cb_layout.cuh"
 #include "sf21_device.cuh"
 #include "sf21_kernels.h"
 
 namespace sf21 {
-
-template <int N>
-struct CbGeom {
-  static constexpr int CW = (N <= 512) ? 16 : 8;  // columns per block (CW * 8 bytes per run)
-  static constexpr int NBLK = N / CW;
-  static constexpr int RT = N / 8;                // threads per row (c-axis pass)
-  static constexpr int ROWS = (256 / RT) > 0 ? (256 / RT) : 1;
-  static constexpr int RTHREADS = RT * ROWS;
-};
-
-template <int N>
-__device__ __forceinline__ long cb_index(int a, int b, int c) {
-  using G = CbGeom<N>;
-  return (((long)(c / G::CW) * N + a) * N + b) * G::CW + (c % G::CW);
-}
 
 // c-axis inverse pass with the top-hat filter of the K radii of the batch
 // (get_HIIbubbles.c:305-322): spectrum row (a, b) read once, K filtered
@@ -111,15 +97,6 @@ k_rows_filter_cb(const float2* __restrict__ spec, Batch bt, const float2* __rest
 // lines x 2 threads, whose shared-memory exchanges of the line FFT are free of
 // bank conflicts.  (Half blocks of 8 columns, two CTAs per SM, measured
 // slower even with a conflict-free exchange padding.)
-template <int N>
-struct KGeom {
-  static constexpr int KW = CbGeom<N>::CW;  // columns per CTA
-  static constexpr int THREADS = KW * (N / 8);
-  static constexpr int LS = LineGeom<N>::LS;  // float2 per exchange line
-  static constexpr size_t SMEM = (size_t)(N + 2 * KW * LS) * sizeof(float2);  // two lines each
-  static constexpr int PER_SM = THREADS <= 512 ? 2 : 1;
-};
-
 template <int N>
 __global__ void __launch_bounds__(KGeom<N>::THREADS, KGeom<N>::PER_SM)
 k_cols_b_cb(Batch bt, const float2* __restrict__ gtw) {

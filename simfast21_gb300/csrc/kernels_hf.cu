@@ -6,7 +6,9 @@
 // parts are the two filtered fields (F is Hermitian and W real, so both are
 // real).  The a-axis inverse pass ends in the threshold of each field and
 // writes one candidate bit per cell and mass (bit t of word t / 32 = cell t,
-// t = (i N + j) N + p, the reference's scan order :236-239).
+// t = (i N + j) N + p, the reference's scan order :236-239).  Two forms: over
+// column-block-major work boxes (the production path) and over natural boxes
+// (the field hook for the tests).
 //
 // Overlap test (:240-268), per mass in the reference's order: the reference
 // accepts a candidate c when none of the cells of its sphere S(c) (the
@@ -30,6 +32,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "cb_layout.cuh"
 #include "sf21_device.cuh"
 #include "sf21_kernels.h"
 
@@ -125,6 +128,119 @@ k_hf_cols_a_thresh(HfBatch hb, const float2* __restrict__ gtw) {
   }
 }
 
+// The same two passes over column-block-major work boxes (cb_layout.cuh),
+// the production form: the c-axis pass writes each row as N / CW runs of CW
+// values, the b-axis pass is kernels_cb.cu's k_cols_b_cb, and an a-axis tile
+// (fixed b, one column block) reads N runs of CW values inside one slab.
+template <int N>
+__global__ void __launch_bounds__(CbGeom<N>::RTHREADS)
+k_hf_rows_filter_cb(const float2* __restrict__ spec, HfBatch hb, const float2* __restrict__ gtw) {
+  using G = CbGeom<N>;
+  using L = LineGeom<N>;
+  constexpr int T = N / 8;
+  __shared__ float2 stw[N];
+  __shared__ float2 sbuf[2 * G::ROWS * L::LS];  // two exchange lines per row
+  for (int t = threadIdx.x; t < N; t += blockDim.x) stw[t] = gtw[t];
+  const int row_in_cta = threadIdx.x / G::RT;
+  const int j = threadIdx.x % G::RT;
+  const long row = (long)blockIdx.x * G::ROWS + row_in_cta;
+  const int a = (int)(row / N), b = (int)(row % N);
+  float2* s0 = sbuf + row_in_cta * L::LS;
+  float2* s1 = sbuf + (G::ROWS + row_in_cta) * L::LS;
+  const int ka = kfreq(a, N), kb = kfreq(b, N);
+  const int kab = ka * ka + kb * kb;
+  float2 z[8];
+  float kmag[8];
+  const float2* src = spec + row * N;
+#pragma unroll
+  for (int r = 0; r < 8; ++r) {
+    const int c = j + r * T;
+    z[r] = __ldg(src + c);
+    const int kc = kfreq(c, N);
+    kmag[r] = sqrtf((float)(kab + kc * kc));
+  }
+  __syncthreads();
+  for (int k = 0; k < hb.K; ++k) {
+    const HfPair& pr = hb.p[k];
+    float2 v[8];
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      const float wa = hb.scale * w_tophat(pr.dkRa * kmag[r]);
+      const float wb = pr.bits_b ? hb.scale * w_tophat(pr.dkRb * kmag[r]) : 0.0f;
+      v[r] = make_float2(z[r].x * wa - z[r].y * wb, z[r].x * wb + z[r].y * wa);
+    }
+    if (FftPP<N>::CALL_SYNC) __syncthreads();
+    fft_line_pp<N, true>(v, s0, s1, stw, j);
+    if constexpr ((N / 8) % G::CW == 0) {
+      float2* dst = pr.work + cb_index<N>(a, b, j);
+      constexpr long RSTRIDE = (long)(N / 8 / G::CW) * N * N * G::CW;
+#pragma unroll
+      for (int r = 0; r < 8; ++r) dst[r * RSTRIDE] = v[r];
+    } else {
+#pragma unroll
+      for (int r = 0; r < 8; ++r) pr.work[cb_index<N>(a, b, j + r * T)] = v[r];
+    }
+  }
+}
+
+template <int N>
+__global__ void __launch_bounds__(KGeom<N>::THREADS, KGeom<N>::PER_SM)
+k_hf_cols_a_thresh_cb(HfBatch hb, const float2* __restrict__ gtw) {
+  using G = CbGeom<N>;
+  using X = KGeom<N>;
+  extern __shared__ float2 dsm[];
+  float2* stw = dsm;
+  float2* sbuf = dsm + N;
+  for (int t = threadIdx.x; t < N; t += blockDim.x) stw[t] = gtw[t];
+  const int col = threadIdx.x % X::KW;
+  const int j = threadIdx.x / X::KW;
+  const int lane = threadIdx.x & 31;
+  const int cb = blockIdx.x / N, b = blockIdx.x % N;
+  const long astride = (long)N * G::CW;
+  const long tbase = ((long)cb * N * N + b) * G::CW + col;  // element (a = 0, b, cb CW + col)
+  constexpr uint32_t cmask = (1u << G::CW) - 1u;
+  auto load = [&](float2 (&v)[8], int k) {
+    const float2* box = hb.p[k].work + tbase;
+#pragma unroll
+    for (int r = 0; r < 8; ++r) v[r] = box[(long)(j + r * (N / 8)) * astride];
+  };
+  auto thresh = [&](const float2 (&v)[8], int k) {
+    const HfPair& pr = hb.p[k];
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      const long t = ((long)(j + r * (N / 8)) * N + b) * N + (long)cb * G::CW;  // first cell of the run
+      const uint32_t ma = __ballot_sync(0xffffffffu, v[r].x > pr.thr_a);
+      const uint32_t mb = __ballot_sync(0xffffffffu, v[r].y > pr.thr_b);
+      if (col == 0) {
+        if (G::CW == 16) {
+          reinterpret_cast<uint16_t*>(pr.bits_a)[t >> 4] = (uint16_t)((ma >> lane) & cmask);
+          if (pr.bits_b) reinterpret_cast<uint16_t*>(pr.bits_b)[t >> 4] = (uint16_t)((mb >> lane) & cmask);
+        } else {
+          reinterpret_cast<uint8_t*>(pr.bits_a)[t >> 3] = (uint8_t)((ma >> lane) & cmask);
+          if (pr.bits_b) reinterpret_cast<uint8_t*>(pr.bits_b)[t >> 3] = (uint8_t)((mb >> lane) & cmask);
+        }
+      }
+    }
+  };
+  float2* s0 = sbuf + col * X::LS;
+  float2* s1 = sbuf + (X::KW + col) * X::LS;
+  float2 va[8], vb[8];
+  load(va, 0);
+  __syncthreads();  // twiddles
+  for (int k = 0; k < hb.K; k += 2) {
+    if (k + 1 < hb.K) load(vb, k + 1);
+    if (FftPP<N>::CALL_SYNC && k > 0) __syncthreads();
+    fft_line_pp<N, true>(va, s0, s1, stw, j);
+    thresh(va, k);
+    if (k + 1 < hb.K) {
+      if (k + 2 < hb.K) load(va, k + 2);
+      if (FftPP<N>::CALL_SYNC) __syncthreads();
+      fft_line_pp<N, true>(vb, s0, s1, stw, j);
+      thresh(vb, k + 1);
+    }
+  }
+}
+
 template <int N>
 struct HfLaunch {
   static constexpr size_t smem_cols() { return (N + ColGeom<N>::CW * LineGeom<N>::LS) * sizeof(float2); }
@@ -137,9 +253,22 @@ struct HfLaunch {
                                                                                                                tw);
     return cudaGetLastError();
   }
+  static cudaError_t rows_cb(const float2* spec, const HfBatch& hb, const float2* tw, cudaStream_t st) {
+    using G = CbGeom<N>;
+    k_hf_rows_filter_cb<N><<<(unsigned)((long)N * N / G::ROWS), G::RTHREADS, 0, st>>>(spec, hb, tw);
+    return cudaGetLastError();
+  }
+  static cudaError_t cols_a_cb(const HfBatch& hb, const float2* tw, cudaStream_t st) {
+    using X = KGeom<N>;
+    k_hf_cols_a_thresh_cb<N><<<(unsigned)(N * CbGeom<N>::NBLK), X::THREADS, X::SMEM, st>>>(hb, tw);
+    return cudaGetLastError();
+  }
   static cudaError_t setup() {
-    return cudaFuncSetAttribute(k_hf_cols_a_thresh<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)smem_cols());
+    cudaError_t e = cudaFuncSetAttribute(k_hf_cols_a_thresh<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem_cols());
+    if (e) return e;
+    return cudaFuncSetAttribute(k_hf_cols_a_thresh_cb<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)KGeom<N>::SMEM);
   }
 };
 
@@ -161,6 +290,13 @@ cudaError_t launch_hf_rows_filter(int N, const float2* spec, const HfBatch& hb, 
 }
 cudaError_t launch_hf_cols_a_thresh(int N, const HfBatch& hb, const float2* tw, cudaStream_t st) {
   SF21_HF_DISPATCH(N, HL::cols_a(hb, tw, st));
+}
+cudaError_t launch_hf_rows_filter_cb(int N, const float2* spec, const HfBatch& hb, const float2* tw,
+                                     cudaStream_t st) {
+  SF21_HF_DISPATCH(N, HL::rows_cb(spec, hb, tw, st));
+}
+cudaError_t launch_hf_cols_a_thresh_cb(int N, const HfBatch& hb, const float2* tw, cudaStream_t st) {
+  SF21_HF_DISPATCH(N, HL::cols_a_cb(hb, tw, st));
 }
 
 // ---------------------------------------------------------------------------

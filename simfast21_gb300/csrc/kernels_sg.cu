@@ -11,22 +11,25 @@
 //      block (the generator is linear over GF(2): 32x32 bit matrices of its
 //      powers), each thread steps 4 consecutive positions, L(s) is computed
 //      for every position (one integer compare decides L = 1; longer chains
-//      multiply in soft-double), and pointer jumping gives, for every entry
+//      multiply with the IEEE double rounding done in integers), and pointer
+//      jumping gives, for every entry
 //      offset e < SG_LMAX, the block's exit offset and draw count;
 //   B  the entries of all blocks follow by composing those tables (groups of
-//      SG_G blocks in parallel, then the groups in order, then the blocks of
-//      each group);
+//      SG_G blocks, supergroups of SG_G groups, in parallel; the supergroups
+//      in order; then down to the groups and the blocks);
 //   C  each block replays its chain from its entry and lists the draws with
 //      k >= 1 (k = 0 writes nothing) with their draw index;
 //   D  draw n belongs to the n-th unflagged cell (binary search in the
 //      per-word prefix counts of the unflagged bit set); nn = (int)
 //      round(k (1 + delta growth hbias)) in soft-double; the records follow
 //      from a prefix sum over nn.
-// No FP64 unit is used: soft-double (softdouble.h) gives the IEEE results.
+// No FP64 unit is used: sg_dmul.h (the draw products) and softdouble.h (the
+// halo counts) give the IEEE results in integer arithmetic.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 #include "sf21_kernels.h"
+#include "sg_dmul.h"
 #include "softdouble.h"
 
 namespace sf21 {
@@ -35,6 +38,14 @@ __device__ __forceinline__ uint32_t gf2_apply(const uint32_t* __restrict__ col, 
   uint32_t r = 0;
 #pragma unroll
   for (int k = 0; k < 32; ++k) r ^= (0u - ((v >> k) & 1u)) & __ldg(col + k);
+  return r;
+}
+
+// the same with the columns SG_LOCAL words apart
+__device__ __forceinline__ uint32_t gf2_apply_strided(const uint32_t* __restrict__ col, uint32_t v) {
+  uint32_t r = 0;
+#pragma unroll
+  for (int k = 0; k < 32; ++k) r ^= (0u - ((v >> k) & 1u)) & __ldg(col + (size_t)k * SG_LOCAL);
   return r;
 }
 
@@ -52,8 +63,11 @@ __device__ __forceinline__ void sg_bad(int* err, int site, uint64_t idx) {
 }
 
 // A ------------------------------------------------------------------------
-// jumps: pow2[k] = T^(2^k) (k < SG_POW2), local[i] = T^(4 i) (i <= (SG_B + SG_LMAX) / 4),
-// each 3 x 32 columns.  S0: the state whose next step gives position 0.
+// jumps: pow2[(k 3 + c) 32 + col] = column col of component c of T^(2^k)
+// (k < SG_POW2); local[(c 32 + col) SG_LOCAL + i] = the same of T^(4 i)
+// (i < SG_LOCAL), stored so that the threads of a warp, each applying its own
+// power, read consecutive words.  S0: the state whose next step gives
+// position 0.
 __global__ void __launch_bounds__(SG_THREADS)
 k_sg_len(SgArgs a, const uint32_t* __restrict__ pow2, const uint32_t* __restrict__ local, uint8_t* __restrict__ Lout,
          uint8_t* __restrict__ X, uint16_t* __restrict__ D, int* __restrict__ err) {
@@ -73,8 +87,9 @@ k_sg_len(SgArgs a, const uint32_t* __restrict__ pow2, const uint32_t* __restrict
   for (int pass = 0; pass < 2; ++pass) {
     const int i0 = pass ? SG_B + 4 * threadIdx.x : 4 * threadIdx.x;
     if (pass && 4 * (int)threadIdx.x >= SG_LMAX) break;
-    const uint32_t* J = local + (size_t)(i0 / 4) * 96;
-    uint32_t x = gf2_apply(J, sS[0]), y = gf2_apply(J + 32, sS[1]), z = gf2_apply(J + 64, sS[2]);
+    const uint32_t* J = local + i0 / 4;
+    uint32_t x = gf2_apply_strided(J, sS[0]), y = gf2_apply_strided(J + 32 * SG_LOCAL, sS[1]),
+             z = gf2_apply_strided(J + 64 * SG_LOCAL, sS[2]);
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
       taus_step(x, y, z);
@@ -83,27 +98,31 @@ k_sg_len(SgArgs a, const uint32_t* __restrict__ pow2, const uint32_t* __restrict
   }
   __syncthreads();
   // L(s): x <= X1 <=> u = x 2^-32 <= exp(-mu) <=> one uniform
+  const DMant emu = dm_from_bits(a.emu);
+  uint32_t packed = 0;
 #pragma unroll
   for (int r = 0; r < 4; ++r) {
     const int i = 4 * threadIdx.x + r;
     int L = 1;
-    uint32_t xv = sx[i];
-    if (xv > a.x1) {
-      sd_t prod = sd_ldexp(sd_from_int((int64_t)xv), -32);
+    const uint32_t xv = sx[i];
+    if (xv > a.x1) {  // u_0 > exp(-mu) > 0, so xv > 0
+      DMant prod = dm_from_u32(xv);
       for (L = 2; L <= SG_LMAX; ++L) {
         const uint32_t xn = sx[i + L - 1];
-        prod = sd_mul(prod, xn ? sd_ldexp(sd_from_int((int64_t)xn), -32) : (sd_t)0);
-        if (!sd_gt(prod, a.emu)) break;
+        if (xn == 0) break;  // a zero factor ends the draw
+        prod = dm_mul_u32(prod, xn);
+        if (dm_le(prod, emu)) break;
       }
       if (L > SG_LMAX) {
         atomicOr(err, 1);
         L = SG_LMAX;
       }
     }
-    Lout[base + i] = (uint8_t)L;
+    packed |= (uint32_t)L << (8 * r);
     nxt[i] = (uint16_t)(i + L);
     cnt[i] = 1;
   }
+  reinterpret_cast<uint32_t*>(Lout + base)[threadIdx.x] = packed;
   __syncthreads();
   // pointer jumping: after log2(SG_B) rounds every chain has left the block
   for (int round = 0; (1 << round) < SG_B; ++round) {
@@ -135,48 +154,55 @@ k_sg_len(SgArgs a, const uint32_t* __restrict__ pow2, const uint32_t* __restrict
 }
 
 // B ------------------------------------------------------------------------
-__global__ void k_sg_group(const uint8_t* __restrict__ X, const uint16_t* __restrict__ D, long nblocks,
-                           uint8_t* __restrict__ GX, uint32_t* __restrict__ GD) {
+// Entries of all blocks, by composing the per-block tables (exit offset X,
+// draws D for each entry offset e < SG_LMAX) in groups of SG_G: blocks ->
+// groups -> supergroups (SG_LMAX threads per parent, each walking one entry
+// through the SG_G children), one thread over the supergroups, then down again
+// (one thread per parent walking its children from the parent's entry).
+template <class TD>
+__global__ void k_sg_compose(const uint8_t* __restrict__ X, const TD* __restrict__ D, long n,
+                             uint8_t* __restrict__ PX, uint32_t* __restrict__ PD) {
   const long g = blockIdx.x;
   const int e0 = threadIdx.x;  // SG_LMAX threads
   int e = e0;
   uint32_t tot = 0;
-  const long b1 = (g + 1) * SG_G < nblocks ? (g + 1) * SG_G : nblocks;
-  for (long b = g * SG_G; b < b1; ++b) {
-    tot += D[(size_t)b * SG_LMAX + e];
-    e = X[(size_t)b * SG_LMAX + e];
+  const long c1 = (g + 1) * SG_G < n ? (g + 1) * SG_G : n;
+  for (long c = g * SG_G; c < c1; ++c) {
+    tot += D[(size_t)c * SG_LMAX + e];
+    e = X[(size_t)c * SG_LMAX + e];
   }
-  GX[(size_t)g * SG_LMAX + e0] = (uint8_t)e;
-  GD[(size_t)g * SG_LMAX + e0] = tot;
+  PX[(size_t)g * SG_LMAX + e0] = (uint8_t)e;
+  PD[(size_t)g * SG_LMAX + e0] = tot;
 }
 
-__global__ void k_sg_top(const uint8_t* __restrict__ GX, const uint32_t* __restrict__ GD, long ngroups,
-                         uint8_t* __restrict__ gentry, uint64_t* __restrict__ gbase) {
+__global__ void k_sg_top(const uint8_t* __restrict__ X, const uint32_t* __restrict__ D, long n,
+                         uint8_t* __restrict__ entry, uint64_t* __restrict__ base_out) {
   if (threadIdx.x || blockIdx.x) return;
   int e = 0;
   uint64_t base = 0;
-  for (long g = 0; g < ngroups; ++g) {
-    gentry[g] = (uint8_t)e;
-    gbase[g] = base;
-    base += GD[(size_t)g * SG_LMAX + e];
-    e = GX[(size_t)g * SG_LMAX + e];
+  for (long c = 0; c < n; ++c) {
+    entry[c] = (uint8_t)e;
+    base_out[c] = base;
+    base += D[(size_t)c * SG_LMAX + e];
+    e = X[(size_t)c * SG_LMAX + e];
   }
-  gbase[ngroups] = base;  // draws available in all generated positions
+  base_out[n] = base;  // draws available in all generated positions
 }
 
-__global__ void k_sg_blocks(const uint8_t* __restrict__ X, const uint16_t* __restrict__ D, long nblocks,
-                            long ngroups, const uint8_t* __restrict__ gentry, const uint64_t* __restrict__ gbase,
-                            uint8_t* __restrict__ bentry, uint64_t* __restrict__ bbase) {
+template <class TD>
+__global__ void k_sg_descend(const uint8_t* __restrict__ X, const TD* __restrict__ D, long n, long nparents,
+                             const uint8_t* __restrict__ pentry, const uint64_t* __restrict__ pbase,
+                             uint8_t* __restrict__ entry, uint64_t* __restrict__ base_out) {
   const long g = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= ngroups) return;
-  int e = gentry[g];
-  uint64_t base = gbase[g];
-  const long b1 = (g + 1) * SG_G < nblocks ? (g + 1) * SG_G : nblocks;
-  for (long b = g * SG_G; b < b1; ++b) {
-    bentry[b] = (uint8_t)e;
-    bbase[b] = base;
-    base += D[(size_t)b * SG_LMAX + e];
-    e = X[(size_t)b * SG_LMAX + e];
+  if (g >= nparents) return;
+  int e = pentry[g];
+  uint64_t base = pbase[g];
+  const long c1 = (g + 1) * SG_G < n ? (g + 1) * SG_G : n;
+  for (long c = g * SG_G; c < c1; ++c) {
+    entry[c] = (uint8_t)e;
+    base_out[c] = base;
+    base += D[(size_t)c * SG_LMAX + e];
+    e = X[(size_t)c * SG_LMAX + e];
   }
 }
 
@@ -379,16 +405,23 @@ cudaError_t launch_sg_len(long nblocks, const SgArgs& a, const uint32_t* pow2, c
   return cudaGetLastError();
 }
 
-cudaError_t launch_sg_entries(const uint8_t* X, const uint16_t* D, long nblocks, uint8_t* GX, uint32_t* GD,
-                              uint8_t* gentry, uint64_t* gbase, uint8_t* bentry, uint64_t* bbase, cudaStream_t st) {
-  const long ngroups = (nblocks + SG_G - 1) / SG_G;
-  k_sg_group<<<(unsigned)ngroups, SG_LMAX, 0, st>>>(X, D, nblocks, GX, GD);
+long sg_groups(long n) { return (n + SG_G - 1) / SG_G; }
+
+cudaError_t launch_sg_entries(const uint8_t* X, const uint16_t* D, long nblocks, const SgEntryBufs& eb,
+                              cudaStream_t st) {
+  const long ng = sg_groups(nblocks), ns = sg_groups(ng);
+  k_sg_compose<uint16_t><<<(unsigned)ng, SG_LMAX, 0, st>>>(X, D, nblocks, eb.gx, eb.gd);
   cudaError_t e = cudaGetLastError();
   if (e) return e;
-  k_sg_top<<<1, 32, 0, st>>>(GX, GD, ngroups, gentry, gbase);
+  k_sg_compose<uint32_t><<<(unsigned)ns, SG_LMAX, 0, st>>>(eb.gx, eb.gd, ng, eb.sx, eb.sd);
   if ((e = cudaGetLastError())) return e;
-  k_sg_blocks<<<(unsigned)((ngroups + 127) / 128), 128, 0, st>>>(X, D, nblocks, ngroups, gentry, gbase, bentry,
-                                                                  bbase);
+  k_sg_top<<<1, 32, 0, st>>>(eb.sx, eb.sd, ns, eb.sentry, eb.sbase);
+  if ((e = cudaGetLastError())) return e;
+  k_sg_descend<uint32_t><<<(unsigned)((ns + 127) / 128), 128, 0, st>>>(eb.gx, eb.gd, ng, ns, eb.sentry, eb.sbase,
+                                                                        eb.gentry, eb.gbase);
+  if ((e = cudaGetLastError())) return e;
+  k_sg_descend<uint16_t><<<(unsigned)((ng + 127) / 128), 128, 0, st>>>(X, D, nblocks, ng, eb.gentry, eb.gbase,
+                                                                        eb.bentry, eb.bbase);
   return cudaGetLastError();
 }
 

@@ -159,6 +159,11 @@ constexpr uint8_t HF_UND = 0, HF_PEND_ACC = 1, HF_PEND_REJ = 2, HF_ACC = 3, HF_A
 cudaError_t hf_setup(int N);
 cudaError_t launch_hf_rows_filter(int N, const float2* spec, const HfBatch& hb, const float2* tw, cudaStream_t st);
 cudaError_t launch_hf_cols_a_thresh(int N, const HfBatch& hb, const float2* tw, cudaStream_t st);
+// column-block-major form: rows_cb -> launch_cols_b_cb (a Batch over the same
+// work boxes) -> cols_a_thresh_cb
+cudaError_t launch_hf_rows_filter_cb(int N, const float2* spec, const HfBatch& hb, const float2* tw,
+                                     cudaStream_t st);
+cudaError_t launch_hf_cols_a_thresh_cb(int N, const HfBatch& hb, const float2* tw, cudaStream_t st);
 long hf_compact_chunks(long nwords);
 cudaError_t launch_bits_count(const uint32_t* W, long nwords, uint32_t* cnt, cudaStream_t st);
 cudaError_t launch_scan_counts(uint32_t* cnt, long n, uint32_t* tot, cudaStream_t st);
@@ -182,7 +187,7 @@ cudaError_t launch_hf_records(const uint32_t* idx, long n, int logN, float mass,
 constexpr int SG_B = 1024;               // stream positions per block
 constexpr int SG_THREADS = SG_B / 4;     // 4 consecutive positions per thread
 constexpr int SG_LMAX = 64;              // uniforms one draw may consume at most
-constexpr int SG_G = 1024;               // blocks per group of the entry composition
+constexpr int SG_G = 64;                 // children per parent in the entry composition
 constexpr int SG_POW2 = 40;              // jump matrices T^(2^k), k < SG_POW2
 constexpr int SG_LOCAL = (SG_B + SG_LMAX) / 4;  // jump matrices T^(4 i), i < SG_LOCAL
 struct SgArgs {
@@ -192,8 +197,17 @@ struct SgArgs {
 };
 cudaError_t launch_sg_len(long nblocks, const SgArgs& a, const uint32_t* pow2, const uint32_t* local, uint8_t* L,
                           uint8_t* X, uint16_t* D, int* err, cudaStream_t st);
-cudaError_t launch_sg_entries(const uint8_t* X, const uint16_t* D, long nblocks, uint8_t* GX, uint32_t* GD,
-                              uint8_t* gentry, uint64_t* gbase, uint8_t* bentry, uint64_t* bbase, cudaStream_t st);
+// composition scratch: groups (sg_groups(nblocks)) and supergroups
+// (sg_groups(groups)) tables (x SG_LMAX), their entries and draw bases
+// (sbase: supergroups + 1, the last = draws available), the blocks' entries
+struct SgEntryBufs {
+  uint8_t *gx, *sx, *gentry, *sentry, *bentry;
+  uint32_t *gd, *sd;
+  uint64_t *gbase, *sbase, *bbase;
+};
+long sg_groups(long n);
+cudaError_t launch_sg_entries(const uint8_t* X, const uint16_t* D, long nblocks, const SgEntryBufs& eb,
+                              cudaStream_t st);
 // err: int[3], [0] a draw longer than SG_LMAX, [1] site of an access outside
 // its buffer (skipped), [2] its index
 cudaError_t launch_sg_walk(int mode, const uint8_t* L, long nblocks, const uint8_t* bentry, const uint64_t* bbase,

@@ -34,3 +34,19 @@ def test_basic_ops_bit_exact(checker):
         n, bad, maxulp = stats[op]
         assert maxulp <= 1 and bad < n * 0.005, (op, stats[op])
     assert stats["pow_then_float"][1] == 0
+
+
+def test_uniform_products_bit_exact(tmp_path):
+    """sg_dmul.h, the subgrid's double products of taus uniforms in integer
+    arithmetic, against the CPU's double multiply (chains of up to 13
+    factors, including uniforms with few significant bits)."""
+    cxx = shutil.which("g++")
+    if not cxx:
+        pytest.skip("g++ not available")
+    exe = str(tmp_path / "dmul_check")
+    subprocess.run([cxx, "-O2", "-std=c++17", "-ffp-contract=off",
+                    "-I", os.path.join(ROOT, "simfast21_gb300", "csrc"),
+                    os.path.join(ROOT, "tests", "native", "dmul_check.cpp"), "-o", exe], check=True)
+    r = subprocess.run([exe, "400000", "7"], capture_output=True, text=True)
+    cases, bad = map(int, r.stdout.split())
+    assert cases > 1_000_000 and bad == 0, r.stdout + r.stderr
