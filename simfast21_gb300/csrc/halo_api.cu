@@ -457,6 +457,8 @@ struct sf21_halo_ctx {
   uint8_t* d_sgX = nullptr;
   uint16_t* d_sgD = nullptr;
   uint32_t* d_sg_cnt = nullptr;
+  uint32_t* d_sg_start = nullptr;  // taus state at each block's first position
+  uint32_t* d_sgLB = nullptr;      // per block: bit set of the positions with draws of k >= 1
   SgEntryBufs sg_eb = {};
   long sg_blocks_cap = 0;
   uint64_t* d_sg_dn = nullptr;
@@ -561,7 +563,7 @@ static void free_hctx(sf21_halo_ctx* c) {
   void* ptrs[] = {c->d_tw,        c->d_spec,      c->d_work,      c->d_delta,     c->d_FL,        c->d_UND,
                   c->d_ACC,       c->d_bits,      c->d_list,      c->d_list2,     c->d_status,    c->d_chunk,
                   c->d_cnt,       c->d_cat,       c->d_runs,      c->d_sg_pow2,   c->d_sg_local,  c->d_sgL,
-                  c->d_sgX,       c->d_sgD,       c->d_sg_cnt,    c->sg_eb.gx,    c->sg_eb.sx,    c->sg_eb.gentry,
+                  c->d_sgX,       c->d_sgD,       c->d_sg_cnt,    c->d_sg_start,  c->d_sgLB,      c->sg_eb.gx,    c->sg_eb.sx,    c->sg_eb.gentry,
                   c->sg_eb.sentry, c->sg_eb.bentry, c->sg_eb.gd,  c->sg_eb.sd,    c->sg_eb.gbase, c->sg_eb.sbase,
                   c->sg_eb.bbase, c->d_sg_dn,     c->d_sg_dk,     c->d_sg_cell,   c->d_sg_nn,     c->d_sg_wpre,
                   c->d_sg_chunk,  c->d_sg_u64,    c->d_sg_err};
@@ -898,7 +900,7 @@ static int subgrid_cycle(sf21_halo_ctx* c, const Cosmo& cs, double z, double gro
         if ((rc = grow(c, &c->d_sgL, Q, &c->sgL_cap))) return rc;
         if (nblocks > c->sg_blocks_cap || !c->d_sgX) {
           const long nb = nblocks, ng = sg_groups(nb), ns = sg_groups(ng);
-          void* old[] = {c->d_sgX,        c->d_sgD,        c->d_sg_cnt,     c->sg_eb.gx,    c->sg_eb.sx,
+          void* old[] = {c->d_sgX,        c->d_sgD,        c->d_sg_cnt,     c->d_sg_start,  c->d_sgLB,      c->sg_eb.gx,    c->sg_eb.sx,
                          c->sg_eb.gentry, c->sg_eb.sentry, c->sg_eb.bentry, c->sg_eb.gd,    c->sg_eb.sd,
                          c->sg_eb.gbase,  c->sg_eb.sbase,  c->sg_eb.bbase};
           for (void* q : old)
@@ -906,11 +908,15 @@ static int subgrid_cycle(sf21_halo_ctx* c, const Cosmo& cs, double z, double gro
           c->d_sgX = nullptr;
           c->d_sgD = nullptr;
           c->d_sg_cnt = nullptr;
+          c->d_sg_start = nullptr;
+          c->d_sgLB = nullptr;
           c->sg_eb = SgEntryBufs{};
           c->sg_blocks_cap = 0;
           HCTX_CUDA(c, cudaMalloc(&c->d_sgX, (size_t)nb * SG_LMAX));
           HCTX_CUDA(c, cudaMalloc(&c->d_sgD, sizeof(uint16_t) * (size_t)nb * SG_LMAX));
           HCTX_CUDA(c, cudaMalloc(&c->d_sg_cnt, sizeof(uint32_t) * (size_t)nb));
+          HCTX_CUDA(c, cudaMalloc(&c->d_sg_start, sizeof(uint32_t) * 3 * (size_t)nb));
+          HCTX_CUDA(c, cudaMalloc(&c->d_sgLB, sizeof(uint32_t) * (SG_B / 32) * (size_t)nb));
           HCTX_CUDA(c, cudaMalloc(&c->sg_eb.gx, (size_t)ng * SG_LMAX));
           HCTX_CUDA(c, cudaMalloc(&c->sg_eb.gd, sizeof(uint32_t) * (size_t)ng * SG_LMAX));
           HCTX_CUDA(c, cudaMalloc(&c->sg_eb.sx, (size_t)ns * SG_LMAX));
@@ -924,8 +930,8 @@ static int subgrid_cycle(sf21_halo_ctx* c, const Cosmo& cs, double z, double gro
           c->sg_blocks_cap = nb;
         }
         HCTX_CUDA(c, cudaMemsetAsync(c->d_sg_err, 0, sizeof(int) * 3, st));
-        HCTX_CUDA(c, launch_sg_len(nblocks, a, c->d_sg_pow2, c->d_sg_local, c->d_sgL, c->d_sgX, c->d_sgD,
-                                   c->d_sg_err, st));
+        HCTX_CUDA(c, launch_sg_len(nblocks, a, c->d_sg_pow2, c->d_sg_local, c->d_sg_start, c->d_sgL, c->d_sgLB,
+                                   c->d_sgX, c->d_sgD, c->d_sg_err, st));
         HCTX_CUDA(c, launch_sg_entries(c->d_sgX, c->d_sgD, nblocks, c->sg_eb, st));
         uint64_t avail = 0;
         int errf = 0;
@@ -940,7 +946,7 @@ static int subgrid_cycle(sf21_halo_ctx* c, const Cosmo& cs, double z, double gro
         nblocks *= 2;
       }
       // draws with k >= 1: count per block, offsets, list
-      HCTX_CUDA(c, launch_sg_walk(0, c->d_sgL, nblocks, c->sg_eb.bentry, c->sg_eb.bbase, U, c->d_sg_cnt, c->d_sg_u64,
+      HCTX_CUDA(c, launch_sg_walk(0, c->d_sgL, c->d_sgLB, nblocks, c->sg_eb.bentry, c->sg_eb.bbase, U, c->d_sg_cnt, c->d_sg_u64,
                                   nullptr, nullptr, 0, c->d_sg_err, st));
       if ((rc = sg_chunk(c, nblocks))) return rc;
       HCTX_CUDA(c, launch_scan_u32(c->d_sg_cnt, nblocks, c->d_sg_cnt, c->d_sg_chunk, c->d_cnt + 3, st));
@@ -959,7 +965,7 @@ static int subgrid_cycle(sf21_halo_ctx* c, const Cosmo& cs, double z, double gro
       c->sg_draw_cap = std::max(c->sg_draw_cap, std::max(nd, 1L));
       long recs = 0;
       if (nd > 0) {
-        HCTX_CUDA(c, launch_sg_walk(1, c->d_sgL, nblocks, c->sg_eb.bentry, c->sg_eb.bbase, U, c->d_sg_cnt, nullptr,
+        HCTX_CUDA(c, launch_sg_walk(1, c->d_sgL, c->d_sgLB, nblocks, c->sg_eb.bentry, c->sg_eb.bbase, U, c->d_sg_cnt, nullptr,
                                     c->d_sg_dn, c->d_sg_dk, (uint64_t)c->sg_draw_cap, c->d_sg_err, st));
         uint64_t gb, hb;
         memcpy(&gb, &growth, 8);

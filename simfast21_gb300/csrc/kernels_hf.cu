@@ -195,7 +195,11 @@ k_hf_cols_a_thresh_cb(HfBatch hb, const float2* __restrict__ gtw) {
   const int col = threadIdx.x % X::KW;
   const int j = threadIdx.x / X::KW;
   const int lane = threadIdx.x & 31;
-  const int cb = blockIdx.x / N, b = blockIdx.x % N;
+  // column block fastest: the NBLK tiles of one b write the neighbouring
+  // half-words (bytes) of the same rows of the bit sets, so they run close
+  // together and the L2 sectors fill before they are evicted (b fastest made
+  // every bit-set store a read-modify-write of a sector from DRAM)
+  const int cb = blockIdx.x % G::NBLK, b = blockIdx.x / G::NBLK;
   const long astride = (long)N * G::CW;
   const long tbase = ((long)cb * N * N + b) * G::CW + col;  // element (a = 0, b, cb CW + col)
   constexpr uint32_t cmask = (1u << G::CW) - 1u;

@@ -68,22 +68,29 @@ __device__ __forceinline__ void sg_bad(int* err, int site, uint64_t idx) {
 // (i < SG_LOCAL), stored so that the threads of a warp, each applying its own
 // power, read consecutive words.  S0: the state whose next step gives
 // position 0.
+// The state at the start of every block, T^(b SG_B) S0: one thread per
+// (block, component), so the jumps of all blocks run in parallel instead of
+// keeping a block's other threads waiting.
+__global__ void k_sg_start(SgArgs a, const uint32_t* __restrict__ pow2, long nblocks, uint32_t* __restrict__ start) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nblocks * 3) return;
+  const long b = t / 3;
+  const int c = (int)(t % 3);
+  const uint64_t base = (uint64_t)b * SG_B;
+  uint32_t v = a.s0[c];
+  for (int k = 0; k < SG_POW2; ++k)
+    if ((base >> k) & 1u) v = gf2_apply(pow2 + ((size_t)k * 3 + c) * 32, v);
+  start[t] = v;
+}
+
 __global__ void __launch_bounds__(SG_THREADS)
-k_sg_len(SgArgs a, const uint32_t* __restrict__ pow2, const uint32_t* __restrict__ local, uint8_t* __restrict__ Lout,
-         uint8_t* __restrict__ X, uint16_t* __restrict__ D, int* __restrict__ err) {
+k_sg_len(SgArgs a, const uint32_t* __restrict__ start, const uint32_t* __restrict__ local, uint8_t* __restrict__ Lout,
+         uint32_t* __restrict__ LB, uint8_t* __restrict__ X, uint16_t* __restrict__ D, int* __restrict__ err) {
   __shared__ uint32_t sx[SG_B + SG_LMAX];
-  __shared__ uint32_t sS[3];
   __shared__ uint16_t nxt[SG_B], cnt[SG_B];
   const long b = blockIdx.x;
   const uint64_t base = (uint64_t)b * SG_B;
-  if (threadIdx.x < 3) {
-    const int c = threadIdx.x;
-    uint32_t v = a.s0[c];
-    for (int k = 0; k < SG_POW2; ++k)
-      if ((base >> k) & 1u) v = gf2_apply(pow2 + ((size_t)k * 3 + c) * 32, v);
-    sS[c] = v;
-  }
-  __syncthreads();
+  const uint32_t sS[3] = {__ldg(start + 3 * b), __ldg(start + 3 * b + 1), __ldg(start + 3 * b + 2)};
   for (int pass = 0; pass < 2; ++pass) {
     const int i0 = pass ? SG_B + 4 * threadIdx.x : 4 * threadIdx.x;
     if (pass && 4 * (int)threadIdx.x >= SG_LMAX) break;
@@ -123,6 +130,16 @@ k_sg_len(SgArgs a, const uint32_t* __restrict__ pow2, const uint32_t* __restrict
     cnt[i] = 1;
   }
   reinterpret_cast<uint32_t*>(Lout + base)[threadIdx.x] = packed;
+  // bit set of the positions whose draw takes two uniforms or more (k >= 1):
+  // 4 bits per thread, 8 threads per word
+  uint32_t nib = 0;
+#pragma unroll
+  for (int r = 0; r < 4; ++r) nib |= (((packed >> (8 * r)) & 0xFFu) >= 2u ? 1u : 0u) << r;
+  uint32_t word = nib << (4 * (threadIdx.x & 7));
+  word |= __shfl_xor_sync(0xffffffffu, word, 1);
+  word |= __shfl_xor_sync(0xffffffffu, word, 2);
+  word |= __shfl_xor_sync(0xffffffffu, word, 4);
+  if ((threadIdx.x & 7) == 0) LB[(size_t)b * (SG_B / 32) + (threadIdx.x >> 3)] = word;
   __syncthreads();
   // pointer jumping: after log2(SG_B) rounds every chain has left the block
   for (int round = 0; (1 << round) < SG_B; ++round) {
@@ -209,10 +226,16 @@ __global__ void k_sg_descend(const uint8_t* __restrict__ X, const TD* __restrict
 // C ------------------------------------------------------------------------
 // mode 0: count the draws with k >= 1 among draws < U per block, and record
 // the position after draw U - 1; mode 1: write them (draw index, k).
-__global__ void k_sg_walk(int mode, const uint8_t* __restrict__ Lb, long nblocks, const uint8_t* __restrict__ bentry,
-                          const uint64_t* __restrict__ bbase, uint64_t U, uint32_t* __restrict__ cnt,
-                          uint64_t* __restrict__ consumed, uint64_t* __restrict__ dn, uint8_t* __restrict__ dk,
-                          uint64_t cap, int* __restrict__ err) {
+constexpr int WALK_THREADS = 128;
+// Each thread walks one block.  Between two long draws (k >= 1) every draw
+// takes one uniform, so the walk jumps from long position to long position
+// with the block's bit set of long positions (LB) and counts the one-uniform
+// draws in between; it touches the draw lengths (L) only at long positions.
+__global__ void __launch_bounds__(WALK_THREADS)
+k_sg_walk(int mode, const uint8_t* __restrict__ Lb, const uint32_t* __restrict__ LB, long nblocks,
+          const uint8_t* __restrict__ bentry, const uint64_t* __restrict__ bbase, uint64_t U,
+          uint32_t* __restrict__ cnt, uint64_t* __restrict__ consumed, uint64_t* __restrict__ dn,
+          uint8_t* __restrict__ dk, uint64_t cap, int* __restrict__ err) {
   const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= nblocks) return;
   uint64_t n = bbase[b];
@@ -221,22 +244,36 @@ __global__ void k_sg_walk(int mode, const uint8_t* __restrict__ Lb, long nblocks
     return;
   }
   const uint64_t base = (uint64_t)b * SG_B;
+  const uint32_t* lb = LB + (size_t)b * (SG_B / 32);
   int s = bentry[b];
   uint32_t c = 0;
   const uint32_t off = mode ? cnt[b] : 0;
   while (s < SG_B && n < U) {
-    const int L = Lb[base + s];
-    if (L >= 2) {
-      if (mode) {
-        if ((uint64_t)off + c < cap) {
-          dn[off + c] = n;
-          dk[off + c] = (uint8_t)(L - 1);
-        } else {
-          sg_bad(err, 1, (uint64_t)off + c);
-        }
-      }
-      ++c;
+    // next long position p >= s (SG_B if none)
+    int w = s >> 5;
+    uint32_t m = __ldg(lb + w) & (0xffffffffu << (s & 31));
+    while (!m && ++w < SG_B / 32) m = __ldg(lb + w);
+    const int p = m ? w * 32 + __ffs(m) - 1 : SG_B;
+    // draws at s .. p-1 take one uniform each
+    const uint64_t steps = (uint64_t)(p - s);
+    if (n + steps >= U) {  // draw U - 1 is one of them
+      if (mode == 0) *consumed = base + s + (U - 1 - n) + 1;
+      n = U;
+      break;
     }
+    n += steps;
+    s = p;
+    if (s >= SG_B) break;
+    const int L = Lb[base + s];
+    if (mode) {
+      if ((uint64_t)off + c < cap) {
+        dn[off + c] = n;
+        dk[off + c] = (uint8_t)(L - 1);
+      } else {
+        sg_bad(err, 1, (uint64_t)off + c);
+      }
+    }
+    ++c;
     if (mode == 0 && n == U - 1) *consumed = base + s + L;
     s += L;
     ++n;
@@ -399,9 +436,12 @@ static unsigned grid_for(long n, int threads) {
   return (unsigned)b;
 }
 
-cudaError_t launch_sg_len(long nblocks, const SgArgs& a, const uint32_t* pow2, const uint32_t* local, uint8_t* L,
-                          uint8_t* X, uint16_t* D, int* err, cudaStream_t st) {
-  k_sg_len<<<(unsigned)nblocks, SG_THREADS, 0, st>>>(a, pow2, local, L, X, D, err);
+cudaError_t launch_sg_len(long nblocks, const SgArgs& a, const uint32_t* pow2, const uint32_t* local, uint32_t* start,
+                          uint8_t* L, uint32_t* LB, uint8_t* X, uint16_t* D, int* err, cudaStream_t st) {
+  k_sg_start<<<(unsigned)((nblocks * 3 + 255) / 256), 256, 0, st>>>(a, pow2, nblocks, start);
+  cudaError_t e = cudaGetLastError();
+  if (e) return e;
+  k_sg_len<<<(unsigned)nblocks, SG_THREADS, 0, st>>>(a, start, local, L, LB, X, D, err);
   return cudaGetLastError();
 }
 
@@ -425,11 +465,11 @@ cudaError_t launch_sg_entries(const uint8_t* X, const uint16_t* D, long nblocks,
   return cudaGetLastError();
 }
 
-cudaError_t launch_sg_walk(int mode, const uint8_t* L, long nblocks, const uint8_t* bentry, const uint64_t* bbase,
-                           uint64_t U, uint32_t* cnt, uint64_t* consumed, uint64_t* dn, uint8_t* dk, uint64_t cap,
-                           int* err, cudaStream_t st) {
-  k_sg_walk<<<(unsigned)((nblocks + 127) / 128), 128, 0, st>>>(mode, L, nblocks, bentry, bbase, U, cnt, consumed,
-                                                                dn, dk, cap, err);
+cudaError_t launch_sg_walk(int mode, const uint8_t* L, const uint32_t* LB, long nblocks, const uint8_t* bentry,
+                           const uint64_t* bbase, uint64_t U, uint32_t* cnt, uint64_t* consumed, uint64_t* dn,
+                           uint8_t* dk, uint64_t cap, int* err, cudaStream_t st) {
+  k_sg_walk<<<(unsigned)((nblocks + WALK_THREADS - 1) / WALK_THREADS), WALK_THREADS, 0, st>>>(
+      mode, L, LB, nblocks, bentry, bbase, U, cnt, consumed, dn, dk, cap, err);
   return cudaGetLastError();
 }
 

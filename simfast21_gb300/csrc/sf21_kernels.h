@@ -195,8 +195,10 @@ struct SgArgs {
   uint32_t x1;     // one uniform suffices <=> its 32-bit draw <= x1 (= floor(exp(-mu) 2^32))
   uint64_t emu;    // exp(-mu), double bits
 };
-cudaError_t launch_sg_len(long nblocks, const SgArgs& a, const uint32_t* pow2, const uint32_t* local, uint8_t* L,
-                          uint8_t* X, uint16_t* D, int* err, cudaStream_t st);
+// start: 3 words per block (the state at its first position); L: draw length
+// per position; LB: SG_B/32 words per block, bit = draw length >= 2
+cudaError_t launch_sg_len(long nblocks, const SgArgs& a, const uint32_t* pow2, const uint32_t* local, uint32_t* start,
+                          uint8_t* L, uint32_t* LB, uint8_t* X, uint16_t* D, int* err, cudaStream_t st);
 // composition scratch: groups (sg_groups(nblocks)) and supergroups
 // (sg_groups(groups)) tables (x SG_LMAX), their entries and draw bases
 // (sbase: supergroups + 1, the last = draws available), the blocks' entries
@@ -210,9 +212,9 @@ cudaError_t launch_sg_entries(const uint8_t* X, const uint16_t* D, long nblocks,
                               cudaStream_t st);
 // err: int[3], [0] a draw longer than SG_LMAX, [1] site of an access outside
 // its buffer (skipped), [2] its index
-cudaError_t launch_sg_walk(int mode, const uint8_t* L, long nblocks, const uint8_t* bentry, const uint64_t* bbase,
-                           uint64_t U, uint32_t* cnt, uint64_t* consumed, uint64_t* dn, uint8_t* dk, uint64_t cap,
-                           int* err, cudaStream_t st);
+cudaError_t launch_sg_walk(int mode, const uint8_t* L, const uint32_t* LB, long nblocks, const uint8_t* bentry,
+                           const uint64_t* bbase, uint64_t U, uint32_t* cnt, uint64_t* consumed, uint64_t* dn,
+                           uint8_t* dk, uint64_t cap, int* err, cudaStream_t st);
 cudaError_t launch_sg_free_count(const uint32_t* FL, long nwords, uint32_t* c, cudaStream_t st);
 cudaError_t launch_sg_nn(const uint64_t* dn, const uint8_t* dk, long nd, const uint32_t* FL, const uint32_t* wpre,
                          long nwords, const float* delta, uint64_t growth, uint64_t hbias, uint32_t* cell,

@@ -57,9 +57,9 @@ def test_filtered_fields_within_tolerance(H):
     hf.close()
 
 
-def _check_case(H, name, zs_limit=None):
+def _check_case(H, name, zs_limit=None, g=None):
     from simfast21_gb300 import halos
-    g = load_halo_golden(name)
+    g = g if g is not None else load_halo_golden(name)
     hf, cfg = _finder(g, halos)
     p = H.params_from_ini(H.parse_ini(g["ini"]))
     rng = H.taus_seed(0)
@@ -85,13 +85,13 @@ def _check_case(H, name, zs_limit=None):
             band += int(near.sum())
             flips += int(diff.sum())
         # the serial loop of the oracle on the GPU's candidates: exact
-        ocat, ocounts, rng = H.find_z(p, z, g["delta"], rng, masks=masks)
+        ocat, ocounts, rng = H.find_z(p, z, g["delta"], rng, masks=masks, cap=2 * len(cat) + 65536)
         assert len(cat) == len(ocat), (name, z, len(cat), len(ocat))
         assert cat.tobytes() == ocat.tobytes(), (name, z)
         np.testing.assert_array_equal(hf.counts()[: len(sch) + 1], ocounts[: len(sch) + 1])
         # the subgrid generator continues identically
         np.testing.assert_array_equal(hf.rng().astype(np.uint64), rng)
-        if flips == 0:
+        if flips == 0 and f"sha_{i}" in g:
             assert hashlib.sha256(cat.tobytes()).hexdigest() == str(g[f"sha_{i}"]), (name, z)
         report.append((z, len(cat), band, flips))
     hf.close()
@@ -143,3 +143,18 @@ def test_driver_writes_library_catalogues(tmp_path):
     r2 = subprocess.run([build.HALO_DRIVER, base], capture_output=True, text=True, timeout=600)
     assert r2.returncode == 0 and r2.stdout.count("already exists") == len(g["zs"])
     hf.close()
+
+
+def test_catalogue_512_full_size(H):
+    """The bench's halo workload at full size (512^3, L = 100 Mpc, z = 7,
+    subgrid on, ~7.7 M halos): candidate sets within the band of the
+    oracle's fields, and the oracle's serial loop on the GPU's candidate sets
+    reproduces the GPU catalogue byte for byte (no reference run exists at
+    this size; the oracle is pinned to it on the fixtures)."""
+    from simfast21_gb300 import synth
+    w = synth.HaloWorkload(N=512, L_mpc=100.0, sigma=4.0, seed=11, subgrid=True)
+    g = {"ini": synth.halo_ini_text(w, 7.0, 7.0, 1.0), "delta": w.density().reshape((512,) * 3),
+         "zs": np.array([7.0])}
+    rep = _check_case(H, "bench512", g=g)
+    print("bench512 (z, halos, band cells, flipped cells):", rep)
+    assert rep[0][1] > 1_000_000
