@@ -12,8 +12,10 @@
  * (an int64 count, then the records, :184-185, :272, :375-376) is written by
  * the drop-in driver sf21_get_halos.
  *
- * Boxes: N_halo^3 float32, C order (x slowest, z fastest), N_halo a power of
- * two from 16 to 1024 (the library's transform sizes).
+ * Boxes: N_halo^3 float32, C order (x slowest, z fastest).  N_halo a power of
+ * two from 16 to 1024 (register transforms), or a product of 2, 3 and 5 with
+ * 8 | N_halo from 24 to 1280 such as the reference's default 1200
+ * (shared-memory transforms).
  * Return codes are the SF21_* codes of sf21_hii.h.
  */
 #ifndef SF21_HALOS_H

@@ -50,7 +50,8 @@ typedef struct {
 } sf21_hii_set;
 
 typedef struct {
-  long N;            /* global_N_smooth: power of two, 16..1024            */
+  long N;            /* global_N_smooth: a power of two 16..1024, or a
+                        product of 2, 3, 5 that 8 divides, 24..1280       */
   long N_halo;       /* global_N_halo (only for SF21_SRC_RION)             */
   double L;          /* global_L in Mpc/h (after the *h of Input_variables.c:121) */
   double hubble;     /* global_hubble                                       */

@@ -412,7 +412,10 @@ int plan_masses(const Cosmo& cs, double z, double growth, std::vector<sf21_halo_
 bool config_ok(const sf21_halo_config* c, std::string* why) {
   if (!c) return (*why = "null config"), false;
   const long N = c->N_halo;
-  if (N < 16 || N > 1024 || (N & (N - 1))) return (*why = "N_halo must be a power of two in [16, 1024]"), false;
+  const bool pow2 = N >= 16 && N <= 1024 && !(N & (N - 1));
+  if (!pow2 && !gen_supported((int)N))
+    return (*why = "N_halo must be a power of two in [16, 1024] or a product of 2, 3 and 5 with 8 | N, 24..1280"),
+           false;
   if (!(c->L > 0) || !(c->hubble > 0) || !(c->omega_m > 0) || !(c->sigma8 > 0) || !(c->halo_dlm > 0) ||
       !(c->delta_c > 0) || !(c->STa > 0))
     return (*why = "need L, hubble, omega_m, sigma8, halo_dlm, critical_overdensity, STa > 0"), false;
@@ -427,11 +430,12 @@ struct sf21_halo_ctx {
   sf21_halo_config cfg;
   int device = 0;
   long N = 0, n3 = 0, nwords = 0;
-  int logN = 0;
   double dx = 0, dk = 0;
   cudaStream_t stream = nullptr;
   float2 *d_tw = nullptr, *d_spec = nullptr, *d_work = nullptr;
   int KP = 2;  // mass pairs per filter-bank pass
+  bool gen = false;  // side not a power of two: the shared-memory transforms (kernels_gen.cu)
+  GenPlan gp = {};
   float* d_delta = nullptr;
   bool have_density = false;
   uint32_t *d_FL = nullptr, *d_UND = nullptr, *d_ACC = nullptr, *d_bits = nullptr;
@@ -606,8 +610,6 @@ extern "C" int sf21_halo_create(const sf21_halo_config* cfg, sf21_halo_ctx** out
   c->N = cfg->N_halo;
   c->n3 = c->N * c->N * c->N;
   c->nwords = c->n3 / 32;
-  c->logN = 0;
-  while ((1L << c->logN) < c->N) ++c->logN;
   c->dx = cfg->L / c->N;
   c->dk = 2 * kPI / cfg->L;
   taus_seed(0, c->rng);
@@ -623,9 +625,15 @@ extern "C" int sf21_halo_create(const sf21_halo_config* cfg, sf21_halo_ctx** out
   const int N = (int)c->N;
   HCREATE(cudaSetDevice(c->device));
   HCREATE(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
-  HCREATE(fft_setup(N));
-  HCREATE(cb_setup(N));
-  HCREATE(hf_setup(N));
+  c->gen = N & (N - 1);
+  if (c->gen) {
+    c->gp = gen_plan(N);
+    HCREATE(gen_setup(N));
+  } else {
+    HCREATE(fft_setup(N));
+    HCREATE(cb_setup(N));
+    HCREATE(hf_setup(N));
+  }
   const size_t box_c = sizeof(float2) * c->n3, bits = sizeof(uint32_t) * c->nwords;
   HCREATE(cudaMalloc(&c->d_spec, box_c));
   HCREATE(cudaMalloc(&c->d_work, box_c * c->KP));
@@ -640,7 +648,12 @@ extern "C" int sf21_halo_create(const sf21_halo_config* cfg, sf21_halo_ctx** out
   HCREATE(cudaMalloc(&c->d_cnt, sizeof(uint32_t) * 4));
   HCREATE(cudaMallocHost(&c->h_cnt, sizeof(uint32_t) * 4));
   std::vector<float2> tw(N);
-  {
+  if (c->gen) {  // plain table exp(-2 pi i t / N)
+    for (int t = 0; t < N; ++t) {
+      const double ang = -2.0 * kPI * t / N;
+      tw[t] = make_float2((float)cos(ang), (float)sin(ang));
+    }
+  } else {
     std::vector<double> tre(N), tim(N);
     twiddle_layout(N, tre.data(), tim.data());
     for (int t = 0; t < N; ++t) tw[t] = make_float2((float)tre[t], (float)tim[t]);
@@ -665,9 +678,15 @@ static int set_density_dev(sf21_halo_ctx* c, const float* d, cudaStream_t st) {
   if (d != c->d_delta) HCTX_CUDA(c, cudaMemcpyAsync(c->d_delta, d, sizeof(float) * c->n3, cudaMemcpyDeviceToDevice, st));
   float2* packed = c->d_work;
   HCTX_CUDA(c, launch_t21_pack(c->n3, c->d_delta, packed, st));
-  HCTX_CUDA(c, launch_fwd_rows(N, packed, c->d_spec, nullptr, c->d_tw, st));
-  HCTX_CUDA(c, launch_cols(N, c->d_spec, none, 1, 1, false, c->d_tw, st));
-  HCTX_CUDA(c, launch_cols(N, c->d_spec, none, 1, 0, false, c->d_tw, st));
+  if (c->gen) {
+    HCTX_CUDA(c, launch_gen_fwd_rows(c->gp, packed, c->d_spec, nullptr, c->d_tw, st));
+    HCTX_CUDA(c, launch_gen_cols(c->gp, c->d_spec, none, 1, false, c->d_tw, st));
+    HCTX_CUDA(c, launch_gen_cols(c->gp, c->d_spec, none, 0, false, c->d_tw, st));
+  } else {
+    HCTX_CUDA(c, launch_fwd_rows(N, packed, c->d_spec, nullptr, c->d_tw, st));
+    HCTX_CUDA(c, launch_cols(N, c->d_spec, none, 1, 1, false, c->d_tw, st));
+    HCTX_CUDA(c, launch_cols(N, c->d_spec, none, 1, 0, false, c->d_tw, st));
+  }
   c->have_density = true;
   return SF21_OK;
 }
@@ -760,7 +779,7 @@ static int append_records(sf21_halo_ctx* c, const uint32_t* idx, long n, double 
   if (n <= 0) return SF21_OK;
   int rc = ensure_cat(c, c->cat_n + n);
   if (rc) return rc;
-  HCTX_CUDA(c, launch_hf_records(idx, n, c->logN, (float)M, c->d_cat + c->cat_n, c->stream));
+  HCTX_CUDA(c, launch_hf_records(idx, n, (int)c->N, (float)M, c->d_cat + c->cat_n, c->stream));
   c->cat_n += n;
   return SF21_OK;
 }
@@ -776,7 +795,7 @@ static int greedy_mass(sf21_halo_ctx* c, const MassPlan& mp, const uint32_t* can
   const int4* runs = c->d_runs + mp.runs_off;
   const int nruns = (int)mp.runs.size();
   HCTX_CUDA(c, cudaMemsetAsync(c->d_cnt + 1, 0, sizeof(uint32_t), st));
-  HCTX_CUDA(c, launch_hf_prefilter(c->d_list, c->d_cnt, c->logN, runs, nruns, c->d_FL, c->d_UND, c->d_status,
+  HCTX_CUDA(c, launch_hf_prefilter(c->d_list, c->d_cnt, (int)c->N, runs, nruns, c->d_FL, c->d_UND, c->d_status,
                                    c->d_cnt + 1, st));
   if ((rc = read_counts(c))) return rc;
   long und = c->h_cnt[1];
@@ -786,16 +805,16 @@ static int greedy_mass(sf21_halo_ctx* c, const MassPlan& mp, const uint32_t* can
     int rounds = 0;
     while (und > 0 && rounds < kMaxRounds) {
       for (int k = 0; k < 4; ++k)
-        HCTX_CUDA(c, launch_hf_round(c->d_list, c->d_cnt, c->logN, druns, nd, c->d_UND, c->d_ACC, c->d_status,
+        HCTX_CUDA(c, launch_hf_round(c->d_list, c->d_cnt, (int)c->N, druns, nd, c->d_UND, c->d_ACC, c->d_status,
                                      c->d_cnt + 1, st));
       rounds += 4;
       if ((rc = read_counts(c))) return rc;
       und = c->h_cnt[1];
     }
   }
-  HCTX_CUDA(c, launch_hf_flag_accepted(c->d_list, c->d_cnt, c->logN, runs, nruns, c->d_FL, c->d_status, st));
+  HCTX_CUDA(c, launch_hf_flag_accepted(c->d_list, c->d_cnt, (int)c->N, runs, nruns, c->d_FL, c->d_status, st));
   if (und > 0)
-    HCTX_CUDA(c, launch_hf_finisher(c->d_list, c->d_cnt, c->logN, runs, nruns, c->d_FL, c->d_ACC, c->d_status, st));
+    HCTX_CUDA(c, launch_hf_finisher(c->d_list, c->d_cnt, (int)c->N, runs, nruns, c->d_FL, c->d_ACC, c->d_status, st));
   long na = 0;
   if ((rc = compact_bits(c, c->d_ACC, 2, &na))) return rc;
   if ((rc = append_records(c, c->d_list2, na, mp.m.M))) return rc;
@@ -979,7 +998,7 @@ static int subgrid_cycle(sf21_halo_ctx* c, const Cosmo& cs, double z, double gro
         if ((rc = read_counts(c))) return rc;
         recs = c->h_cnt[3];
         if ((rc = ensure_cat(c, c->cat_n + recs))) return rc;
-        HCTX_CUDA(c, launch_sg_records(c->d_sg_cell, c->d_sg_nn, off, nd, c->logN, (float)M, c->d_cat + c->cat_n,
+        HCTX_CUDA(c, launch_sg_records(c->d_sg_cell, c->d_sg_nn, off, nd, (int)c->N, (float)M, c->d_cat + c->cat_n,
                                        (uint64_t)(c->cat_cap - c->cat_n), c->d_sg_err, st));
         c->cat_n += recs;
       }
@@ -1028,9 +1047,15 @@ static int run_filter_bank(sf21_halo_ctx* c, const std::vector<MassPlan>& plan, 
       ++hb.K;
     }
     bt.K = hb.K;
-    HCTX_CUDA(c, launch_hf_rows_filter_cb(N, c->d_spec, hb, c->d_tw, st));
-    HCTX_CUDA(c, launch_cols_b_cb(N, bt, c->d_tw, st));
-    HCTX_CUDA(c, launch_hf_cols_a_thresh_cb(N, hb, c->d_tw, st));
+    if (c->gen) {
+      HCTX_CUDA(c, launch_gen_hf_rows_filter(c->gp, c->d_spec, hb, c->d_tw, st));
+      HCTX_CUDA(c, launch_gen_hf_cols(c->gp, hb, 1, false, c->d_tw, st));
+      HCTX_CUDA(c, launch_gen_hf_cols(c->gp, hb, 0, true, c->d_tw, st));
+    } else {
+      HCTX_CUDA(c, launch_hf_rows_filter_cb(N, c->d_spec, hb, c->d_tw, st));
+      HCTX_CUDA(c, launch_cols_b_cb(N, bt, c->d_tw, st));
+      HCTX_CUDA(c, launch_hf_cols_a_thresh_cb(N, hb, c->d_tw, st));
+    }
   }
   return SF21_OK;
 }
@@ -1189,9 +1214,15 @@ extern "C" int sf21_halo_field(sf21_halo_ctx* c, double z, int m, float* out) {
   bt.r[0].work = c->d_work;
   Batch none;
   memset(&none, 0, sizeof(none));
-  HCTX_CUDA(c, launch_hf_rows_filter(N, c->d_spec, hb, c->d_tw, st));
-  HCTX_CUDA(c, launch_cols(N, nullptr, bt, 1, 1, true, c->d_tw, st));
-  HCTX_CUDA(c, launch_cols(N, c->d_work, none, 1, 0, true, c->d_tw, st));
+  if (c->gen) {
+    HCTX_CUDA(c, launch_gen_hf_rows_filter(c->gp, c->d_spec, hb, c->d_tw, st));
+    HCTX_CUDA(c, launch_gen_cols(c->gp, c->d_work, none, 1, true, c->d_tw, st));
+    HCTX_CUDA(c, launch_gen_cols(c->gp, c->d_work, none, 0, true, c->d_tw, st));
+  } else {
+    HCTX_CUDA(c, launch_hf_rows_filter(N, c->d_spec, hb, c->d_tw, st));
+    HCTX_CUDA(c, launch_cols(N, nullptr, bt, 1, 1, true, c->d_tw, st));
+    HCTX_CUDA(c, launch_cols(N, c->d_work, none, 1, 0, true, c->d_tw, st));
+  }
   std::vector<float2> h(c->n3);
   HCTX_CUDA(c, cudaMemcpyAsync(h.data(), c->d_work, sizeof(float2) * c->n3, cudaMemcpyDeviceToHost, st));
   HCTX_CUDA(c, cudaStreamSynchronize(st));

@@ -69,6 +69,8 @@ constexpr int NPATH = 7;
 
 struct sf21_hii_ctx {
   int device = 0;
+  bool gen = false;  // side not a power of two: shared-memory transforms (kernels_gen.cu), pipeline 1 only
+  GenPlan gp = {};
   long N = 0, N_halo = 0, n3 = 0;
   double L = 0, hubble = 0, dx = 0, dk = 0;
   int K = 8;
@@ -355,8 +357,10 @@ extern "C" int sf21_hii_create(const sf21_hii_config* cfg, sf21_hii_ctx** out) {
     return SF21_E_ARG;
   }
   const long N = cfg->N;
-  if (N < 16 || N > 1024 || (N & (N - 1))) {
-    g_create_err = "N_smoothed must be a power of two between 16 and 1024";
+  const bool pow2 = N >= 16 && N <= 1024 && !(N & (N - 1));
+  if (!pow2 && !gen_supported((int)N)) {
+    g_create_err = "N_smoothed must be a power of two between 16 and 1024, or a product of 2, 3 and 5 that 8 divides, "
+                   "from 24 to 1280";
     return SF21_E_UNSUPPORTED;
   }
   if (!(cfg->L > 0) || !(cfg->hubble > 0)) {
@@ -406,10 +410,16 @@ extern "C" int sf21_hii_create(const sf21_hii_config* cfg, sf21_hii_ctx** out) {
   } while (0)
   CREATE_CUDA(cudaSetDevice(c->device));
   CREATE_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
-  CREATE_CUDA(fft_setup((int)N));
+  c->gen = !pow2;
+  if (c->gen) {
+    c->gp = gen_plan((int)N);
+    CREATE_CUDA(gen_setup((int)N));
+  } else {
+    CREATE_CUDA(fft_setup((int)N));
+    CREATE_CUDA(cb_setup((int)N));
+    CREATE_CUDA(adj_setup((int)N));
+  }
   CREATE_CUDA(dt_setup((int)N));
-  CREATE_CUDA(cb_setup((int)N));
-  CREATE_CUDA(adj_setup((int)N));
   CREATE_CUDA(cudaMalloc(&c->d_delta, box_f));
   CREATE_CUDA(cudaMalloc(&c->d_src, box_f));
   CREATE_CUDA(cudaMalloc(&c->d_rec0, box_f));
@@ -428,9 +438,15 @@ extern "C" int sf21_hii_create(const sf21_hii_config* cfg, sf21_hii_ctx** out) {
   c->pro_blocks = prologue_blocks(c->n3);
   CREATE_CUDA(cudaMalloc(&c->d_partials, sizeof(float) * 2 * c->pro_blocks));
   CREATE_CUDA(cudaMalloc(&c->d_alpha, sizeof(float)));
-  // twiddles exp(-2 pi i t / N) in double, rounded once
+  // twiddles exp(-2 pi i t / N) in double, rounded once (stage layout for the
+  // register transforms, plain table for the shared-memory ones)
   std::vector<float2> tw(N);
-  {
+  if (c->gen) {
+    for (long t = 0; t < N; ++t) {
+      const double ang = -2.0 * kPI * t / N;
+      tw[t] = make_float2((float)cos(ang), (float)sin(ang));
+    }
+  } else {
     std::vector<double> tre(N), tim(N);
     twiddle_layout((int)N, tre.data(), tim.data());
     for (long t = 0; t < N; ++t) tw[t] = make_float2((float)tre[t], (float)tim[t]);
@@ -442,16 +458,16 @@ extern "C" int sf21_hii_create(const sf21_hii_config* cfg, sf21_hii_ctx** out) {
     CREATE_CUDA(cudaMemcpy(s.d_nmax, s.nmax.data(), sizeof(int) * s.nmax.size(), cudaMemcpyHostToDevice));
   }
   // path: explicit, or tuned by timing one K-radius batch of each variant
-  const bool can_plane = plane_supported((int)N) && plane_setup((int)N) == cudaSuccess &&
+  const bool can_plane = !c->gen && plane_supported((int)N) && plane_setup((int)N) == cudaSuccess &&
                          plane_max_active_clusters((int)N) > 0;
   bool can_pipe = false;
-  if (pipe_supported((int)N) && pipe_setup((int)N) == cudaSuccess &&
+  if (!c->gen && pipe_supported((int)N) && pipe_setup((int)N) == cudaSuccess &&
       pipe_make_maps((int)N, &c->pmaps, K, c->d_work_base) == cudaSuccess)
     can_pipe = true;
   cudaGetLastError();
   const int want = cfg->path;
   if ((want == 2 && !can_plane) || ((want == 3 || want == 4 || want == 6 || want == 7) && !can_pipe) ||
-      want < 0 || want > NPATH) {
+      (c->gen && want > 1) || want < 0 || want > NPATH) {
     g_create_err = "requested radius pipeline not available for this box on this device";
     free_ctx(c);
     return SF21_E_UNSUPPORTED;
@@ -540,6 +556,31 @@ extern "C" int sf21_hii_radii(const sf21_hii_ctx* ctx, int set, double* R, int c
   return (int)s.R.size();
 }
 
+// ---- transform passes: register kernels (power-of-two sides) or shared-memory
+// kernels (other sides), same arguments ------------------------------------
+static cudaError_t x_fwd_rows(sf21_hii_ctx* c, const float2* in, float2* out, const float* alpha, cudaStream_t st) {
+  return c->gen ? launch_gen_fwd_rows(c->gp, in, out, alpha, c->d_tw, st)
+                : launch_fwd_rows((int)c->N, in, out, alpha, c->d_tw, st);
+}
+static cudaError_t x_inv_rows_plain(sf21_hii_ctx* c, float2* box, cudaStream_t st) {
+  return c->gen ? launch_gen_inv_rows_plain(c->gp, box, c->d_tw, st) : launch_inv_rows_plain((int)c->N, box, c->d_tw, st);
+}
+static cudaError_t x_inv_rows_filter(sf21_hii_ctx* c, const float2* spec, const Batch& bt, cudaStream_t st) {
+  return c->gen ? launch_gen_inv_rows_filter(c->gp, spec, bt, c->d_tw, st)
+                : launch_inv_rows_filter((int)c->N, spec, bt, c->d_tw, st);
+}
+// box, or (box null) the batch's nbox = bt.K boxes
+static cudaError_t x_cols(sf21_hii_ctx* c, float2* box, const Batch& bt, int nbox, int axis, bool inverse,
+                          cudaStream_t st) {
+  if (!c->gen) return launch_cols((int)c->N, box, bt, nbox, axis, inverse, c->d_tw, st);
+  if (!box && nbox != bt.K) return cudaErrorInvalidValue;
+  return launch_gen_cols(c->gp, box, bt, axis, inverse, c->d_tw, st);
+}
+static cudaError_t x_cols_a_test(sf21_hii_ctx* c, const Batch& bt, cudaStream_t st) {
+  return c->gen ? launch_gen_cols_a_test(c->gp, bt, c->d_rc, c->d_alpha, c->d_tw, st)
+                : launch_cols_a_test((int)c->N, bt, c->d_rc, c->d_alpha, c->d_tw, st);
+}
+
 // ---- schedule pieces --------------------------------------------------------
 static int enqueue_front(sf21_hii_ctx* c, double z, int kind, const float* delta, const float* src,
                          cudaStream_t st) {
@@ -555,11 +596,11 @@ static int enqueue_front(sf21_hii_ctx* c, double z, int kind, const float* delta
   int e1 = mark(c, st);
   CTX_CUDA(c, launch_alpha(c->d_partials, c->pro_blocks, c->d_alpha, st));
   int e2 = mark(c, st);
-  CTX_CUDA(c, launch_fwd_rows(N, packed, c->d_spec, c->d_alpha, c->d_tw, st));
+  CTX_CUDA(c, x_fwd_rows(c, packed, c->d_spec, c->d_alpha, st));
   int e3 = mark(c, st);
-  CTX_CUDA(c, launch_cols(N, c->d_spec, none, 1, 1, false, c->d_tw, st));
+  CTX_CUDA(c, x_cols(c, c->d_spec, none, 1, 1, false, st));
   int e4 = mark(c, st);
-  CTX_CUDA(c, launch_cols(N, c->d_spec, none, 1, 0, false, c->d_tw, st));
+  CTX_CUDA(c, x_cols(c, c->d_spec, none, 1, 0, false, st));
   int e5 = mark(c, st);
   CTX_CUDA(c, launch_finish_prep(c->n3, src, c->d_fres, c->pa, c->d_chain, c->d_om, st));
   int e6 = mark(c, st);
@@ -579,7 +620,7 @@ static int enqueue_batch(sf21_hii_ctx* c, const Batch& bt, cudaStream_t st) {
     int e0 = mark(c, st);
     CTX_CUDA(c, launch_plane_filter(N, c->d_spec, bt, c->d_tw, st));
     int e1 = mark(c, st);
-    CTX_CUDA(c, launch_cols_a_test(N, bt, c->d_rc, c->d_alpha, c->d_tw, st));
+    CTX_CUDA(c, x_cols_a_test(c, bt, st));
     int e2 = mark(c, st);
     span(c, KD_PLANE, e0, e1);
     span(c, KD_ICA, e1, e2);
@@ -608,7 +649,7 @@ static int enqueue_batch(sf21_hii_ctx* c, const Batch& bt, cudaStream_t st) {
   }
   if (c->path == 3 || c->path == 4) {
     int e0 = mark(c, st);
-    CTX_CUDA(c, launch_inv_rows_filter(N, c->d_spec, bt, c->d_tw, st));
+    CTX_CUDA(c, x_inv_rows_filter(c, c->d_spec, bt, st));
     int e1 = mark(c, st);
     CTX_CUDA(c, launch_pipe(N, 0, 0, c->pmaps, bt, c->d_work_base, c->d_rc, c->d_alpha, c->d_tw, c->d_err, c->nsm,
                             st));
@@ -617,7 +658,7 @@ static int enqueue_batch(sf21_hii_ctx* c, const Batch& bt, cudaStream_t st) {
       CTX_CUDA(c, launch_pipe(N, 1, 0, c->pmaps, bt, c->d_work_base, c->d_rc, c->d_alpha, c->d_tw, c->d_err,
                               c->nsm, st));
     else
-      CTX_CUDA(c, launch_cols_a_test(N, bt, c->d_rc, c->d_alpha, c->d_tw, st));
+      CTX_CUDA(c, x_cols_a_test(c, bt, st));
     int e3 = mark(c, st);
     span(c, KD_IROWS, e0, e1);
     span(c, KD_ICB, e1, e2);
@@ -625,11 +666,11 @@ static int enqueue_batch(sf21_hii_ctx* c, const Batch& bt, cudaStream_t st) {
     return SF21_OK;
   }
   int e0 = mark(c, st);
-  CTX_CUDA(c, launch_inv_rows_filter(N, c->d_spec, bt, c->d_tw, st));
+  CTX_CUDA(c, x_inv_rows_filter(c, c->d_spec, bt, st));
   int e1 = mark(c, st);
-  CTX_CUDA(c, launch_cols(N, nullptr, bt, bt.K, 1, true, c->d_tw, st));
+  CTX_CUDA(c, x_cols(c, nullptr, bt, bt.K, 1, true, st));
   int e2 = mark(c, st);
-  CTX_CUDA(c, launch_cols_a_test(N, bt, c->d_rc, c->d_alpha, c->d_tw, st));
+  CTX_CUDA(c, x_cols_a_test(c, bt, st));
   int e3 = mark(c, st);
   span(c, KD_IROWS, e0, e1);
   span(c, KD_ICB, e1, e2);
@@ -873,9 +914,9 @@ extern "C" int sf21_hii_filtered(sf21_hii_ctx* c, double z, int kind, const floa
   bt.r[0].ridx = ridx;
   bt.r[0].work = c->d_work[0];
   const int N = (int)c->N;
-  CTX_CUDA(c, launch_inv_rows_filter(N, c->d_spec, bt, c->d_tw, c->stream));
-  CTX_CUDA(c, launch_cols(N, c->d_work[0], bt, 1, 1, true, c->d_tw, c->stream));
-  CTX_CUDA(c, launch_cols(N, c->d_work[0], bt, 1, 0, true, c->d_tw, c->stream));
+  CTX_CUDA(c, x_inv_rows_filter(c, c->d_spec, bt, c->stream));
+  CTX_CUDA(c, x_cols(c, c->d_work[0], bt, 1, 1, true, c->stream));
+  CTX_CUDA(c, x_cols(c, c->d_work[0], bt, 1, 0, true, c->stream));
   std::vector<float2> box(c->n3);
   float alpha = 1.f;
   CTX_CUDA(c, cudaMemcpyAsync(box.data(), c->d_work[0], sizeof(float2) * c->n3, cudaMemcpyDeviceToHost, c->stream));
@@ -965,21 +1006,21 @@ extern "C" int sf21_hii_run_z_plain_device(sf21_hii_ctx* c, double z, int kind, 
     bt.r[0].ridx = i;
     bt.r[0].work = box;
     // filtered fields (:305-325)
-    CTX_CUDA(c, launch_inv_rows_filter(N, c->d_spec, bt, c->d_tw, st));
-    CTX_CUDA(c, launch_cols(N, box, none, 1, 1, true, c->d_tw, st));
-    CTX_CUDA(c, launch_cols(N, box, none, 1, 0, true, c->d_tw, st));
+    CTX_CUDA(c, x_inv_rows_filter(c, c->d_spec, bt, st));
+    CTX_CUDA(c, x_cols(c, box, none, 1, 1, true, st));
+    CTX_CUDA(c, x_cols(c, box, none, 1, 0, true, st));
     CTX_CUDA(c, cudaMemsetAsync(c->d_flag, 0, sizeof(int), st));
     CTX_CUDA(c, launch_plain_centres(n3, box, c->d_alpha, (float)s.fesc, c->d_mask, c->d_flag, st));
     if (i < s.n_fft) {
       // FFT convolution with the discrete sphere (:358-393)
       CTX_CUDA(c, launch_plain_pack_sphere(N, s.nmax[i], c->d_mask, c->d_flag, c->d_box2, st));
-      CTX_CUDA(c, launch_fwd_rows(N, c->d_box2, c->d_box2, nullptr, c->d_tw, st));
-      CTX_CUDA(c, launch_cols(N, c->d_box2, none, 1, 1, false, c->d_tw, st));
-      CTX_CUDA(c, launch_cols(N, c->d_box2, none, 1, 0, false, c->d_tw, st));
+      CTX_CUDA(c, x_fwd_rows(c, c->d_box2, c->d_box2, nullptr, st));
+      CTX_CUDA(c, x_cols(c, c->d_box2, none, 1, 1, false, st));
+      CTX_CUDA(c, x_cols(c, c->d_box2, none, 1, 0, false, st));
       CTX_CUDA(c, launch_plain_product(N, c->d_box2, c->d_flag, box, st));
-      CTX_CUDA(c, launch_inv_rows_plain(N, box, c->d_tw, st));
-      CTX_CUDA(c, launch_cols(N, box, none, 1, 1, true, c->d_tw, st));
-      CTX_CUDA(c, launch_cols(N, box, none, 1, 0, true, c->d_tw, st));
+      CTX_CUDA(c, x_inv_rows_plain(c, box, st));
+      CTX_CUDA(c, x_cols(c, box, none, 1, 1, true, st));
+      CTX_CUDA(c, x_cols(c, box, none, 1, 0, true, st));
       CTX_CUDA(c, launch_plain_threshold(n3, box, c->d_flag, xhii_dev, st));
     } else {
       // ball painting (:427-458)
@@ -1017,6 +1058,7 @@ extern "C" int sf21_hii_check(sf21_hii_ctx* c) {
 
 // ---- criterion C(x) = max_R ion_R / rec_R and its vector-Jacobian product ----
 static int ensure_adj_buffers(sf21_hii_ctx* c) {
+  if (c->gen) CTX_FAIL(c, SF21_E_UNSUPPORTED, "the criterion and its adjoint need a power-of-two box side");
   const long n3 = c->n3;
   if (!c->d_C) CTX_CUDA(c, cudaMalloc(&c->d_C, sizeof(float) * n3));
   if (!c->d_A) CTX_CUDA(c, cudaMalloc(&c->d_A, n3));
@@ -1032,9 +1074,9 @@ static int enqueue_recompute(sf21_hii_ctx* c, const Batch& bt, cudaStream_t st) 
     span(c, KD_PLANE, e0, mark(c, st));
   } else {
     int e0 = mark(c, st);
-    CTX_CUDA(c, launch_inv_rows_filter(N, c->d_spec, bt, c->d_tw, st));
+    CTX_CUDA(c, x_inv_rows_filter(c, c->d_spec, bt, st));
     int e1 = mark(c, st);
-    CTX_CUDA(c, launch_cols(N, nullptr, bt, bt.K, 1, true, c->d_tw, st));
+    CTX_CUDA(c, x_cols(c, nullptr, bt, bt.K, 1, true, st));
     span(c, KD_IROWS, e0, e1);
     span(c, KD_ICB, e1, mark(c, st));
   }
@@ -1113,7 +1155,7 @@ extern "C" int sf21_hii_vjp_device(sf21_hii_ctx* c, double z, int kind, const fl
     int e0 = mark(c, st);
     CTX_CUDA(c, launch_cols_a_adj(N, bt, dC_dev, c->d_A, c->d_alpha, c->d_zpart, c->d_tw, st));
     int e1 = mark(c, st);
-    CTX_CUDA(c, launch_cols(N, nullptr, bt, bt.K, 1, false, c->d_tw, st));
+    CTX_CUDA(c, x_cols(c, nullptr, bt, bt.K, 1, false, st));
     int e2 = mark(c, st);
     CTX_CUDA(c, launch_rows_adj_acc(N, bt, c->d_acc, c->d_tw, st));
     int e3 = mark(c, st);
@@ -1123,9 +1165,9 @@ extern "C" int sf21_hii_vjp_device(sf21_hii_ctx* c, double z, int kind, const fl
   }
   // back to real space: sum_R B_R (cotangents)
   int f0 = mark(c, st);
-  CTX_CUDA(c, launch_inv_rows_plain(N, c->d_acc, c->d_tw, st));
-  CTX_CUDA(c, launch_cols(N, c->d_acc, none, 1, 1, true, c->d_tw, st));
-  CTX_CUDA(c, launch_cols(N, c->d_acc, none, 1, 0, true, c->d_tw, st));
+  CTX_CUDA(c, x_inv_rows_plain(c, c->d_acc, st));
+  CTX_CUDA(c, x_cols(c, c->d_acc, none, 1, 1, true, st));
+  CTX_CUDA(c, x_cols(c, c->d_acc, none, 1, 0, true, st));
   double mul = 1.0;
   for (int m = 0; m < c->pa.n_src_mul; ++m) {
     double v;
@@ -1267,9 +1309,9 @@ static int power_spectrum_device(sf21_hii_ctx* c, const float* box_dev, int flag
   memset(&none, 0, sizeof(none));
   CTX_CUDA(c, cudaMemcpyAsync(c->d_pk_w, wax.data(), sizeof(float) * N, cudaMemcpyHostToDevice, st));
   CTX_CUDA(c, launch_pk_pack(N, box_dev, c->d_pk_w, packed, st));
-  CTX_CUDA(c, launch_fwd_rows(N, packed, c->d_pk, nullptr, c->d_tw, st));
-  CTX_CUDA(c, launch_cols(N, c->d_pk, none, 1, 1, false, c->d_tw, st));
-  CTX_CUDA(c, launch_cols(N, c->d_pk, none, 1, 0, false, c->d_tw, st));
+  CTX_CUDA(c, x_fwd_rows(c, packed, c->d_pk, nullptr, st));
+  CTX_CUDA(c, x_cols(c, c->d_pk, none, 1, 1, false, st));
+  CTX_CUDA(c, x_cols(c, c->d_pk, none, 1, 0, false, st));
   CTX_CUDA(c, cudaMemsetAsync(c->d_pk_cnt, 0, sizeof(unsigned long long) * nk, st));
   CTX_CUDA(c, launch_pk_bin(N, c->d_pk, nk, c->d_pk_part, c->d_pk_cnt, st));
   std::vector<float> part((size_t)grid * nk);
@@ -1377,13 +1419,13 @@ extern "C" int sf21_t21_run_z(sf21_hii_ctx* c, const sf21_t21_cosmo* cosmo, doub
   memset(&none, 0, sizeof(none));
   float2* packed = c->d_work[0];
   CTX_CUDA(c, launch_t21_pack(n3, c->d_delta, packed, st));
-  CTX_CUDA(c, launch_fwd_rows(N, packed, c->d_pk, nullptr, c->d_tw, st));
-  CTX_CUDA(c, launch_cols(N, c->d_pk, none, 1, 1, false, c->d_tw, st));
-  CTX_CUDA(c, launch_cols(N, c->d_pk, none, 1, 0, false, c->d_tw, st));
+  CTX_CUDA(c, x_fwd_rows(c, packed, c->d_pk, nullptr, st));
+  CTX_CUDA(c, x_cols(c, c->d_pk, none, 1, 1, false, st));
+  CTX_CUDA(c, x_cols(c, c->d_pk, none, 1, 0, false, st));
   CTX_CUDA(c, launch_t21_kfilter(N, cosmo->vel_comp, c->d_pk, st));
-  CTX_CUDA(c, launch_inv_rows_plain(N, c->d_pk, c->d_tw, st));
-  CTX_CUDA(c, launch_cols(N, c->d_pk, none, 1, 1, true, c->d_tw, st));
-  CTX_CUDA(c, launch_cols(N, c->d_pk, none, 1, 0, true, c->d_tw, st));
+  CTX_CUDA(c, x_inv_rows_plain(c, c->d_pk, st));
+  CTX_CUDA(c, x_cols(c, c->d_pk, none, 1, 1, true, st));
+  CTX_CUDA(c, x_cols(c, c->d_pk, none, 1, 0, true, st));
   CTX_CUDA(c, launch_t21_finish(n3, c->d_pk, c->d_delta, c->d_xhii, spin ? d_xc : nullptr, spin ? d_xa : nullptr,
                                 spin ? d_tk : nullptr, ta, d_tb, c->d_t21_part, st));
   std::vector<float> part(2 * (size_t)nb);

@@ -17,10 +17,11 @@
 // strip slide by one element per step, so they are kept in registers as two
 // 8-element chunks on each side and refilled 8 elements at a time; every
 // (output, distance) pair then costs one max and one fused add-max
-// (__viaddmax_s32).  Chunks are 8-aligned, so periodic wrap never splits one.
+// (__viaddmax_s32).  Chunks are 8-aligned and N is a multiple of 8, so
+// periodic wrap never splits one.
 //
 // Data layout of the two intermediates (int per voxel):
-//   I1 (after the a pass): column-block major with nc = min(32, N) columns,
+//   I1 (after the a pass): column-block major with nc = dt_cols(N) columns,
 //     ((c/nc N + b) N + a) nc + c%nc,
 //     so that an a-pass tile (fixed b, 32 columns) writes one contiguous run
 //     and a b-pass tile (fixed a) reads runs of 128 bytes inside one slab;
@@ -56,12 +57,18 @@ __device__ __forceinline__ int dt_blocks(int vmax, int N) {
 // Strip of 8 outputs y0..y0+7 (y0 multiple of 8) of one periodic line of
 // length N; ld8(p, dst) loads the 8 elements p..p+7 (p multiple of 8, taken
 // mod N by the caller's accessor).
+// periodic index of a chunk start (N a multiple of 8: chunks never split)
+__device__ __forceinline__ int dt_wrap(int x, int N) {
+  x %= N;
+  return x < 0 ? x + N : x;
+}
+
 template <class LD8>
 __device__ __forceinline__ void dt_strip(const LD8& ld8, int y0, int nblk, int N, int (&acc)[8]) {
   int A[8], B[8], C[8], D[8];
   ld8(y0, A);
-  ld8((y0 + 8) & (N - 1), B);
-  ld8((y0 - 8) & (N - 1), C);
+  ld8(dt_wrap(y0 + 8, N), B);
+  ld8(dt_wrap(y0 - 8, N), C);
 #pragma unroll
   for (int r = 0; r < 8; ++r) {
     acc[r] = A[r];
@@ -87,15 +94,18 @@ __device__ __forceinline__ void dt_strip(const LD8& ld8, int y0, int nblk, int N
         A[r] = B[r];
         D[r] = C[r];
       }
-      ld8((y0 + 8 * m + 16) & (N - 1), B);
-      ld8((y0 - 8 * m - 16) & (N - 1), C);
+      ld8(dt_wrap(y0 + 8 * m + 16, N), B);
+      ld8(dt_wrap(y0 - 8 * m - 16, N), C);
     }
   }
 #pragma unroll
   for (int r = 0; r < 8; ++r) acc[r] = acc[r] < -1 ? -1 : acc[r];
 }
 
-__host__ __device__ __forceinline__ int dt_cols(int N) { return N < DT_COLS ? N : DT_COLS; }
+// columns of a column tile: the largest of 32, 16, 8 that divides N (N if N < 32)
+__host__ __device__ __forceinline__ int dt_cols(int N) {
+  return N < DT_COLS ? N : (N % 32 == 0 ? 32 : (N % 16 == 0 ? 16 : 8));
+}
 
 // Column tile: N lines of the pass axis x nc columns in shared memory,
 // s[pos * (nc + 1) + col]; one warp = the 32 columns of one strip.
@@ -286,10 +296,12 @@ cudaError_t dt_setup(int N) {
   return cudaFuncSetAttribute(k_dt_pc_finish<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, row_tile);
 }
 
-// at least one full warp (the block reduction shuffles over all 32 lanes)
+// whole warps (the block reduction shuffles over all 32 lanes of every warp;
+// threads past the last strip only load and reduce)
 static int dt_threads(int N) {
-  const int t = N * dt_cols(N) / 8;
-  return t < 32 ? 32 : (t < DT_THREADS ? t : DT_THREADS);
+  int t = N * dt_cols(N) / 8;
+  t = (t + 31) / 32 * 32;
+  return t < DT_THREADS ? t : DT_THREADS;
 }
 static size_t dt_col_smem(int N) { return (size_t)N * (dt_cols(N) + 1) * sizeof(int); }
 static unsigned dt_col_grid(int N) { return (unsigned)((long)(N / dt_cols(N)) * N); }
@@ -308,8 +320,8 @@ cudaError_t launch_dt_pb(int N, const int* i1, int* i2, cudaStream_t st) {
 
 cudaError_t launch_dt_pc_finish(int N, const int* i2, uint64_t zeta, const uint64_t* chain, const float* rec0,
                                 const float2* om, float* xhii, cudaStream_t st) {
-  int thr = DT_ROWS * N / 8;
-  thr = thr < 32 ? 32 : (thr < DT_THREADS ? thr : DT_THREADS);
+  int thr = (DT_ROWS * N / 8 + 31) / 32 * 32;  // whole warps, as dt_threads
+  thr = thr < DT_THREADS ? thr : DT_THREADS;
   const unsigned grid = (unsigned)((long)N * N / DT_ROWS);
   const size_t smem = (size_t)DT_ROWS * N * sizeof(int);
   if (((uintptr_t)xhii & 15) == 0)

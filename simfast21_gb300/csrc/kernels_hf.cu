@@ -372,12 +372,12 @@ __device__ __forceinline__ int wrapi(int x, int N) { return x < 0 ? x + N : (x >
 struct Cell {
   int i, j, p;
 };
-__device__ __forceinline__ Cell decode(uint32_t u, int logN) {
-  const int N = 1 << logN;
+__device__ __forceinline__ Cell decode(uint32_t u, int N) {
   Cell c;
-  c.p = (int)(u & (N - 1));
-  c.j = (int)((u >> logN) & (N - 1));
-  c.i = (int)(u >> (2 * logN));
+  const uint32_t q = u / (uint32_t)N;
+  c.p = (int)(u - q * (uint32_t)N);
+  c.i = (int)(q / (uint32_t)N);
+  c.j = (int)(q - (uint32_t)c.i * (uint32_t)N);
   return c;
 }
 
@@ -519,14 +519,14 @@ __device__ __forceinline__ long warp_id_global() { return ((long)blockIdx.x * bl
 __device__ __forceinline__ long warps_total() { return ((long)gridDim.x * blockDim.x) >> 5; }
 
 __global__ void __launch_bounds__(GL_THREADS)
-k_hf_prefilter(const uint32_t* __restrict__ list, const uint32_t* __restrict__ n_ptr, int logN,
+k_hf_prefilter(const uint32_t* __restrict__ list, const uint32_t* __restrict__ n_ptr, int N,
                const int4* __restrict__ runs, int nruns, const uint32_t* __restrict__ FL, uint32_t* __restrict__ UND,
                uint8_t* __restrict__ status, uint32_t* __restrict__ n_und) {
   const long n = *n_ptr;
-  const int N = 1 << logN, lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31;
   for (long c = warp_id_global(); c < n; c += warps_total()) {
     const uint32_t u = list[c];
-    const Cell cl = decode(u, logN);
+    const Cell cl = decode(u, N);
     bool hit = false;
     for (int r0 = 0; r0 < nruns && !hit; r0 += 32) {
       const int r = r0 + lane;
@@ -544,17 +544,17 @@ k_hf_prefilter(const uint32_t* __restrict__ list, const uint32_t* __restrict__ n
 }
 
 __global__ void __launch_bounds__(GL_THREADS)
-k_hf_round_decide(const uint32_t* __restrict__ list, const uint32_t* __restrict__ n_ptr, int logN,
+k_hf_round_decide(const uint32_t* __restrict__ list, const uint32_t* __restrict__ n_ptr, int N,
                   const int4* __restrict__ druns, int ndruns, const uint32_t* __restrict__ UND,
                   const uint32_t* __restrict__ ACC, uint8_t* __restrict__ status,
                   const uint32_t* __restrict__ n_und) {
   if (*n_und == 0) return;
   const long n = *n_ptr;
-  const int N = 1 << logN, lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31;
   for (long c = warp_id_global(); c < n; c += warps_total()) {
     if (status[c] != HF_UND) continue;
     const uint32_t u = list[c];
-    const Cell cl = decode(u, logN);
+    const Cell cl = decode(u, N);
     bool acc = false, earlier = false;
     for (int r0 = 0; r0 < ndruns && !acc; r0 += 32) {
       const int r = r0 + lane;
@@ -601,13 +601,13 @@ k_hf_round_apply(const uint32_t* __restrict__ list, const uint32_t* __restrict__
 
 // Flag the spheres of candidates accepted by the rounds (status HF_ACC).
 __global__ void __launch_bounds__(GL_THREADS)
-k_hf_flag_accepted(const uint32_t* __restrict__ list, const uint32_t* __restrict__ n_ptr, int logN,
+k_hf_flag_accepted(const uint32_t* __restrict__ list, const uint32_t* __restrict__ n_ptr, int N,
                    const int4* __restrict__ runs, int nruns, uint32_t* __restrict__ FL, uint8_t* __restrict__ status) {
   const long n = *n_ptr;
-  const int N = 1 << logN, lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31;
   for (long c = warp_id_global(); c < n; c += warps_total()) {
     if (status[c] != HF_ACC) continue;
-    const Cell cl = decode(list[c], logN);
+    const Cell cl = decode(list[c], N);
     for (int r = lane; r < nruns; r += 32) run_set(FL, N, cl, runs[r]);
     __syncwarp();
     if (lane == 0) status[c] = HF_ACC_FLAGGED;
@@ -618,11 +618,10 @@ k_hf_flag_accepted(const uint32_t* __restrict__ list, const uint32_t* __restrict
 // index order, on one CTA.
 constexpr int FIN_THREADS = 1024;
 __global__ void __launch_bounds__(FIN_THREADS)
-k_hf_finisher(const uint32_t* __restrict__ list, const uint32_t* __restrict__ n_ptr, int logN,
+k_hf_finisher(const uint32_t* __restrict__ list, const uint32_t* __restrict__ n_ptr, int N,
               const int4* __restrict__ runs, int nruns, uint32_t* __restrict__ FL, uint32_t* __restrict__ ACC,
               uint8_t* __restrict__ status) {
   const long n = *n_ptr;
-  const int N = 1 << logN;
   __shared__ uint32_t todo[FIN_THREADS];
   __shared__ int ntodo;
   __shared__ int wcnt[FIN_THREADS / 32];
@@ -649,7 +648,7 @@ k_hf_finisher(const uint32_t* __restrict__ list, const uint32_t* __restrict__ n_
     const int nt = ntodo;
     for (int k = 0; k < nt; ++k) {
       const long ck = c0 + todo[k];
-      const Cell cl = decode(list[ck], logN);
+      const Cell cl = decode(list[ck], N);
       bool h = false;
       for (int r = threadIdx.x; r < nruns && !h; r += FIN_THREADS) h = run_any(FL, N, cl, runs[r]);
       const int hit = __syncthreads_or(h);
@@ -708,36 +707,36 @@ __global__ void k_hf_cell(long nwords, const float* __restrict__ delta, float tc
 
 // Catalogue records {Mass, x, y, z} (Halo_t, auxiliary.h:13-17) of a sorted
 // cell list.
-__global__ void k_hf_records(const uint32_t* __restrict__ idx, long n, int logN, float mass,
+__global__ void k_hf_records(const uint32_t* __restrict__ idx, long n, int N, float mass,
                              float4* __restrict__ out) {
   for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
-    const Cell c = decode(idx[k], logN);
+    const Cell c = decode(idx[k], N);
     out[k] = make_float4(mass, (float)c.i, (float)c.j, (float)c.p);
   }
 }
 
-cudaError_t launch_hf_prefilter(const uint32_t* list, const uint32_t* n_ptr, int logN, const int4* runs, int nruns,
+cudaError_t launch_hf_prefilter(const uint32_t* list, const uint32_t* n_ptr, int N, const int4* runs, int nruns,
                                 const uint32_t* FL, uint32_t* UND, uint8_t* status, uint32_t* n_und,
                                 cudaStream_t st) {
-  k_hf_prefilter<<<gl_grid(), GL_THREADS, 0, st>>>(list, n_ptr, logN, runs, nruns, FL, UND, status, n_und);
+  k_hf_prefilter<<<gl_grid(), GL_THREADS, 0, st>>>(list, n_ptr, N, runs, nruns, FL, UND, status, n_und);
   return cudaGetLastError();
 }
-cudaError_t launch_hf_round(const uint32_t* list, const uint32_t* n_ptr, int logN, const int4* druns, int ndruns,
+cudaError_t launch_hf_round(const uint32_t* list, const uint32_t* n_ptr, int N, const int4* druns, int ndruns,
                             uint32_t* UND, uint32_t* ACC, uint8_t* status, uint32_t* n_und, cudaStream_t st) {
-  k_hf_round_decide<<<gl_grid(), GL_THREADS, 0, st>>>(list, n_ptr, logN, druns, ndruns, UND, ACC, status, n_und);
+  k_hf_round_decide<<<gl_grid(), GL_THREADS, 0, st>>>(list, n_ptr, N, druns, ndruns, UND, ACC, status, n_und);
   cudaError_t e = cudaGetLastError();
   if (e) return e;
   k_hf_round_apply<<<gl_grid(), GL_THREADS, 0, st>>>(list, n_ptr, UND, ACC, status, n_und);
   return cudaGetLastError();
 }
-cudaError_t launch_hf_flag_accepted(const uint32_t* list, const uint32_t* n_ptr, int logN, const int4* runs,
+cudaError_t launch_hf_flag_accepted(const uint32_t* list, const uint32_t* n_ptr, int N, const int4* runs,
                                     int nruns, uint32_t* FL, uint8_t* status, cudaStream_t st) {
-  k_hf_flag_accepted<<<gl_grid(), GL_THREADS, 0, st>>>(list, n_ptr, logN, runs, nruns, FL, status);
+  k_hf_flag_accepted<<<gl_grid(), GL_THREADS, 0, st>>>(list, n_ptr, N, runs, nruns, FL, status);
   return cudaGetLastError();
 }
-cudaError_t launch_hf_finisher(const uint32_t* list, const uint32_t* n_ptr, int logN, const int4* runs, int nruns,
+cudaError_t launch_hf_finisher(const uint32_t* list, const uint32_t* n_ptr, int N, const int4* runs, int nruns,
                                uint32_t* FL, uint32_t* ACC, uint8_t* status, cudaStream_t st) {
-  k_hf_finisher<<<1, FIN_THREADS, 0, st>>>(list, n_ptr, logN, runs, nruns, FL, ACC, status);
+  k_hf_finisher<<<1, FIN_THREADS, 0, st>>>(list, n_ptr, N, runs, nruns, FL, ACC, status);
   return cudaGetLastError();
 }
 cudaError_t launch_hf_clear(const uint32_t* list, const uint32_t* n_ptr, uint32_t* UND, uint32_t* ACC,
@@ -750,11 +749,11 @@ cudaError_t launch_hf_cell(long nwords, const float* delta, float tcell, uint32_
   k_hf_cell<<<gl_grid(), GL_THREADS, 0, st>>>(nwords, delta, tcell, FL, bits);
   return cudaGetLastError();
 }
-cudaError_t launch_hf_records(const uint32_t* idx, long n, int logN, float mass, float4* out, cudaStream_t st) {
+cudaError_t launch_hf_records(const uint32_t* idx, long n, int N, float mass, float4* out, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
   long b = (n + 255) / 256;
   if (b > 152 * 16) b = 152 * 16;
-  k_hf_records<<<(unsigned)b, 256, 0, st>>>(idx, n, logN, mass, out);
+  k_hf_records<<<(unsigned)b, 256, 0, st>>>(idx, n, N, mass, out);
   return cudaGetLastError();
 }
 

@@ -15,6 +15,12 @@ namespace sf21 {
 
 constexpr int EL_THREADS = 256;
 
+// periodic index for any side N
+__device__ __forceinline__ int pwrap(int x, int N) {
+  x %= N;
+  return x < 0 ? x + N : x;
+}
+
 static unsigned el_grid(long n) {
   long b = (n + EL_THREADS - 1) / EL_THREADS;
   return (unsigned)(b < 152 * 32 ? b : 152 * 32);
@@ -54,10 +60,9 @@ __global__ void k_plain_product(int N, const float2* __restrict__ Z, const int* 
                                 float2* __restrict__ P) {
   if (!*flag) return;
   const long n3 = (long)N * N * N;
-  const int m = N - 1;
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += (long)gridDim.x * blockDim.x) {
     const int a = (int)(i / ((long)N * N)), b = (int)((i / N) % N), c = (int)(i % N);
-    const long j = ((long)((N - a) & m) * N + ((N - b) & m)) * N + ((N - c) & m);
+    const long j = ((long)(a ? N - a : 0) * N + (b ? N - b : 0)) * N + (c ? N - c : 0);
     const float2 z = Z[i], w = Z[j];
     const float2 s = make_float2(0.5f * (z.x + w.x), 0.5f * (z.y - w.y));
     // (z - conj w) / (2i) = ((z.y + w.y) / 2, -(z.x - w.x) / 2)
@@ -80,7 +85,6 @@ __global__ void k_plain_threshold(long n3, const float2* __restrict__ conv, cons
 __global__ void k_plain_paint(int N, int nc, int nmax, const float* __restrict__ mask,
                               float* __restrict__ bubblef) {
   const long n3 = (long)N * N * N;
-  const int m = N - 1;
   const int w = nc + 1;
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += (long)gridDim.x * blockDim.x) {
     const int a = (int)(i / ((long)N * N)), b = (int)((i / N) % N), c = (int)(i % N);
@@ -89,7 +93,7 @@ __global__ void k_plain_paint(int N, int nc, int nmax, const float* __restrict__
       for (int db = -w; db <= w && !hit; ++db)
         for (int dc = -w; dc <= w && !hit; ++dc) {
           if (da * da + db * db + dc * dc > nmax) continue;
-          const long j = ((long)((a - da) & m) * N + ((b - db) & m)) * N + ((c - dc) & m);
+          const long j = ((long)pwrap(a - da, N) * N + pwrap(b - db, N)) * N + pwrap(c - dc, N);
           hit = mask[j] != 0.0f;
         }
     if (hit) bubblef[i] = 1.0f;

@@ -339,13 +339,12 @@ __global__ void k_sg_nn(const uint64_t* __restrict__ dn, const uint8_t* __restri
 }
 
 __global__ void k_sg_records(const uint32_t* __restrict__ cell, const uint32_t* __restrict__ nn,
-                             const uint32_t* __restrict__ off, long nd, int logN, float mass,
+                             const uint32_t* __restrict__ off, long nd, int N, float mass,
                              float4* __restrict__ out, uint64_t cap, int* __restrict__ err) {
-  const int N = 1 << logN;
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nd; i += (long)gridDim.x * blockDim.x) {
     const uint32_t t = cell[i];
-    const float4 rec = make_float4(mass, (float)(t >> (2 * logN)), (float)((t >> logN) & (N - 1)),
-                                   (float)(t & (N - 1)));
+    const uint32_t q = t / (uint32_t)N, a = q / (uint32_t)N;
+    const float4 rec = make_float4(mass, (float)a, (float)(q - a * (uint32_t)N), (float)(t - q * (uint32_t)N));
     const uint32_t o = off[i];
     for (uint32_t r = 0; r < nn[i]; ++r) {
       if ((uint64_t)o + r < cap)
@@ -486,10 +485,10 @@ cudaError_t launch_sg_nn(const uint64_t* dn, const uint8_t* dk, long nd, const u
   return cudaGetLastError();
 }
 
-cudaError_t launch_sg_records(const uint32_t* cell, const uint32_t* nn, const uint32_t* off, long nd, int logN,
+cudaError_t launch_sg_records(const uint32_t* cell, const uint32_t* nn, const uint32_t* off, long nd, int N,
                               float mass, float4* out, uint64_t cap, int* err, cudaStream_t st) {
   if (nd <= 0) return cudaSuccess;
-  k_sg_records<<<grid_for(nd, 256), 256, 0, st>>>(cell, nn, off, nd, logN, mass, out, cap, err);
+  k_sg_records<<<grid_for(nd, 256), 256, 0, st>>>(cell, nn, off, nd, N, mass, out, cap, err);
   return cudaGetLastError();
 }
 

@@ -169,19 +169,19 @@ cudaError_t launch_bits_count(const uint32_t* W, long nwords, uint32_t* cnt, cud
 cudaError_t launch_scan_counts(uint32_t* cnt, long n, uint32_t* tot, cudaStream_t st);
 cudaError_t launch_bits_emit(const uint32_t* W, long nwords, const uint32_t* off, uint32_t* out, cudaStream_t st);
 // runs: {di, dj, m, 0}: the cells (i+di, j+dj, p-m .. p+m) of a sphere (or of D)
-cudaError_t launch_hf_prefilter(const uint32_t* list, const uint32_t* n_ptr, int logN, const int4* runs, int nruns,
+cudaError_t launch_hf_prefilter(const uint32_t* list, const uint32_t* n_ptr, int N, const int4* runs, int nruns,
                                 const uint32_t* FL, uint32_t* UND, uint8_t* status, uint32_t* n_und, cudaStream_t st);
-cudaError_t launch_hf_round(const uint32_t* list, const uint32_t* n_ptr, int logN, const int4* druns, int ndruns,
+cudaError_t launch_hf_round(const uint32_t* list, const uint32_t* n_ptr, int N, const int4* druns, int ndruns,
                             uint32_t* UND, uint32_t* ACC, uint8_t* status, uint32_t* n_und, cudaStream_t st);
-cudaError_t launch_hf_flag_accepted(const uint32_t* list, const uint32_t* n_ptr, int logN, const int4* runs,
+cudaError_t launch_hf_flag_accepted(const uint32_t* list, const uint32_t* n_ptr, int N, const int4* runs,
                                     int nruns, uint32_t* FL, uint8_t* status, cudaStream_t st);
-cudaError_t launch_hf_finisher(const uint32_t* list, const uint32_t* n_ptr, int logN, const int4* runs, int nruns,
+cudaError_t launch_hf_finisher(const uint32_t* list, const uint32_t* n_ptr, int N, const int4* runs, int nruns,
                                uint32_t* FL, uint32_t* ACC, uint8_t* status, cudaStream_t st);
 cudaError_t launch_hf_clear(const uint32_t* list, const uint32_t* n_ptr, uint32_t* UND, uint32_t* ACC,
                             cudaStream_t st);
 cudaError_t launch_hf_cell(long nwords, const float* delta, float tcell, uint32_t* FL, uint32_t* bits,
                            cudaStream_t st);
-cudaError_t launch_hf_records(const uint32_t* idx, long n, int logN, float mass, float4* out, cudaStream_t st);
+cudaError_t launch_hf_records(const uint32_t* idx, long n, int N, float mass, float4* out, cudaStream_t st);
 
 // Subgrid Poisson cycle of the halo finder (kernels_sg.cu).
 constexpr int SG_B = 1024;               // stream positions per block
@@ -219,13 +219,40 @@ cudaError_t launch_sg_free_count(const uint32_t* FL, long nwords, uint32_t* c, c
 cudaError_t launch_sg_nn(const uint64_t* dn, const uint8_t* dk, long nd, const uint32_t* FL, const uint32_t* wpre,
                          long nwords, const float* delta, uint64_t growth, uint64_t hbias, uint32_t* cell,
                          uint32_t* nn, int* err, cudaStream_t st);
-cudaError_t launch_sg_records(const uint32_t* cell, const uint32_t* nn, const uint32_t* off, long nd, int logN,
+cudaError_t launch_sg_records(const uint32_t* cell, const uint32_t* nn, const uint32_t* off, long nd, int N,
                               float mass, float4* out, uint64_t cap, int* err, cudaStream_t st);
 // exclusive prefix sums of n uint32 (out may equal a); chunk: scan_chunks(n)
 // words of scratch; *total (device) receives the sum
 long scan_chunks(long n);
 cudaError_t launch_scan_u32(const uint32_t* a, long n, uint32_t* out, uint32_t* chunk, uint32_t* total,
                             cudaStream_t st);
+
+// Transforms of any side N = 2^a 3^b 5^c (8 | N, 24 <= N <= 1280) in shared
+// memory (kernels_gen.cu), over natural-layout boxes; twiddles: the plain
+// table tw[t] = exp(-2 pi i t / N) (gen_twiddles).
+struct GenPlan {
+  int N;
+  int nst;        // stages
+  int radix[16];  // radix of each stage (8, 4, 2, 3 or 5)
+};
+bool gen_supported(int N);
+GenPlan gen_plan(int N);
+cudaError_t gen_setup(int N);
+cudaError_t launch_gen_fwd_rows(const GenPlan& p, const float2* in, float2* out, const float* alpha, const float2* tw,
+                                cudaStream_t st);
+cudaError_t launch_gen_inv_rows_plain(const GenPlan& p, float2* box, const float2* tw, cudaStream_t st);
+cudaError_t launch_gen_inv_rows_filter(const GenPlan& p, const float2* spec, const Batch& bt, const float2* tw,
+                                       cudaStream_t st);
+cudaError_t launch_gen_hf_rows_filter(const GenPlan& p, const float2* spec, const HfBatch& hb, const float2* tw,
+                                      cudaStream_t st);
+// strided axis (1 = b, 0 = a) in place: `box`, or the batch's K boxes when box is null
+cudaError_t launch_gen_cols(const GenPlan& p, float2* box, const Batch& bt, int axis, bool inverse, const float2* tw,
+                            cudaStream_t st);
+cudaError_t launch_gen_cols_a_test(const GenPlan& p, const Batch& bt, uint8_t* rc, const float* alpha,
+                                   const float2* tw, cudaStream_t st);
+// the pair boxes of hb: inverse pass along axis, and with thresholds (a axis) the bit sets
+cudaError_t launch_gen_hf_cols(const GenPlan& p, const HfBatch& hb, int axis, bool thresholds, const float2* tw,
+                               cudaStream_t st);
 
 // Plain form (kernels_plain.cu).
 cudaError_t launch_plain_centres(long n3, const float2* box, const float* alpha, float zmul, float* mask, int* flag,

@@ -12,7 +12,8 @@
  * catalogue that already exists is skipped, as the reference does (:174-177);
  * the subgrid generator runs on across the redshifts of one invocation, as
  * the reference's single gsl_rng does (:70-71).  The per-redshift work goes
- * through sf21_halo_find_z; N_halo must be a power of two in [16, 1024].
+ * through sf21_halo_find_z (N_halo: a power of two in [16, 1024], or a
+ * product of 2, 3 and 5 that 8 divides in [24, 1280]).
  */
 #define _POSIX_C_SOURCE 200809L
 #include <dirent.h>

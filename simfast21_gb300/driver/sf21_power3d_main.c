@@ -7,8 +7,9 @@
  * Same arguments (nthreads accepted and ignored), same input (raw float or
  * double box, N3 fastest), same text on standard output: the parameter line,
  * the window sum, and one "k P(k)" line per spherical bin.  Only cubic boxes
- * with a power-of-two side from 16 to 1024 (the library's transform sizes);
- * anything else exits 1 with a message.  The window is applied on the host
+ * of the library's transform sizes (a power of two from 16 to 1024, or a
+ * product of 2, 3 and 5 that 8 divides, from 24 to 1280); anything else exits
+ * 1 with a message.  The window is applied on the host
  * in double exactly as the tool does ((float)(value * window),
  * power3d_f.c:134-156) and the sum of its square is taken in the tool's
  * loop order (:121-128); transform and binning run through
@@ -51,9 +52,8 @@ int main(int argc, char **argv) {
   if (2.0 * PI / L3 > dk) dk = 2.0 * PI / L3;
   printf("# Input parameters - Nbytes:%d, N1:%ld,  N2:%ld, N3:%ld, dl:%f, flag:%d, L1:%f, L2:%f, L3:%f, dk:%f, "
          "input file:%s\n", bsize, N1, N2, N3, dl, flag, L1, L2, L3, dk, fname);
-  if (N1 != N2 || N2 != N3 || N1 < 16 || N1 > 1024 || (N1 & (N1 - 1)) || (bsize != 4 && bsize != 8) ||
-      !(dl > 0)) {
-    printf("sf21_power3d_f: only cubic boxes with a power-of-two side in [16, 1024], Nbytes 4 or 8, dl > 0\n");
+  if (N1 != N2 || N2 != N3 || (bsize != 4 && bsize != 8) || !(dl > 0)) {
+    printf("sf21_power3d_f: only cubic boxes, Nbytes 4 or 8, dl > 0\n");
     return 1;
   }
   const long N = N1, n3 = N * N * N;

@@ -8,6 +8,7 @@ compressed .npz files next to this script:
   hii_n32_sfr.npz   N=32,  L=25 Mpc/h, z = 7, 8 (SFR boxes, use_SFR = T)
   hii_n64_sfr.npz   N=64,  L=50 Mpc/h, z = 8
   hii_n32_halo.npz  N=32 (N_halo=64), L=25 Mpc/h, z = 8 (halo catalogue, use_SFR = F)
+  hii_n40_sfr.npz   N=40 (not a power of two), L=31.25 Mpc/h, z = 7, 8
   pk_n32.npz        power3d_f on a 32^3 lognormal box, dl = 0.75, window flags 0, 1, 2
   pk_n64.npz        power3d_f on a 64^3 lognormal box, dl = 1.5, Bartlett window
   t21_n32.npz       t21.c on 32^3 boxes, z = 9, 8, 7, Lya/X-rays off, Vel_comp 3
@@ -17,6 +18,10 @@ compressed .npz files next to this script:
                     to 8), L=100 Mpc, z = 2, 1: tens of thousands of halos
   halos_n64_sgrid.npz  get_halos.c, 64^3 integer-hash field, L=40 Mpc, z = 8, 7,
                     subgrid on (halo_Mmin 1e9)
+  halos_n96.npz     get_halos.c, 96^3 (not a power of two) integer-hash field,
+                    L=60 Mpc, z = 3, 2
+  halos_n120_sgrid.npz  get_halos.c, 120^3 integer-hash field, L=60 Mpc, z = 6,
+                    subgrid on
 The integer-hash boxes (synth.hash_field) are rebuilt bit for bit from their
 recipe on any machine and are not stored.
 
@@ -219,6 +224,7 @@ CASES = {
     "hii_n32_sfr": lambda: case_sfr("hii_n32_sfr.npz", 32, 25.0, 7.0, 8.0, seed=101),
     "hii_n64_sfr": lambda: case_sfr("hii_n64_sfr.npz", 64, 50.0, 8.0, 8.0, seed=202),
     "hii_n32_halo": lambda: case_halo("hii_n32_halo.npz", 32, 64, 25.0, 8.0, seed=303),
+    "hii_n40_sfr": lambda: case_sfr("hii_n40_sfr.npz", 40, 31.25, 7.0, 8.0, seed=131),
     "pk_n32": lambda: case_pk("pk_n32.npz", 32, 0.75, seed=404),
     "pk_n64": lambda: case_pk("pk_n64.npz", 64, 1.5, seed=505, flags=(1,)),
     "t21_n32": lambda: case_t21("t21_n32.npz", 32, 25.0, seed=606, vel_comp=3, lya=False),
@@ -228,6 +234,13 @@ CASES = {
     "halos_n128_dense": lambda: case_halos("halos_n128_dense.npz",
                                            synth.HaloWorkload(N=128, L_mpc=100.0, sigma=4.0, seed=7, smooth=3),
                                            1.0, 2.0, 1.0),
+    "halos_n96": lambda: case_halos("halos_n96.npz",
+                                    synth.HaloWorkload(N=96, L_mpc=60.0, sigma=3.0, seed=1111, smooth=2),
+                                    2.0, 3.0, 1.0),
+    "halos_n120_sgrid": lambda: case_halos("halos_n120_sgrid.npz",
+                                           synth.HaloWorkload(N=120, L_mpc=60.0, sigma=3.0, seed=1212, smooth=1,
+                                                              subgrid=True, Mmin=1e9),
+                                           6.0, 6.0, 1.0),
     "halos_n64_sgrid": lambda: case_halos("halos_n64_sgrid.npz",
                                           synth.HaloWorkload(N=64, L_mpc=40.0, sigma=3.0, seed=1010, smooth=1,
                                                              subgrid=True, Mmin=1e9),

@@ -43,4 +43,4 @@ def load_halo_golden(name):
     return d
 
 
-HALO_CASES = ["halos_n64.npz", "halos_n128_dense.npz", "halos_n64_sgrid.npz"]
+HALO_CASES = ["halos_n64.npz", "halos_n128_dense.npz", "halos_n64_sgrid.npz", "halos_n96.npz", "halos_n120_sgrid.npz"]

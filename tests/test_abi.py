@@ -47,5 +47,5 @@ def test_no_cpu_fallback_without_gpu(lib):
 def test_rejects_unsupported_box(lib):
     from simfast21_gb300 import hii
     with pytest.raises(hii.HIIError) as e:
-        hii.FilterBank(600, 150.0, 0.71, [(30.0, 60.0, 50)])
+        hii.FilterBank(56, 150.0, 0.71, [(30.0, 60.0, 50)])  # 56 = 8 x 7: no radix-7 transforms
     assert e.value.code == 5  # SF21_E_UNSUPPORTED

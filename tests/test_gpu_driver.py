@@ -42,7 +42,7 @@ def _run_driver(hii, base):
     return r.stdout
 
 
-@pytest.mark.parametrize("name", ["hii_n32_sfr.npz", "hii_n64_sfr.npz"])
+@pytest.mark.parametrize("name", ["hii_n32_sfr.npz", "hii_n64_sfr.npz", "hii_n40_sfr.npz"])
 def test_driver_sfr_branch(hii, oracle_lib, tmp_path, name):
     g = load_golden(name)
     sp = g["params"]

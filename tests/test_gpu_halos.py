@@ -145,6 +145,30 @@ def test_driver_writes_library_catalogues(tmp_path):
     hf.close()
 
 
+@pytest.mark.parametrize("name", ["halos_n96.npz", "halos_n120_sgrid.npz"])
+def test_catalogue_mixed_radix(H, name):
+    """Box sides that are not powers of two (the shared-memory radix-2/3/5
+    transforms): the same bar as above."""
+    rep = _check_case(H, name)
+    print(name, "(z, halos, band cells, flipped cells):", rep)
+
+
+def test_filtered_fields_mixed_radix(H):
+    from simfast21_gb300 import halos
+    g = load_halo_golden("halos_n96.npz")
+    hf, cfg = _finder(g, halos)
+    p = H.params_from_ini(H.parse_ini(g["ini"]))
+    z = float(g["zs"][-1])
+    sch = halos.schedule(cfg, z)
+    act = [m for m, s in enumerate(sch) if s["active"]]
+    for m in act[:2] + act[-2:]:
+        ref = H.field(p, z, g["delta"], m)
+        got = hf.field(z, m)
+        err = np.abs(got - ref).max() / np.abs(ref).max()
+        assert err < FIELD_TOL, (m, err)
+    hf.close()
+
+
 def test_catalogue_512_full_size(H):
     """The bench's halo workload at full size (512^3, L = 100 Mpc, z = 7,
     subgrid on, ~7.7 M halos): candidate sets within the band of the

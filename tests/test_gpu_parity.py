@@ -31,7 +31,7 @@ def _case(name):
     return g, g["params"]
 
 
-@pytest.mark.parametrize("name", ["hii_n32_sfr.npz", "hii_n64_sfr.npz"])
+@pytest.mark.parametrize("name", ["hii_n32_sfr.npz", "hii_n64_sfr.npz", "hii_n40_sfr.npz"])
 def test_prologue_bit_exact(hii, oracle_lib, name):
     g, sp = _case(name)
     fb = _bank(hii, sp)
@@ -65,7 +65,7 @@ def _bounds(oracle_lib, sp, z, delta, sfrd):
     return ref, b, lo, hi
 
 
-@pytest.mark.parametrize("name", ["hii_n32_sfr.npz", "hii_n64_sfr.npz"])
+@pytest.mark.parametrize("name", ["hii_n32_sfr.npz", "hii_n64_sfr.npz", "hii_n40_sfr.npz"])
 def test_xhii_matches_reference_outside_band(hii, oracle_lib, name):
     g, sp = _case(name)
     fb = _bank(hii, sp)
@@ -85,7 +85,7 @@ def test_xhii_matches_reference_outside_band(hii, oracle_lib, name):
             assert "%f" % neutral[0] == "%f" % xhi_ref[i]
 
 
-@pytest.mark.parametrize("name", ["hii_n32_sfr.npz", "hii_n64_sfr.npz"])
+@pytest.mark.parametrize("name", ["hii_n32_sfr.npz", "hii_n64_sfr.npz", "hii_n40_sfr.npz"])
 def test_first_hit_within_bounds(hii, oracle_lib, name):
     g, sp = _case(name)
     fb = _bank(hii, sp)
@@ -144,11 +144,12 @@ def test_halo_catalogue_branch(hii, oracle_lib):
     assert np.array_equal(x[0][certain].view(np.uint32), ref_x[certain].view(np.uint32))
 
 
-def test_plain_form_matches_reference(hii, oracle_lib):
+@pytest.mark.parametrize("name", ["hii_n64_sfr.npz", "hii_n40_sfr.npz"])
+def test_plain_form_matches_reference(hii, oracle_lib, name):
     """The plain one-radius-per-launch form (reference structure: FP32 FFT
     convolution with the sphere, painting for R < 2 dx) through the C-ABI."""
     import torch
-    g, sp = _case("hii_n64_sfr.npz")
+    g, sp = _case(name)
     fb = _bank(hii, sp)
     z = float(g["zs"][0])
     d = torch.from_numpy(g["delta_0"]).cuda()

@@ -44,9 +44,9 @@ def test_t21_matches_reference(hii, name):
             assert abs(tsm - ts[n]) <= TOL * abs(ts[n])
 
 
-@pytest.mark.parametrize("vel_comp", [1, 2, 3])
-def test_t21_matches_oracle_128(hii, vel_comp):
-    N, L, z = 128, 100.0, 8.0
+@pytest.mark.parametrize("vel_comp,N", [(1, 128), (2, 128), (3, 128), (3, 120)])  # 120: radix-2/3/5 transforms
+def test_t21_matches_oracle_128(hii, vel_comp, N):
+    L, z = 100.0 * N / 128, 8.0
     delta = synth.lognormal_delta(synth.gaussian_field(N, 808), 0.8).astype(np.float32)
     xhii = np.clip(np.random.default_rng(9).random(delta.shape) * 1.6 - 0.3, 0, 1).astype(np.float32)
     fb = _bank(hii, N, L)

@@ -8,7 +8,7 @@ import pytest
 from helpers import load_golden, oracle_params
 
 
-@pytest.mark.parametrize("name", ["hii_n32_sfr.npz", "hii_n64_sfr.npz"])
+@pytest.mark.parametrize("name", ["hii_n32_sfr.npz", "hii_n64_sfr.npz", "hii_n40_sfr.npz"])
 def test_port_matches_reference_sfr(oracle_lib, name):
     O = oracle_lib
     g = load_golden(name)
