@@ -924,7 +924,7 @@ extern "C" int sf21_hii_filtered(sf21_hii_ctx* c, double z, int kind, const floa
   CTX_CUDA(c, cudaStreamSynchronize(c->stream));
   for (long i = 0; i < c->n3; ++i) {
     rec_R[i] = box[i].x;
-    ion_R[i] = (float)((double)box[i].y * s.fesc / alpha);
+    ion_R[i] = alpha > 0.f ? (float)((double)box[i].y * s.fesc / alpha) : 0.0f;  // alpha < 0: no source
   }
   return SF21_OK;
 }

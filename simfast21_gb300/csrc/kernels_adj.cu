@@ -58,7 +58,9 @@ k_cols_a_crit(Batch bt, float* __restrict__ Cbuf, uint8_t* __restrict__ Abuf, co
   float2* stw = dsm;
   float2* sbuf = dsm + N;
   adj_load_tw<N>(stw, gtw);
-  const float alpha = *alpha_ptr;
+  const float alpha = fabsf(*alpha_ptr);  // sign: the no-source mark
+  // no source anywhere: ion_R is exactly zero (the imaginary half is cross-talk)
+  const float zmul = *alpha_ptr > 0.0f ? bt.zmul : 0.0f;
   const int nblk = N / G::CW;
   const long base = (long)(blockIdx.x / nblk) * N + (blockIdx.x % nblk) * G::CW;
   const long stride = (long)N * N;
@@ -82,7 +84,7 @@ k_cols_a_crit(Batch bt, float* __restrict__ Cbuf, uint8_t* __restrict__ Abuf, co
     for (int r = 0; r < 8; ++r) {
       const float den = v[r].x * alpha;  // alpha * rec_R
       if (den > 0.0f) {
-        const float ratio = __fdiv_rn(v[r].y * bt.zmul, den);
+        const float ratio = __fdiv_rn(v[r].y * zmul, den);
         if (ratio > best[r]) {
           best[r] = ratio;
           arg[r] = bt.r[k].ridx;
@@ -115,7 +117,7 @@ k_cols_a_adj(Batch bt, const float* __restrict__ g, const uint8_t* __restrict__ 
   float2* sbuf = dsm + N;
   __shared__ float red[32];
   adj_load_tw<N>(stw, gtw);
-  const float alpha = *alpha_ptr;
+  const float alpha = fabsf(*alpha_ptr);  // sign: the no-source mark
   const float inv_alpha = 1.0f / alpha;  // exact: alpha is a power of two
   const int nblk = N / G::CW;
   const long base = (long)(blockIdx.x / nblk) * N + (blockIdx.x % nblk) * G::CW;
@@ -216,7 +218,7 @@ k_rows_adj_acc(Batch bt, float2* __restrict__ acc, const float2* __restrict__ gt
 __global__ void k_grad_finish(long n3, const float2* __restrict__ Gbox, const float* __restrict__ alpha_ptr,
                               const float* __restrict__ delta, const float* __restrict__ rec0, float r2,
                               float r3, float src_mul, float* __restrict__ gdelta, float* __restrict__ gsrc) {
-  const float alpha = *alpha_ptr;
+  const float alpha = fabsf(*alpha_ptr);  // sign: the no-source mark
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += (long)gridDim.x * blockDim.x) {
     const float2 G = Gbox[i];
     const float od = 1.0f + delta[i];

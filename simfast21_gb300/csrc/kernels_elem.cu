@@ -48,6 +48,7 @@ k_prologue(long n3, const float* __restrict__ delta, const float* __restrict__ s
            const PrologueArgs pa, float* __restrict__ rec0, float* __restrict__ fres,
            float2* __restrict__ packed, float* __restrict__ partials) {
   float sd2 = 0.f, sh2 = 0.f;
+  int nz = 0;  // some ionisation rate is not exactly zero
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += (long)gridDim.x * blockDim.x) {
     const float d = delta[i];
     const sd_t one_d = sd_add(SD_ONE, sd_from_float(d));  // 1. + density_map[i]
@@ -65,7 +66,9 @@ k_prologue(long n3, const float* __restrict__ delta, const float* __restrict__ s
     packed[i] = make_float2(rr, h1);
     sd2 += rr * rr;
     sh2 += h1 * h1;
+    nz |= (h1 != 0.0f);
   }
+  nz = __syncthreads_or(nz);
   // block reduction of the two sums of squares (only their ratio is used)
   __shared__ float red[2][PRO_THREADS / 32];
   for (int o = 16; o > 0; o >>= 1) {
@@ -83,6 +86,9 @@ k_prologue(long n3, const float* __restrict__ delta, const float* __restrict__ s
       a += red[0][w];
       b += red[1][w];
     }
+    // a block with a nonzero rate reports a nonzero sum even when every
+    // square underflows, so that an all-zero box is told apart exactly
+    if (nz && b == 0.f) b = __int_as_float(1);
     partials[2 * blockIdx.x] = a;
     partials[2 * blockIdx.x + 1] = b;
   }
@@ -101,7 +107,12 @@ cudaError_t launch_prologue(long n3, const float* delta, const float* src, const
 }
 
 // alpha = 2^round(log2(|rec| / |ion|)), so that the two halves of the packed
-// transform have comparable norms.
+// transform have comparable norms.  An ionisation box that is zero in every
+// cell gets alpha = -1: the reference's filtered ionisation field is then
+// exactly zero and no cell is a centre (its test wants ion_R > 0,
+// get_HIIbubbles.c:339-348), while the packed transform's imaginary half
+// holds rounding cross-talk from the recombination half; is_centre reads
+// alpha <= 0 as "no centre", and the other users take |alpha|.
 __global__ void k_alpha(const float* __restrict__ partials, int nblocks, float* __restrict__ alpha) {
   __shared__ float sa[256], sb[256];
   float a = 0.f, b = 0.f;
@@ -121,7 +132,9 @@ __global__ void k_alpha(const float* __restrict__ partials, int nblocks, float* 
   }
   if (threadIdx.x == 0) {
     float r = 1.0f;
-    if (sa[0] > 0.f && sb[0] > 0.f && isfinite(sa[0]) && isfinite(sb[0])) {
+    if (sb[0] == 0.f) {
+      r = -1.0f;
+    } else if (sa[0] > 0.f && sb[0] > 0.f && isfinite(sa[0]) && isfinite(sb[0])) {
       float e = rintf(0.5f * log2f(sa[0] / sb[0]));
       e = fminf(fmaxf(e, -60.f), 60.f);
       r = exp2f(e);

@@ -40,7 +40,7 @@ k_fwd_rows(const float2* __restrict__ in, float2* __restrict__ out,
   const int row_in_cta = threadIdx.x / G::T;
   const int j = threadIdx.x % G::T;
   const long row = (long)blockIdx.x * G::ROWS + row_in_cta;
-  const float alpha = alpha_ptr ? *alpha_ptr : 1.0f;
+  const float alpha = alpha_ptr ? fabsf(*alpha_ptr) : 1.0f;
   float2 v[8];
   const float2* src = in + row * N;
 #pragma unroll

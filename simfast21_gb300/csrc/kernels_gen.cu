@@ -150,7 +150,7 @@ __global__ void __launch_bounds__(GR_THREADS) k_gen_rows(GenRowsArgs ga, GenPlan
   const long row0 = (long)blockIdx.x * GR_LINES;
   const long nrows = (long)N * N;
   const int L = (int)(row0 + GR_LINES <= nrows ? GR_LINES : nrows - row0);
-  const float alpha = (ga.mode == 0 && ga.alpha) ? *ga.alpha : 1.0f;
+  const float alpha = (ga.mode == 0 && ga.alpha) ? fabsf(*ga.alpha) : 1.0f;
   // load
   for (int t = threadIdx.x; t < L * N; t += blockDim.x) {
     const int l = t / N, c = t - l * N;

@@ -60,8 +60,9 @@ __device__ __forceinline__ float w_tophat(float x) {
 // and rec <= 0 already give ion >= rec, so the test reduces to
 // v.y > 0 && v.y * zeta >= v.x * alpha (alpha a power of two: exact scaling).
 // The one difference, a NaN rec, does not arise from finite boxes.
+// alpha <= 0 marks an ionisation box that is zero everywhere: no centre.
 __device__ __forceinline__ bool is_centre(float2 v, float alpha, float zeta) {
-  return (v.y > 0.0f) && (v.y * zeta >= v.x * alpha);
+  return (alpha > 0.0f) && (v.y > 0.0f) && (v.y * zeta >= v.x * alpha);
 }
 
 // Signed frequency index of position i on an N-point axis (:309-311).

@@ -182,3 +182,32 @@ def test_catalogue_512_full_size(H):
     rep = _check_case(H, "bench512", g=g)
     print("bench512 (z, halos, band cells, flipped cells):", rep)
     assert rep[0][1] > 1_000_000
+
+
+def _edge_case(kind):
+    from simfast21_gb300 import synth
+    if kind == "zero_density":  # no excursion-set or cell-size halos; the subgrid draws at the mean
+        w = synth.HaloWorkload(N=32, L_mpc=20.0, sigma=1.0, seed=1, subgrid=True, Mmin=1e9)
+        d = np.zeros((32,) * 3, np.float32)
+    elif kind == "single_spike":  # one very dense cell: overlapping spheres of every mass around it
+        w = synth.HaloWorkload(N=32, L_mpc=20.0, sigma=1.0, seed=1)
+        d = np.zeros((32,) * 3, np.float32)
+        d[5, 31, 0] = 300.0  # next to the periodic edges (spheres stay below the reference's N^3/200 buffer)
+    elif kind == "n16":  # smallest power-of-two side
+        w = synth.HaloWorkload(N=16, L_mpc=12.0, sigma=3.0, seed=2, smooth=1)
+        d = w.density()
+    elif kind == "n24":  # smallest 2-3-5 side
+        w = synth.HaloWorkload(N=24, L_mpc=18.0, sigma=3.0, seed=3, smooth=1, subgrid=True, Mmin=1e9)
+        d = w.density()
+    else:  # the cell mass below halo_Mmin: no cell-size or subgrid cycle
+        w = synth.HaloWorkload(N=32, L_mpc=10.0, sigma=3.0, seed=4, smooth=1, subgrid=True, Mmin=1e11)
+        d = w.density()
+    return {"ini": synth.halo_ini_text(w, 2.0, 3.0, 1.0), "delta": d.reshape((w.N,) * 3), "zs": np.array([3.0, 2.0])}
+
+
+@pytest.mark.parametrize("kind", ["zero_density", "single_spike", "n16", "n24", "no_cell_cycle"])
+def test_edge_cases(H, kind):
+    """Empty and degenerate inputs and the smallest sides, against the
+    oracle's serial loop (byte for byte on the GPU's candidate sets)."""
+    rep = _check_case(H, kind, g=_edge_case(kind))
+    print(kind, "(z, halos, band cells, flipped cells):", rep)

@@ -282,3 +282,32 @@ def test_filtered_fields_cufft_crosscheck(hii, oracle_lib):
             print(f"R={R:.3f}: library {e_ours:.2e}, cuFFT {e_cu:.2e} (of max |field|)")
             assert e_ours <= TOL_FIELD
             assert e_ours <= 4.0 * e_cu + 1e-7
+
+
+@pytest.mark.parametrize("kind", ["no_sources", "saturated", "uniform_density"])
+def test_edge_boxes(hii, oracle_lib, kind):
+    """Degenerate inputs against the CPU restatement (byte-identical to the
+    reference on the fixtures): no sources (no centre anywhere), sources so
+    strong that every cell is a centre at the largest radius, and a uniform
+    density box with sparse sources."""
+    g, sp = _case("hii_n32_sfr.npz")
+    z = float(g["zs"][0])
+    delta = np.ascontiguousarray(g["delta_0"], np.float32)
+    sfrd = np.ascontiguousarray(g["sfrd_0"], np.float32)
+    if kind == "no_sources":
+        sfrd = np.zeros_like(sfrd)
+    elif kind == "saturated":
+        sfrd = (sfrd + 1.0) * np.float32(1e3)
+    else:
+        delta = np.zeros_like(delta)
+    fb = _bank(hii, sp)
+    x, neutral = fb.run_z(z, delta, sfrd)
+    _, b, lo, hi = _bounds(oracle_lib, sp, z, delta, sfrd)
+    certain = b["ionised_lo"] == b["ionised_hi"]
+    ref = oracle_lib.run_z_sfr(oracle_params(oracle_lib, sp), z, delta, sfrd)["xhii"]
+    assert np.array_equal(x[0][certain].view(np.uint32), ref[certain].view(np.uint32))
+    assert np.all((x[0] == lo) | (x[0] == hi))
+    if kind == "no_sources":
+        assert not np.any(x[0] == 1.0)
+    if kind == "saturated":
+        assert np.mean(x[0] > 0.5) > 0.99
