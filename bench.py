@@ -323,6 +323,70 @@ def halo_metrics(rank: int, with_cpu: bool, N: int = 512, z: float = 7.0, reps: 
     return res
 
 
+def sfr_catalogue(n: int, N_halo: int, seed: int):
+    """Seeded Halo_t catalogue: log-uniform masses 1e8-1e12 Msun, uniform
+    positions in N_halo cells."""
+    from simfast21_gb300.halos import HALO_DTYPE
+    rng = np.random.default_rng(seed)
+    cat = np.empty(n, HALO_DTYPE)
+    cat["Mass"] = (10.0 ** rng.uniform(8.0, 12.0, n)).astype(np.float32)
+    for ax in ("x", "y", "z"):
+        cat[ax] = (rng.random(n, dtype=np.float32) * np.float32(N_halo)).astype(np.float32)
+    return cat
+
+
+def sfr_metrics(rank: int, with_cpu: bool, N_halo: int = 1200, N: int = 600, n_halos: int = 20_000_000,
+                z: float = 8.0, reps: int = 3):
+    """Star-formation-rate stage of get_SFR.c at the reference's default grids
+    (N_halo 1200 -> N_smoothed 600, L = 150 Mpc, h = 0.7) on a seeded
+    catalogue: device time per redshift with the catalogue resident (CUDA
+    events on the launching stream), end to end through sf21_sfr_box (host
+    catalogue in, host box out), and the CPU restatement on the same inputs."""
+    import torch
+
+    from simfast21_gb300 import sfr
+    L = 150.0 * 0.7
+    cat = sfr_catalogue(n_halos, N_halo, seed=2024)
+    s = sfr.SFRBox(N_halo, N, L)
+    d_cat = torch.from_numpy(cat.view(np.uint8)).cuda()
+    d_out = torch.empty(N ** 3, dtype=torch.float32, device="cuda")
+    st = torch.cuda.current_stream()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    dev = []
+    for r in range(reps + 1):
+        torch.cuda.synchronize()
+        ev0.record(st)
+        s.box_device(z, n_halos, d_cat.data_ptr(), d_out.data_ptr(), st.cuda_stream)
+        ev1.record(st)
+        torch.cuda.synchronize()
+        if r:
+            dev.append(ev0.elapsed_time(ev1))
+    host_out = np.empty((N,) * 3, np.float32)
+    e2e = []
+    L_ = s._L
+    for r in range(reps + 1):
+        t0 = time.perf_counter()
+        s._check(L_.sf21_sfr_box(s._h, z, n_halos, cat.ctypes.data, host_out.ctypes.data, None))
+        if r:
+            e2e.append((time.perf_counter() - t0) * 1e3)
+    s.close()
+    ms, ms_e2e = float(np.median(dev)), float(np.median(e2e))
+    res = {"N_halo": N_halo, "N_smoothed": N, "halos": n_halos, "z": z, "ms_per_redshift": ms,
+           "halos_per_s": n_halos / (ms / 1e3), "e2e_ms_per_redshift": ms_e2e,
+           "e2e_halos_per_s": n_halos / (ms_e2e / 1e3), "h2d_bytes": 16 * n_halos, "d2h_bytes": 4 * N ** 3}
+    if rank == 0 and with_cpu:
+        from oracle import oracle as O
+        p = O.params(N, L, 0.7, L / 2, 10, 30.0, N_halo=N_halo, nthreads=os.cpu_count() or 1)
+        t0 = time.perf_counter()
+        O.sfrd_box(p, z, cat)
+        cpu_s = time.perf_counter() - t0
+        res["cpu_baseline"] = {"value": n_halos / cpu_s, "unit": "halos/s", "cores": os.cpu_count() or 1,
+                               "kind": "port", "sample": f"restatement of get_SFR.c (serial CIC, OpenMP "
+                                                         f"smooth_box, serial mean), same catalogue and grids, "
+                                                         f"{cpu_s:.1f} s"}
+    return res
+
+
 def run_ours(args, w, rank, world):
     import torch
     from simfast21_gb300 import build as B
@@ -494,6 +558,11 @@ def run_ours(args, w, rank, world):
     if not args.no_halos:
         halo = halo_metrics(rank, not args.no_cpu_baseline)
 
+    # star-formation-rate stage (get_SFR.c) at the reference's default grids
+    sfr_res = None
+    if not args.no_halos:
+        sfr_res = sfr_metrics(rank, not args.no_cpu_baseline)
+
     # CPU baseline (rank 0 only)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -532,6 +601,7 @@ def run_ours(args, w, rank, world):
             "power_spectrum": pk,
             "t21": t21,
             "halo_finder": halo,
+            "sfr": sfr_res,
             "cpu_baseline": cpu,
         }
         print(json.dumps(out))
@@ -548,9 +618,12 @@ def main():
     ap.add_argument("--kmax", type=int, default=0, help="radii per spectrum read (0 = library default)")
     ap.add_argument("--no-grad", action="store_true", help="skip the bwd/fwd measurement")
     ap.add_argument("--no-pk", action="store_true", help="skip the power-spectrum and 21-cm measurements")
-    ap.add_argument("--no-halos", action="store_true", help="skip the halo-finder measurement")
+    ap.add_argument("--no-halos", action="store_true",
+                    help="skip the halo-finder and star-formation-rate measurements")
     ap.add_argument("--halos-only", type=int, default=0, metavar="N",
                     help="run only the halo-finder measurement at N^3 and print it (profiling entry point)")
+    ap.add_argument("--sfr-only", action="store_true",
+                    help="run only the star-formation-rate measurement and print it (profiling entry point)")
     ap.add_argument("--grad-large", action="store_true", help="also time fwd+bwd at 1024^3 (peak HBM)")
     ap.add_argument("--path", type=int, default=0,
                     help="radius pipeline: 0 = tuned, else one of PIPELINES")
@@ -561,6 +634,11 @@ def main():
         from simfast21_gb300 import build as B
         B.build()
         print(json.dumps({"halo_finder": halo_metrics(rank, not args.no_cpu_baseline, N=args.halos_only)}))
+        return
+    if args.sfr_only:
+        from simfast21_gb300 import build as B
+        B.build()
+        print(json.dumps({"sfr": sfr_metrics(rank, not args.no_cpu_baseline)}))
         return
     w = workload(args.workload, rank)
     if args.impl == "reference":

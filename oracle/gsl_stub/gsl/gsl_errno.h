@@ -1,0 +1,7 @@
+/*
+ * Included by get_SFR.c:20, which calls nothing from it.
+ * ORACLE / TEST INFRASTRUCTURE ONLY.
+ */
+#ifndef SF21_ORACLE_GSL_ERRNO_STUB_H
+#define SF21_ORACLE_GSL_ERRNO_STUB_H
+#endif

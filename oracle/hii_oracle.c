@@ -458,6 +458,34 @@ int sf21o_halo_smoothed(const sf21o_params *p, double z, long nhalos,
   return 0;
 }
 
+/* ---- get_SFR.c:104-146 : SFRD box of one catalogue ---------------------
+ * sfr(M, z) = Rion(M, z) / Qion(z) (user_functions.c:71-75) into CIC's float
+ * weight on the N_halo^3 grid (:119-121), block average (:123), then each
+ * cell / pow(dx_halo, 3) in double, rounded to float (:129-131); mean is the
+ * serial double sum / N^3 (:141-145). */
+int sf21o_sfrd_box(const sf21o_params *p, double z, long nhalos,
+                   const sf21o_halo *halos, float *out, double *mean) {
+  const long Nh = p->N_halo, N = p->N;
+  if (N > Nh) return 2;
+  float *fine = calloc((size_t)(Nh * Nh * Nh), sizeof(float));
+  if (!fine) return 1;
+  const double q = sf21o_Qion(z);
+  for (long i = 0; i < nhalos; i++)
+    cic_deposit(halos[i].x, halos[i].y, halos[i].z,
+                (float)(sf21o_Rion(halos[i].Mass, z, p) / q), fine, Nh);
+  block_average(fine, out, Nh, N, p->nthreads > 0 ? p->nthreads : 1);
+  free(fine);
+  const double dxh = p->L / Nh;
+  const long N3 = N * N * N;
+  for (long i = 0; i < N3; i++) out[i] = out[i] / pow(dxh, 3);
+  if (mean) {
+    double s = 0.0;
+    for (long i = 0; i < N3; i++) s += out[i];
+    *mean = s / N3;
+  }
+  return 0;
+}
+
 int sf21o_filtered(const sf21o_params *p, const float *rec0, const float *ion0,
                    double R, float *rec_R, float *ion_R) {
   work_t w;

@@ -69,6 +69,12 @@ int sf21o_halo_source(const sf21o_params *p, double z, long nhalos,
 int sf21o_halo_smoothed(const sf21o_params *p, double z, long nhalos,
                         const sf21o_halo *halos, float *out);
 
+/* SFRD box of the star-formation-rate stage (get_SFR.c:104-146): CIC of
+ * sfr(M, z) = Rion/Qion on the N_halo^3 grid, block average to N^3, / dx_halo^3.
+ * mean (may be NULL) receives the serial double average of :141-145. */
+int sf21o_sfrd_box(const sf21o_params *p, double z, long nhalos,
+                   const sf21o_halo *halos, float *out, double *mean);
+
 /* Filtered fields at one radius exactly as the reference computes them
  * (:305-325): unnormalised c2r outputs of the filtered Rrec and Rion boxes. */
 int sf21o_filtered(const sf21o_params *p, const float *rec0, const float *ion0,

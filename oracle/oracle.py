@@ -49,6 +49,8 @@ def lib():
         L.sf21o_filtered.argtypes = [ctypes.POINTER(_Params), f, f, ctypes.c_double, f, f]
         L.sf21o_halo_source.argtypes = [ctypes.POINTER(_Params), ctypes.c_double, ctypes.c_long, f, f]
         L.sf21o_halo_smoothed.argtypes = [ctypes.POINTER(_Params), ctypes.c_double, ctypes.c_long, f, f]
+        L.sf21o_sfrd_box.argtypes = [ctypes.POINTER(_Params), ctypes.c_double, ctypes.c_long, f, f,
+                                     ctypes.POINTER(ctypes.c_double)]
         L.sf21o_radii.argtypes = [ctypes.POINTER(_Params), ctypes.POINTER(ctypes.c_double),
                                   ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
         for fn in ("sf21o_Rrec", "sf21o_Rion"):
@@ -132,6 +134,18 @@ def halo_smoothed(p: _Params, z: float, cat: np.ndarray) -> np.ndarray:
     if rc:
         raise RuntimeError(f"oracle sf21o_halo_smoothed failed ({rc})")
     return out.reshape((p.N,) * 3)
+
+
+def sfrd_box(p: _Params, z: float, cat: np.ndarray):
+    """SFRD box and its average (get_SFR.c:104-146): p.N = N_smoothed,
+    p.N_halo the catalogue's grid, p.L in Mpc/h."""
+    out = np.empty(p.N ** 3, np.float32)
+    cat = np.ascontiguousarray(cat)
+    mean = ctypes.c_double(0.0)
+    rc = lib().sf21o_sfrd_box(ctypes.byref(p), z, len(cat), _ptr(cat), _ptr(out), ctypes.byref(mean))
+    if rc:
+        raise RuntimeError(f"oracle sf21o_sfrd_box failed ({rc})")
+    return out.reshape((p.N,) * 3), mean.value
 
 
 def radii(p: _Params):

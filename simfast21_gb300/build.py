@@ -25,9 +25,11 @@ T21_DRIVER = os.path.join(HERE, "sf21_t21")  # drop-in for t21.x
 T21_DRIVER_SRC = [os.path.join(HERE, "driver", f) for f in ("sf21_t21_main.c", "sf21_stage.c")]
 HALO_DRIVER = os.path.join(HERE, "sf21_get_halos")  # drop-in for get_halos.x
 HALO_DRIVER_SRC = [os.path.join(HERE, "driver", f) for f in ("sf21_get_halos_main.c", "sf21_stage.c")]
+SFR_DRIVER = os.path.join(HERE, "sf21_get_SFR")  # drop-in for get_SFR.x
+SFR_DRIVER_SRC = [os.path.join(HERE, "driver", f) for f in ("sf21_get_SFR_main.c", "sf21_stage.c")]
 SOURCES = ["kernels_fft.cu", "kernels_plane.cu", "kernels_pipe.cu", "kernels_adj.cu", "kernels_elem.cu",
            "kernels_plain.cu", "kernels_halo.cu", "kernels_cb.cu", "kernels_dt.cu", "kernels_pk.cu", "kernels_t21.cu",
-           "kernels_hf.cu", "kernels_sg.cu", "kernels_gen.cu", "hii_api.cu", "halo_api.cu"]
+           "kernels_hf.cu", "kernels_sg.cu", "kernels_gen.cu", "hii_api.cu", "halo_api.cu", "sfr_api.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3"]
 
@@ -67,12 +69,14 @@ def _link_exe(exe: str, srcs, force: bool) -> str:
 
 def build_driver(force: bool = False) -> str:
     """The sf21_hii executable (drop-in for get_HIIbubbles.x), sf21_t21
-    (drop-in for t21.x), sf21_get_halos (drop-in for get_halos.x) and
-    sf21_power3d_f (drop-in for tools/power3d_f), linked to the library with
-    an $ORIGIN rpath; returns the sf21_hii path."""
+    (drop-in for t21.x), sf21_get_halos (drop-in for get_halos.x),
+    sf21_get_SFR (drop-in for get_SFR.x) and sf21_power3d_f (drop-in for
+    tools/power3d_f), linked to the library with an $ORIGIN rpath; returns
+    the sf21_hii path."""
     _link_exe(PK_DRIVER, PK_DRIVER_SRC, force)
     _link_exe(T21_DRIVER, T21_DRIVER_SRC, force)
     _link_exe(HALO_DRIVER, HALO_DRIVER_SRC, force)
+    _link_exe(SFR_DRIVER, SFR_DRIVER_SRC, force)
     return _link_exe(DRIVER, DRIVER_SRC, force)
 
 

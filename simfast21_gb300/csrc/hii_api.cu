@@ -48,7 +48,6 @@ double host_G_H(double z) {
   double hi = 7.18335221e-02 * pow(z, 2.) - 8.85791388e-02 * z - 1.20887500e+01;
   return 4.19232273531e-13 / pow(10.0, lo + hi);
 }
-double host_Qion(double z) { return pow(10.0, 2.05707274e-02 * z + 5.29944413e+01) / 1.e+45; }
 
 struct SetInfo {
   double fesc, Rmax;
@@ -61,6 +60,11 @@ struct SetInfo {
 };
 
 }  // namespace
+
+namespace sf21 {
+// Qion(z) (user_functions.c:84-88), shared with the star-formation-rate stage.
+double host_Qion(double z) { return pow(10.0, 2.05707274e-02 * z + 5.29944413e+01) / 1.e+45; }
+}  // namespace sf21
 
 // Radius pipelines: 1 three axis passes, 2 plane clusters + kx pass,
 // 3 TMA ky + kx pass, 4 TMA ky + TMA kx, and over column-block-major work
@@ -1231,7 +1235,7 @@ static int enqueue_halo_source(sf21_hii_ctx* c, double z, long nhalos, const voi
                                cudaStream_t st) {
   if (nhalos < 0 || (nhalos > 0 && !halos)) CTX_FAIL(c, SF21_E_ARG, "bad halo catalogue");
   if (c->N_halo < c->N) CTX_FAIL(c, SF21_E_ARG, "N_halo < N_smoothed (smooth_box, auxiliary.c:651-654)");
-  if (nhalos > (1L << 28)) CTX_FAIL(c, SF21_E_UNSUPPORTED, "more than 2^28 halos");
+  if (nhalos >= (1L << 28)) CTX_FAIL(c, SF21_E_UNSUPPORTED, "2^28 halos or more (8 CIC entries each, int count)");
   const long nh3 = c->N_halo * c->N_halo * c->N_halo;
   if (!c->d_fine) CTX_CUDA(c, cudaMalloc(&c->d_fine, sizeof(float) * nh3));
   if (nhalos > c->halo_cap) {

@@ -2,7 +2,9 @@
 // get_HIIbubbles.c:229-253): Rion(M, z) of every halo (user_functions.c:40-47),
 // cloud-in-cell deposit on the N_halo^3 grid (auxiliary.c:761-808) and the
 // block average to N_smooth^3 (auxiliary.c:643-684) -- bit-identical with the
-// reference's serial loop.
+// reference's serial loop.  The star-formation-rate stage (get_SFR.c:114-131)
+// is the same deposit with the weight sfr(M, z) = Rion(M, z) / Qion(z)
+// (user_functions.c:71-75) and each smoothed cell divided by dx_halo^3.
 //
 // The reference adds the 8 CIC contributions of halo 0, then halo 1, ... into
 // a float box (float += double each time), so a cell's value depends on the
@@ -39,18 +41,21 @@ __device__ __forceinline__ long wrap_cell(long x, long n) {  // check_borders, a
 }
 
 // Constants of Rion (user_functions.c:33-38) and pow(1+z, c4), as double bit
-// patterns set on the host.
+// patterns set on the host; qion = Qion(z) for the sfr weight, 0 for Rion.
 struct RionConst {
-  sd_t c1, c2, c3, three, vnorm, p1;
+  sd_t c1, c2, c3, three, vnorm, p1, qion;
 };
 
 // Rion(hmass, z) = c1 hmass (1+z)^c4 (hmass/c2)^c3 exp(-(c2/hmass)^3) / V_norm
-__device__ __forceinline__ float rion_sd(float m, const RionConst& k) {
+// in double; the value CIC receives is that double (or sfr = Rion / Qion,
+// user_functions.c:71-75) rounded to its float parameter (auxiliary.c:761).
+__device__ __forceinline__ float weight_sd(float m, const RionConst& k) {
   const sd_t M = sd_from_float(m);
   const sd_t t1 = sd_mul(sd_mul(k.c1, M), k.p1);
   const sd_t t2 = sd_pow(sd_div(M, k.c2), k.c3);
   const sd_t t3 = sd_exp(sd_neg(sd_pow(sd_div(k.c2, M), k.three)));
-  return sd_to_float(sd_div(sd_mul(sd_mul(t1, t2), t3), k.vnorm));
+  const sd_t rion = sd_div(sd_mul(sd_mul(t1, t2), t3), k.vnorm);
+  return sd_to_float(k.qion ? sd_div(rion, k.qion) : rion);
 }
 
 // 8 contributions per halo, in the reference's corner order.
@@ -59,7 +64,7 @@ __global__ void k_halo_contrib(long nh, const HaloRec* __restrict__ halos, RionC
                                sd_t* __restrict__ vals) {
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nh; i += (long)gridDim.x * blockDim.x) {
     const HaloRec h = halos[i];
-    const float map_in = rion_sd(h.Mass, rk);
+    const float map_in = weight_sd(h.Mass, rk);
     float x1 = h.x, y1 = h.y, z1 = h.z;
     long x = (long)x1, y = (long)y1, z = (long)z1;
     x1 -= (float)x;
@@ -117,9 +122,10 @@ __global__ void k_halo_accumulate(long ne, const unsigned long long* __restrict_
 }
 
 // Block average (smooth_box): av = sum of the sm^3 fine values in double in
-// the reference's loop order, / sm^3, rounded to float.
+// the reference's loop order, / sm^3, rounded to float; post_div != 0 then
+// divides that float by a double and rounds again (get_SFR.c:129-131).
 __global__ void k_smooth_box(const float* __restrict__ fine, float* __restrict__ out, long N, long Ns, long sm,
-                             sd_t sm3) {
+                             sd_t sm3, sd_t post_div) {
   const long n3 = Ns * Ns * Ns;
   for (long o = (long)blockIdx.x * blockDim.x + threadIdx.x; o < n3; o += (long)gridDim.x * blockDim.x) {
     const long i = o / (Ns * Ns), j = (o / Ns) % Ns, p = o % Ns;
@@ -128,7 +134,9 @@ __global__ void k_smooth_box(const float* __restrict__ fine, float* __restrict__
       for (long b = 0; b < sm; b++)
         for (long c = 0; c < sm; c++)
           av = sd_add(av, sd_from_float(fine[(i * sm + a) * N * N + (j * sm + b) * N + (p * sm + c)]));
-    out[o] = sd_to_float(sd_div(av, sm3));
+    float v = sd_to_float(sd_div(av, sm3));
+    if (post_div) v = sd_to_float(sd_div(sd_from_float(v), post_div));
+    out[o] = v;
   }
 }
 
@@ -151,8 +159,7 @@ static uint64_t bits_of(double d) {
   return u;
 }
 
-cudaError_t launch_halo_source(long nh, const void* halos_dev, double z, long N_halo, long N_smooth, float* fine,
-                               float* out, void* scratch, size_t scratch_bytes, cudaStream_t st) {
+static RionConst rion_const(double z, double qion) {
   RionConst rk;
   rk.c1 = bits_of(1.575e39);
   rk.c2 = bits_of(9.367608e+07);
@@ -160,6 +167,14 @@ cudaError_t launch_halo_source(long nh, const void* halos_dev, double z, long N_
   rk.three = bits_of(3.0);
   rk.vnorm = bits_of(1.e+45);
   rk.p1 = bits_of(pow((1.0 + z), 2.27044695e+00));
+  rk.qion = qion != 0.0 ? bits_of(qion) : 0;
+  return rk;
+}
+
+cudaError_t launch_halo_source(long nh, const void* halos_dev, double z, long N_halo, long N_smooth, float* fine,
+                               float* out, void* scratch, size_t scratch_bytes, cudaStream_t st, double qion,
+                               double post_div) {
+  const RionConst rk = rion_const(z, qion);
   const long ne = 8 * nh;
   const long Nh3 = N_halo * N_halo * N_halo;
   cudaError_t e;
@@ -191,7 +206,8 @@ cudaError_t launch_halo_source(long nh, const void* halos_dev, double z, long N_
   const double sm3d = 1.0 * sm * sm * sm;
   uint64_t sm3;
   memcpy(&sm3, &sm3d, 8);
-  k_smooth_box<<<grid_for(N_smooth * N_smooth * N_smooth), 256, 0, st>>>(fine, out, N_halo, N_smooth, sm, sm3);
+  k_smooth_box<<<grid_for(N_smooth * N_smooth * N_smooth), 256, 0, st>>>(
+      fine, out, N_halo, N_smooth, sm, sm3, post_div != 0.0 ? bits_of(post_div) : 0);
   return cudaGetLastError();
 }
 
@@ -276,13 +292,7 @@ int halo_source_noalloc(double z, long N_halo, long N_smooth, long nh, const voi
   }
   unsigned char* p = (unsigned char*)base;
   float* fine = (float*)p;
-  RionConst rk;
-  rk.c1 = bits_of(1.575e39);
-  rk.c2 = bits_of(9.367608e+07);
-  rk.c3 = bits_of(0.44);
-  rk.three = bits_of(3.0);
-  rk.vnorm = bits_of(1.e+45);
-  rk.p1 = bits_of(pow((1.0 + z), 2.27044695e+00));
+  const RionConst rk = rion_const(z, 0.0);
   // The fine grid is the only part that must start at zero (the CIC chains
   // write each touched cell once, untouched cells stay 0); keys, sequence
   // numbers and values are written in full before they are read, and CUB
@@ -307,7 +317,7 @@ int halo_source_noalloc(double z, long N_halo, long N_smooth, long nh, const voi
     long sm = (long)roundf((float)((1.0 * N_halo) / N_smooth));
     if (N_smooth * sm > N_halo) sm = sm - 1;
     k_smooth_box<<<grid_for(N_smooth * N_smooth * N_smooth), 256, 0, st>>>(fine, out, N_halo, N_smooth, sm,
-                                                                           bits_of(1.0 * sm * sm * sm));
+                                                                           bits_of(1.0 * sm * sm * sm), 0);
     e = cudaGetLastError();
   }
   if (e != cudaSuccess) {

@@ -106,15 +106,20 @@ cudaError_t launch_crit_finalize(long n3, float* C, const uint8_t* A, cudaStream
 // Halo-catalogue source box (kernels_halo.cu): CIC of Rion + block average,
 // bit-identical with the reference's serial loop.  halos_dev: nh records
 // {float Mass, x, y, z}; fine: N_halo^3 floats; out: N_smooth^3 floats.
+// qion != 0: the weight is Rion / qion (sfr, get_SFR.c:119-121); post_div != 0:
+// each smoothed cell is then divided by it (get_SFR.c:129-131).
 size_t halo_scratch_bytes(long nh);
 cudaError_t launch_halo_source(long nh, const void* halos_dev, double z, long N_halo, long N_smooth, float* fine,
-                               float* out, void* scratch, size_t scratch_bytes, cudaStream_t st);
+                               float* out, void* scratch, size_t scratch_bytes, cudaStream_t st, double qion = 0.0,
+                               double post_div = 0.0);
 // The same with its scratch in a fixed static device array (no allocation);
 // returns an SF21_* status and writes a message into err on failure.
 int halo_source_noalloc(double z, long N_halo, long N_smooth, long nh, const void* halos_dev, float* out,
                         cudaStream_t st, char* err, size_t errlen);
 // Error text of the context-free entry points (hii_api.cu).
 void set_global_error(const char* msg);
+// Qion(z) of user_functions.c:84-88 in double, host side (hii_api.cu).
+double host_Qion(double z);
 
 // Power spectrum (kernels_pk.cu): window into a complex box, spherical binning
 // of |F|^2 over the half-spectrum (per-CTA float sums, exact counts).

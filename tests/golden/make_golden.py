@@ -22,6 +22,11 @@ compressed .npz files next to this script:
                     L=60 Mpc, z = 3, 2
   halos_n120_sgrid.npz  get_halos.c, 120^3 integer-hash field, L=60 Mpc, z = 6,
                     subgrid on
+  sfr_n32.npz       get_SFR.c, N_halo=64 -> N_smoothed=32, L=25 Mpc/h, z = 8, 7
+                    (use_SFR = T)
+  sfr_n48_lya.npz   get_SFR.c, N_halo=100 -> N_smoothed=48 (a block side that
+                    does not divide), use_SFR = F with Lya/X-rays on (Zminsfr
+                    = 9 of z = 10, 9, 8)
 The integer-hash boxes (synth.hash_field) are rebuilt bit for bit from their
 recipe on any machine and are not stored.
 
@@ -220,6 +225,50 @@ def case_halos(name: str, w, zmin: float, zmax: float, dz: float, keep_full: int
         shutil.rmtree(base)
 
 
+def case_sfrd(name: str, N: int, N_halo: int, L: float, zmin: float, zmax: float, seed: int,
+              use_sfr: bool = True, zminsfr: float | None = None):
+    """The reference's star-formation-rate stage (get_SFR.c, built by
+    ``make -C oracle ref``) on seeded halo catalogues, one per redshift."""
+    w = synth.Workload(N=N, L=L, zs=[], zeta=30.0, Rmax=L / 2, factor=1.1, seed=seed)
+    base = tempfile.mkdtemp(prefix="sf21gold_")
+    try:
+        os.makedirs(os.path.join(base, "Halos"))
+        ini = synth.ini_text(w, zmin, zmax, 1.0, nthreads=4, use_sfr=use_sfr, n_halo=N_halo)
+        if zminsfr is not None:
+            ini += f"use_Lya_xrays = T\nZminsfr = {zminsfr!r}\n"
+        with open(os.path.join(base, "simfast21.ini"), "w") as f:
+            f.write(ini)
+        sp = P.derive(P.read_ini(os.path.join(base, "simfast21.ini")))
+        g = synth.gaussian_field(N, seed)
+        delta = synth.lognormal_delta(g, w.sigma)
+        zs = synth.halo_redshifts(zmin, zmax, 1.0)
+        out = {"ini": ini, "zs": np.array(zs), "N_halo": N_halo}
+        for i, z in enumerate(zs):
+            cat = synth.halo_catalogue(delta, seed + 10 + i, n_halo=N_halo)
+            with open(os.path.join(base, f"Halos/halonl_z{z:.3f}_N{N_halo}_L{sp.L_file:.1f}.dat.catalog"), "wb") as f:
+                np.array([len(cat)], dtype=np.int64).tofile(f)
+                cat.tofile(f)
+            out[f"catalogue_{i}"] = cat
+        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True)
+        r = subprocess.run([os.path.join(ROOT, "oracle", "_ref", "get_SFR.x"), base], capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(r.stdout + r.stderr)
+        zrun = [z for z in zs if z > (zminsfr if zminsfr is not None else zmin) - 0.1]
+        out["zs_written"] = np.array(zrun)
+        for i, z in enumerate(zs):
+            path = os.path.join(base, f"SFR/sfrd_z{z:.3f}_N{N}_L{sp.L_file:.1f}.dat")
+            if os.path.exists(path):
+                out[f"sfrd_{i}"] = np.fromfile(path, np.float32).reshape(N, N, N)
+        out["sfrd_av_txt"] = open(os.path.join(base, "Output_text_files",
+                                               f"sfrd_av_N{N}_L{sp.L_file:.1f}.dat")).read()
+        out["stdout"] = r.stdout
+        np.savez_compressed(os.path.join(HERE, name), **out)
+        print(name, "z =", zs, "halos", [len(out[f"catalogue_{i}"]) for i in range(len(zs))],
+              out["sfrd_av_txt"].split())
+    finally:
+        shutil.rmtree(base)
+
+
 CASES = {
     "hii_n32_sfr": lambda: case_sfr("hii_n32_sfr.npz", 32, 25.0, 7.0, 8.0, seed=101),
     "hii_n64_sfr": lambda: case_sfr("hii_n64_sfr.npz", 64, 50.0, 8.0, 8.0, seed=202),
@@ -245,6 +294,9 @@ CASES = {
                                           synth.HaloWorkload(N=64, L_mpc=40.0, sigma=3.0, seed=1010, smooth=1,
                                                              subgrid=True, Mmin=1e9),
                                           7.0, 8.0, 1.0),
+    "sfr_n32": lambda: case_sfrd("sfr_n32.npz", 32, 64, 25.0, 7.0, 8.0, seed=1313),
+    "sfr_n48_lya": lambda: case_sfrd("sfr_n48_lya.npz", 48, 100, 30.0, 8.0, 10.0, seed=1414, use_sfr=False,
+                                     zminsfr=9.0),
 }
 
 

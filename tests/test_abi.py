@@ -26,12 +26,12 @@ def lib():
 
 
 def test_exports_every_declared_symbol(lib):
-    from simfast21_gb300 import halos, hii
+    from simfast21_gb300 import halos, hii, sfr
     syms = declared_symbols()
     assert len(syms) >= 12
     for s in syms:
         assert hasattr(lib, s), s
-    assert sorted(hii.EXPORTS + halos.EXPORTS) == syms
+    assert sorted(hii.EXPORTS + halos.EXPORTS + sfr.EXPORTS) == syms
 
 
 def test_no_cpu_fallback_without_gpu(lib):
@@ -42,6 +42,10 @@ def test_no_cpu_fallback_without_gpu(lib):
     with pytest.raises(hii.HIIError) as e:
         hii.FilterBank(32, 25.0, 0.71, [(30.0, 12.5, 29)])
     assert e.value.code == 3  # SF21_E_CUDA
+    from simfast21_gb300 import sfr
+    with pytest.raises(hii.HIIError) as e:
+        sfr.SFRBox(64, 32, 25.0)
+    assert e.value.code == 3
 
 
 def test_rejects_unsupported_box(lib):
