@@ -324,12 +324,16 @@ def halo_metrics(rank: int, with_cpu: bool, N: int = 512, z: float = 7.0, reps: 
 
 
 def sfr_catalogue(n: int, N_halo: int, seed: int):
-    """Seeded Halo_t catalogue: log-uniform masses 1e8-1e12 Msun, uniform
-    positions in N_halo cells."""
+    """Seeded Halo_t catalogue with the halo finder's mass structure: masses
+    on its schedule (halo_Mmin = 1e8 Msun, halo_dlm = 0.2, up to 1e12: 21
+    distinct values), abundance falling as dn/dlnM ~ M^-0.9; uniform positions
+    in N_halo cells."""
     from simfast21_gb300.halos import HALO_DTYPE
     rng = np.random.default_rng(seed)
     cat = np.empty(n, HALO_DTYPE)
-    cat["Mass"] = (10.0 ** rng.uniform(8.0, 12.0, n)).astype(np.float32)
+    sched = 1e8 * 10.0 ** (0.2 * np.arange(21))
+    p = sched ** -0.9
+    cat["Mass"] = sched[rng.choice(len(sched), size=n, p=p / p.sum())].astype(np.float32)
     for ax in ("x", "y", "z"):
         cat[ax] = (rng.random(n, dtype=np.float32) * np.float32(N_halo)).astype(np.float32)
     return cat

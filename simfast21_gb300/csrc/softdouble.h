@@ -255,6 +255,64 @@ SD_HD sd_t sd_div(sd_t a, sd_t b) {
   return sd_round_pack(sign, e, q | (r != 0));
 }
 
+// Division by an invariant divisor.  The 128/64-bit integer step of sd_div
+// is done with a precomputed reciprocal, the method of N. Moeller and
+// T. Granlund, "Improved division by invariant integers", IEEE Trans.
+// Computers 60(2), 2011 (Algorithm 4): two multiplications and at most two
+// corrections instead of a software 128-bit division.  Same results as
+// sd_div (the quotient and its remainder are exact).
+typedef struct {
+  uint64_t d;     // divisor significand, leading one at bit 63
+  uint64_t v;     // floor((2^128 - 1) / d) - 2^64
+  uint64_t sign;  // divisor sign bit
+  int eb;         // divisor's unbiased exponent
+  int ok;         // 0: divisor zero, subnormal, infinite or NaN (results are NaN)
+} sd_divc;
+
+SD_HD sd_divc sd_divc_prepare(sd_t b) {
+  sd_divc k;
+  const int eb = (int)((b >> 52) & 0x7FF);
+  k.ok = !(sd_is_zero(b) || eb == 0x7FF || eb == 0);
+  const uint64_t mb = (b & 0xFFFFFFFFFFFFFULL) | (1ULL << 52);
+  k.d = mb << 11;
+  // (2^128 - 1) / d - 2^64 = ((2^64 - 1 - d) * 2^64 + 2^64 - 1) / d
+  k.v = (uint64_t)((((sd_u128)(~k.d)) << 64 | (sd_u128)0xFFFFFFFFFFFFFFFFULL) / k.d);
+  k.sign = b & SD_SIGN;
+  k.eb = eb - 1023;
+  return k;
+}
+
+SD_HD sd_t sd_div_c(sd_t a, const sd_divc k) {
+  const uint64_t sign = (a & SD_SIGN) ^ k.sign;
+  if (!k.ok) return SD_QNAN;
+  if (sd_is_zero(a)) return sign;
+  const int ea = (int)((a >> 52) & 0x7FF);
+  if (ea == 0x7FF || ea == 0) return SD_QNAN;
+  uint64_t ma = (a & 0xFFFFFFFFFFFFFULL) | (1ULL << 52);
+  const uint64_t mb = k.d >> 11;
+  int e = (ea - 1023) - k.eb;
+  if (ma < mb) {
+    ma <<= 1;
+    e -= 1;
+  }
+  // (ma << 62) / mb = ((ma << 62) << 11) / d: the two-word numerator is
+  // u1 = ma << 9, u0 = 0, with u1 < d since ma < 2 mb
+  const uint64_t u1 = ma << 9, u0 = 0;
+  const sd_u128 p = (sd_u128)k.v * u1;
+  uint64_t q0 = (uint64_t)p + u0;
+  uint64_t q1 = (uint64_t)(p >> 64) + u1 + (q0 < u0 ? 1 : 0) + 1;
+  uint64_t r = u0 - q1 * k.d;
+  if (r > q0) {
+    q1 -= 1;
+    r += k.d;
+  }
+  if (r >= k.d) {
+    q1 += 1;
+    r -= k.d;
+  }
+  return sd_round_pack(sign, e, q1 | (r != 0));
+}
+
 SD_HD sd_t sd_sqrt(sd_t a) {
   if (sd_is_zero(a)) return a;
   if (a >> 63) return SD_QNAN;

@@ -39,7 +39,7 @@ static void acc(Stat& s, uint64_t got, uint64_t want) {
 int main(int argc, char** argv) {
   long n = argc > 1 ? atol(argv[1]) : 1000000;
   rng_state = argc > 2 ? strtoull(argv[2], 0, 10) : 88172645463325252ULL;
-  Stat sa{"add"}, ss{"sub"}, sm{"mul"}, sdv{"div"}, sq{"sqrt"}, sf{"to_float"},
+  Stat sa{"add"}, ss{"sub"}, sm{"mul"}, sdv{"div"}, sdc{"div_c"}, sq{"sqrt"}, sf{"to_float"},
       sff{"from_float"}, sp{"pow"}, sp4{"pow4"}, spf{"pow_then_float"}, se{"exp"}, sp3{"pow3"};
   for (long i = 0; i < n; i++) {
     double a = rnd_double(-40, 40, true), b = rnd_double(-40, 40, true);
@@ -49,6 +49,14 @@ int main(int argc, char** argv) {
     acc(ss, sd_sub(d2bits(a), d2bits(b)), d2bits(a - b));
     acc(sm, sd_mul(d2bits(a), d2bits(b)), d2bits(a * b));
     acc(sdv, sd_div(d2bits(a), d2bits(b)), d2bits(a / b));
+    acc(sdc, sd_div_c(d2bits(a), sd_divc_prepare(d2bits(b))), d2bits(a / b));
+    {  // float numerators (the smoothed boxes) over a few fixed divisors
+      float fa; uint32_t fb2 = (uint32_t)rnd64() & 0x7FFFFFFFu; std::memcpy(&fa, &fb2, 4);
+      const double dvs[4] = {std::pow(0.0875, 3.0), std::pow(150.0 * 0.7 / 1200, 3.0), 27.0, 1.0 / 3.0};
+      const double dv = dvs[i & 3];
+      if (std::isfinite(fa) && fa != 0.0f && std::fabs(fa) >= 1.17549435e-38f)
+        acc(sdc, sd_div_c(sd_from_float(fa), sd_divc_prepare(d2bits(dv))), d2bits((double)fa / dv));
+    }
     double pa = std::fabs(a);
     acc(sq, sd_sqrt(d2bits(pa)), d2bits(std::sqrt(pa)));
     double fsrc = rnd_double(-150, 130, true);
@@ -69,7 +77,7 @@ int main(int argc, char** argv) {
     spf.n++;
     if (f2bits(sd_to_float(sd_pow(d2bits(x), d2bits(y)))) != f2bits((float)std::pow(x, y))) spf.bad++;
   }
-  Stat* all[] = {&sa, &ss, &sm, &sdv, &sq, &sf, &sff, &sp, &sp4, &spf, &se, &sp3};
+  Stat* all[] = {&sa, &ss, &sm, &sdv, &sdc, &sq, &sf, &sff, &sp, &sp4, &spf, &se, &sp3};
   for (Stat* s : all) printf("%s %ld %ld %ld\n", s->name, s->n, s->bad, s->maxulp);
   return 0;
 }

@@ -68,11 +68,14 @@ def test_driver_matches_reference_files(hii, tmp_path, name):
     assert r.stdout.count("Writing SFRD file...") == len(g["zs_written"])
 
 
-def _random_catalogue(n, N_halo, seed, edges=True):
+def _random_catalogue(n, N_halo, seed, edges=True, discrete=False):
     from simfast21_gb300.halos import HALO_DTYPE
     rng = np.random.default_rng(seed)
     cat = np.zeros(n, HALO_DTYPE)
-    cat["Mass"] = (10.0 ** rng.uniform(7.5, 12.5, n)).astype(np.float32)
+    if discrete:  # the halo finder's masses: a schedule of 10^(0.2 k) steps
+        cat["Mass"] = (1e8 * 10.0 ** (0.2 * rng.integers(0, 21, n))).astype(np.float32)
+    else:
+        cat["Mass"] = (10.0 ** rng.uniform(7.5, 12.5, n)).astype(np.float32)
     for ax in ("x", "y", "z"):
         cat[ax] = (rng.random(n) * N_halo).astype(np.float32)
     if edges and n >= 64:
@@ -88,16 +91,19 @@ def _random_catalogue(n, N_halo, seed, edges=True):
     return cat
 
 
-@pytest.mark.parametrize("N_halo,N,n,z", [(128, 64, 200_000, 9.0), (96, 96, 50_000, 7.5), (100, 48, 30_000, 6.0),
-                                           (64, 32, 0, 8.0), (64, 16, 1, 8.0)])
-def test_sfrd_vs_restatement(hii, oracle_lib, N_halo, N, n, z):
-    """Catalogues with edge positions, one crowded cell, equal grids (block
-    side 1), a block side that does not divide, an empty and a one-halo
+@pytest.mark.parametrize("N_halo,N,n,z,discrete", [(128, 64, 200_000, 9.0, False), (128, 64, 200_000, 9.0, True),
+                                                    (96, 96, 50_000, 7.5, False), (100, 48, 30_000, 6.0, True),
+                                                    (81, 27, 20_000, 7.0, True), (64, 32, 0, 8.0, False),
+                                                    (64, 16, 1, 8.0, False)])
+def test_sfrd_vs_restatement(hii, oracle_lib, N_halo, N, n, z, discrete):
+    """Catalogues with edge positions, one crowded cell, distinct or schedule
+    masses, equal grids (block side 1), block sides that do not divide or
+    whose cube is not a power of two (3^3), an empty and a one-halo
     catalogue, against the CPU restatement bit for bit."""
     O = oracle_lib
     L = 40.0
     p = O.params(N, L, 0.71, L / 2, 10, 30.0, N_halo=N_halo)
-    cat = _random_catalogue(n, N_halo, seed=N_halo * 7 + n)
+    cat = _random_catalogue(n, N_halo, seed=N_halo * 7 + n, discrete=discrete)
     want, wmean = O.sfrd_box(p, z, cat)
     from simfast21_gb300 import sfr
     s = sfr.SFRBox(N_halo, N, L)
