@@ -62,6 +62,9 @@ def workload(name: str, rank: int = 0):
     elif name == "single256":
         N, L, z, seed = 256, 150.0, 7.0, 1236
         zetas, rmaxs = np.array([30.0]), np.array([30.0])
+    elif name == "single600":  # the reference's default N_smoothed (2-3-5 transforms)
+        N, L, z, seed = 600, 150.0 * h, 7.0, 1236
+        zetas, rmaxs = np.array([30.0]), np.array([50.0 * h])
     elif name == "plain128":
         N, L, z, seed = 128, 100.0, 8.0, 1234
         zetas, rmaxs = np.array([30.0]), np.array([50.0])
@@ -99,6 +102,8 @@ def describe(w):
             "batched256": "HII filter bank, batched: 256^3, L=150 Mpc/h, z=7, 16 sets",
             "single256": "HII filter bank: 256^3, L=150 Mpc/h, z=7, 1 set (zeta=30, Rmax=30 Mpc/h, factor 1.05)",
             "single512": "HII filter bank: 512^3, L=300 Mpc/h, z=7, 1 set (zeta=30, Rmax=35 Mpc/h, factor 1.05)",
+            "single600": "HII filter bank: 600^3 (the reference's default N_smoothed, 2-3-5 transforms), "
+                         "L=106.5 Mpc/h, z=7, 1 set (zeta=30, Rmax=35.5 Mpc/h, factor 1.05)",
             "plain128": "HII filter bank: 128^3, L=100 Mpc/h, z=8, zeta=30, Rmax=50, factor 1.1"}[w["name"]]
 
 

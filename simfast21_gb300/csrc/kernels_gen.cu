@@ -125,6 +125,88 @@ __device__ float2* gen_fft_lines(float2* x, float2* y, int L, int ld, const GenP
   return in;
 }
 
+// ---- the same line FFT with a compile-time plan (the sides in use: the
+// stage radices, spans and strides become constants, so the index arithmetic
+// needs no runtime division and each butterfly no radix switch) ----
+struct GenPlanC {
+  int nst;
+  int radix[16];
+};
+
+constexpr GenPlanC gen_plan_c(int N) {  // the radix order of gen_plan
+  GenPlanC p{0, {}};
+  int m = N;
+  while (m % 5 == 0) { p.radix[p.nst++] = 5; m /= 5; }
+  while (m % 3 == 0) { p.radix[p.nst++] = 3; m /= 3; }
+  while (m % 8 == 0) { p.radix[p.nst++] = 8; m /= 8; }
+  while (m % 4 == 0) { p.radix[p.nst++] = 4; m /= 4; }
+  while (m % 2 == 0) { p.radix[p.nst++] = 2; m /= 2; }
+  return p;
+}
+
+template <int N>
+struct GenPlanOf {
+  static constexpr GenPlanC P = gen_plan_c(N);
+};
+
+template <bool INV, int R>
+__device__ __forceinline__ void gen_butterfly_t(float2 (&v)[8]) {
+  if constexpr (R == 8)
+    dft8<INV>(v);
+  else if constexpr (R == 4)
+    dft4<INV>(v[0], v[1], v[2], v[3]);
+  else if constexpr (R == 5)
+    dft5<INV>(v[0], v[1], v[2], v[3], v[4]);
+  else if constexpr (R == 3)
+    dft3<INV>(v[0], v[1], v[2]);
+  else
+    dft2<INV>(v[0], v[1]);
+}
+
+template <bool INV, int N, int ST, int NS>
+__device__ __forceinline__ float2* gen_stages_t(float2* in, float2* out, int L, int ld, const float2* tw) {
+  if constexpr (ST >= GenPlanOf<N>::P.nst) {
+    return in;
+  } else {
+    constexpr int R = GenPlanOf<N>::P.radix[ST];
+    constexpr int M = N / R;
+    constexpr int tstep = N / (NS * R);
+    for (int g = threadIdx.x; g < L * M; g += blockDim.x) {
+      const int l = g / M, j = g - l * M;
+      const float2* src = in + l * ld;
+      float2* dst = out + l * ld;
+      const int k = j % NS;
+      float2 v[8];
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[r] = src[j + r * M];
+      if constexpr (NS > 1) {
+#pragma unroll
+        for (int r = 1; r < R; ++r) {
+          float2 w = tw[k * r * tstep];
+          if (INV) w.y = -w.y;
+          v[r] = cmul(v[r], w);
+        }
+      }
+      gen_butterfly_t<INV, R>(v);
+      const int base = (j / NS) * NS * R + k;
+#pragma unroll
+      for (int r = 0; r < R; ++r) dst[base + r * NS] = v[r];
+    }
+    __syncthreads();
+    return gen_stages_t<INV, N, ST + 1, NS * R>(out, in, L, ld, tw);
+  }
+}
+
+// Line FFT with the plan fixed at compile time (NT > 0) or read at run time.
+template <bool INV, int NT>
+__device__ __forceinline__ float2* gen_lines(float2* x, float2* y, int L, int ld, const GenPlan& p,
+                                             const float2* tw) {
+  if constexpr (NT > 0)
+    return gen_stages_t<INV, NT, 0, 1>(x, y, L, ld, tw);
+  else
+    return gen_fft_lines<INV>(x, y, L, ld, p, tw);
+}
+
 // ---- rows (c axis) ----
 constexpr int GR_LINES = 2;     // lines per CTA
 constexpr int GR_THREADS = 256;
@@ -139,9 +221,10 @@ struct GenRowsArgs {
   HfBatch hb;             // mode 3
 };
 
+template <int NT>
 __global__ void __launch_bounds__(GR_THREADS) k_gen_rows(GenRowsArgs ga, GenPlan p, const float2* __restrict__ gtw) {
   extern __shared__ float2 gsm[];
-  const int N = p.N;
+  const int N = NT > 0 ? NT : p.N;
   float2* tw = gsm;                       // N
   float2* zs = gsm + N;                   // GR_LINES x N: spectrum rows (filter modes)
   float2* b0 = zs + GR_LINES * N;         // GR_LINES x N
@@ -160,7 +243,7 @@ __global__ void __launch_bounds__(GR_THREADS) k_gen_rows(GenRowsArgs ga, GenPlan
   }
   __syncthreads();
   if (ga.mode <= 1) {
-    float2* r = ga.mode == 0 ? gen_fft_lines<false>(b0, b1, L, N, p, tw) : gen_fft_lines<true>(b0, b1, L, N, p, tw);
+    float2* r = ga.mode == 0 ? gen_lines<false, NT>(b0, b1, L, N, p, tw) : gen_lines<true, NT>(b0, b1, L, N, p, tw);
     for (int t = threadIdx.x; t < L * N; t += blockDim.x) {
       const int l = t / N, c = t - l * N;
       ga.out[(row0 + l) * N + c] = r[l * N + c];
@@ -187,7 +270,7 @@ __global__ void __launch_bounds__(GR_THREADS) k_gen_rows(GenRowsArgs ga, GenPlan
       }
     }
     __syncthreads();
-    float2* r = gen_fft_lines<true>(b0, b1, L, N, p, tw);
+    float2* r = gen_lines<true, NT>(b0, b1, L, N, p, tw);
     float2* dst = ga.mode == 2 ? ga.bt.r[k].work : ga.hb.p[k].work;
     for (int t = threadIdx.x; t < L * N; t += blockDim.x) {
       const int l = t / N, c = t - l * N;
@@ -213,14 +296,18 @@ struct GenColsArgs {
 
 __host__ __device__ __forceinline__ int gen_cw(int N) { return (N <= 600 && N % 16 == 0) ? 16 : 8; }
 
-__global__ void __launch_bounds__(GC_THREADS) k_gen_cols(GenColsArgs ga, GenPlan p, const float2* __restrict__ gtw) {
+// Lines in shared memory have the stride N + 1: the transposing load and
+// store (consecutive threads on consecutive columns) then meet distinct banks.
+template <int NT, int TH>
+__global__ void __launch_bounds__(TH) k_gen_cols(GenColsArgs ga, GenPlan p, const float2* __restrict__ gtw) {
   extern __shared__ float2 gsm[];
-  const int N = p.N;
+  const int N = NT > 0 ? NT : p.N;
   const int CW = gen_cw(N);
+  const int ld = N + 1;
   float2* tw = gsm;
-  float2* b0 = gsm + N;            // CW lines of N
-  float2* b1 = b0 + CW * N;
-  uint8_t* hit = reinterpret_cast<uint8_t*>(b1 + CW * N);  // CW x N (epi 1)
+  float2* b0 = gsm + N;            // CW lines of N, stride ld
+  float2* b1 = b0 + CW * ld;
+  uint8_t* hit = reinterpret_cast<uint8_t*>(b1 + CW * ld);  // CW x N (epi 1)
   for (int t = threadIdx.x; t < N; t += blockDim.x) tw[t] = gtw[t];
   const int nblk = N / CW;
   const int outer = blockIdx.x / nblk;
@@ -237,20 +324,20 @@ __global__ void __launch_bounds__(GC_THREADS) k_gen_cols(GenColsArgs ga, GenPlan
     __syncthreads();  // previous use of b0/b1 (and the twiddles on k = 0)
     for (int t = threadIdx.x; t < CW * N; t += blockDim.x) {
       const int row = t / CW, col = t - row * CW;
-      b0[col * N + row] = box[base + (long)row * stride + col];
+      b0[col * ld + row] = box[base + (long)row * stride + col];
     }
     __syncthreads();
-    float2* r = ga.inverse ? gen_fft_lines<true>(b0, b1, CW, N, p, tw) : gen_fft_lines<false>(b0, b1, CW, N, p, tw);
+    float2* r = ga.inverse ? gen_lines<true, NT>(b0, b1, CW, ld, p, tw) : gen_lines<false, NT>(b0, b1, CW, ld, p, tw);
     if (ga.epi == 0) {
       for (int t = threadIdx.x; t < CW * N; t += blockDim.x) {
         const int row = t / CW, col = t - row * CW;
-        box[base + (long)row * stride + col] = r[col * N + row];
+        box[base + (long)row * stride + col] = r[col * ld + row];
       }
     } else if (ga.epi == 1) {
       const int ridx = ga.bt.r[k].ridx;
       for (int t = threadIdx.x; t < CW * N; t += blockDim.x) {
         const int row = t / CW, col = t - row * CW;
-        if (is_centre(r[col * N + row], alpha, ga.bt.zmul) && ridx < hit[t]) hit[t] = (uint8_t)ridx;
+        if (is_centre(r[col * ld + row], alpha, ga.bt.zmul) && ridx < hit[t]) hit[t] = (uint8_t)ridx;
       }
     } else {
       // a-axis rows a: the CW cells (a, outer = b, c0 .. c0 + CW - 1) are one
@@ -259,7 +346,7 @@ __global__ void __launch_bounds__(GC_THREADS) k_gen_cols(GenColsArgs ga, GenPlan
       for (int row = threadIdx.x; row < N; row += blockDim.x) {
         uint32_t ma = 0, mb = 0;
         for (int col = 0; col < CW; ++col) {
-          const float2 v = r[col * N + row];
+          const float2 v = r[col * ld + row];
           ma |= (v.x > pr.thr_a ? 1u : 0u) << col;
           mb |= (v.y > pr.thr_b ? 1u : 0u) << col;
         }
@@ -310,24 +397,71 @@ GenPlan gen_plan(int N) {
 }
 
 static size_t rows_smem(int N) { return (size_t)(N + 3 * GR_LINES * N) * sizeof(float2); }
-static size_t cols_smem(int N) { return (size_t)(N + 2 * gen_cw(N) * N) * sizeof(float2) + (size_t)gen_cw(N) * N; }
+static size_t cols_smem(int N) {
+  return (size_t)(N + 2 * gen_cw(N) * (N + 1)) * sizeof(float2) + (size_t)gen_cw(N) * N;
+}
+
+// Sides with a compile-time plan: the reference's defaults (600, 1200) and the
+// sides of the reference fixtures that exercise this code (40, 120); others
+// run the same kernels with the plan read at run time.  The large sides get
+// 512-thread column CTAs.
+#define SF21_GEN_SIDES(X) X(40, 256) X(120, 256) X(600, 512) X(1200, 512)
+
+template <int NT, int TH>
+static cudaError_t setup_t(int N) {
+  cudaError_t e = cudaFuncSetAttribute(k_gen_rows<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows_smem(N));
+  if (e) return e;
+  return cudaFuncSetAttribute(k_gen_cols<NT, TH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cols_smem(N));
+}
 
 cudaError_t gen_setup(int N) {
-  cudaError_t e = cudaFuncSetAttribute(k_gen_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows_smem(N));
-  if (e) return e;
-  return cudaFuncSetAttribute(k_gen_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cols_smem(N));
+  switch (N) {
+#define SF21_GEN_CASE(n, th) \
+  case n:                    \
+    return setup_t<n, th>(N);
+    SF21_GEN_SIDES(SF21_GEN_CASE)
+#undef SF21_GEN_CASE
+    default:
+      return setup_t<0, GC_THREADS>(N);
+  }
+}
+
+template <int NT>
+static cudaError_t rows_t(const GenRowsArgs& ga, const GenPlan& p, const float2* tw, cudaStream_t st) {
+  const long nrows = (long)p.N * p.N;
+  k_gen_rows<NT><<<(unsigned)((nrows + GR_LINES - 1) / GR_LINES), GR_THREADS, rows_smem(p.N), st>>>(ga, p, tw);
+  return cudaGetLastError();
 }
 
 static cudaError_t rows(const GenRowsArgs& ga, const GenPlan& p, const float2* tw, cudaStream_t st) {
-  const long nrows = (long)p.N * p.N;
-  k_gen_rows<<<(unsigned)((nrows + GR_LINES - 1) / GR_LINES), GR_THREADS, rows_smem(p.N), st>>>(ga, p, tw);
+  switch (p.N) {
+#define SF21_GEN_CASE(n, th) \
+  case n:                    \
+    return rows_t<n>(ga, p, tw, st);
+    SF21_GEN_SIDES(SF21_GEN_CASE)
+#undef SF21_GEN_CASE
+    default:
+      return rows_t<0>(ga, p, tw, st);
+  }
+}
+
+template <int NT, int TH>
+static cudaError_t cols_t(const GenColsArgs& ga, const GenPlan& p, const float2* tw, cudaStream_t st) {
+  const int N = p.N;
+  k_gen_cols<NT, TH><<<(unsigned)((long)N * (N / gen_cw(N))), TH, cols_smem(N), st>>>(ga, p, tw);
   return cudaGetLastError();
 }
 
 static cudaError_t cols(const GenColsArgs& ga, const GenPlan& p, const float2* tw, cudaStream_t st) {
-  const int N = p.N;
-  k_gen_cols<<<(unsigned)((long)N * (N / gen_cw(N))), GC_THREADS, cols_smem(N), st>>>(ga, p, tw);
-  return cudaGetLastError();
+  switch (p.N) {
+#define SF21_GEN_CASE(n, th) \
+  case n:                    \
+    return cols_t<n, th>(ga, p, tw, st);
+    SF21_GEN_SIDES(SF21_GEN_CASE)
+#undef SF21_GEN_CASE
+    default:
+      return cols_t<0, GC_THREADS>(ga, p, tw, st);
+  }
 }
 
 cudaError_t launch_gen_fwd_rows(const GenPlan& p, const float2* in, float2* out, const float* alpha, const float2* tw,

@@ -311,3 +311,28 @@ def test_edge_boxes(hii, oracle_lib, kind):
         assert not np.any(x[0] == 1.0)
     if kind == "saturated":
         assert np.mean(x[0] > 0.5) > 0.99
+
+
+def test_filtered_fields_600_vs_fp64(hii):
+    """The reference's default N_smoothed = 600 (the shared-memory 2-3-5
+    transforms with a compile-time plan): filtered fields at the largest and
+    the smallest FFT-branch radius against float64 transforms of the same
+    prologue outputs (rec0 from the library, bit-exact with the reference;
+    ion0 = sfrd dx^3 Qion(z) fesc, get_HIIbubbles.c:273)."""
+    N, L, h, z, fesc = 600, 106.5, 0.71, 7.0, 30.0
+    w = synth.Workload(N=N, L=L, zs=[z], seed=4242)
+    delta, sfrd = synth.make_boxes(w, z)
+    fb = hii.FilterBank(N, L, h, [(fesc, 35.5, 109)])
+    rec0, _, _ = fb.prologue(z, delta, sfrd)
+    dx = L / N
+    qion = 10.0 ** (2.05707274e-02 * z + 5.29944413e+01) / 1e45
+    ion0 = sfrd.astype(np.float64) * dx * dx * dx * qion * fesc
+    radii, nf = fb.radii()
+    for ridx in (0, nf - 1):
+        rec, ion = fb.filtered(z, delta, sfrd, ridx)
+        d64, h64 = F.filtered_fields(rec0, ion0, radii[ridx], 2 * np.pi / L)
+        e_rec = np.abs(rec - d64).max() / np.abs(d64).max()
+        e_ion = np.abs(ion - h64).max() / np.abs(h64).max()
+        print(f"600^3 R={radii[ridx]:.3f}: rec {e_rec:.2e}, ion {e_ion:.2e} (of max |field|)")
+        assert e_rec <= TOL_FIELD and e_ion <= TOL_FIELD
+    fb.close()

@@ -35,7 +35,7 @@ def test_pk_matches_reference_tool(hii, name):
         assert np.max(np.abs(P - Pr) / np.abs(Pr)) <= TOL_P
 
 
-@pytest.mark.parametrize("N", [128, 256, 120])  # 120: shared-memory radix-2/3/5 transforms
+@pytest.mark.parametrize("N", [128, 256, 120, 600])  # 120, 600: shared-memory radix-2/3/5 transforms
 def test_pk_matches_oracle(hii, N):
     dl = 300.0 / 512
     box = synth.lognormal_delta(synth.gaussian_field(N, 606 + N), 0.8).astype(np.float32)
