@@ -333,6 +333,8 @@ static int prologue_args(sf21_hii_ctx* c, double z, int kind, PrologueArgs* pa) 
   pa->r2 = dbits(1.76105133);
   pa->r3 = dbits(0.81722878);
   pa->v_norm = dbits(1.e+45);
+  pa->r2c = sd_divc_prepare(pa->r2);
+  pa->v_normc = sd_divc_prepare(pa->v_norm);
   if (kind == SF21_SRC_SFRD) {
     // halo_map*dx*dx*dx*Qion(z) [*fesc]  (:273)
     pa->src_mul[0] = pa->src_mul[1] = pa->src_mul[2] = dbits(c->dx);

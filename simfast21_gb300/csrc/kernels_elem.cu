@@ -21,17 +21,17 @@ __device__ __forceinline__ sd_t xhi_sd(sd_t r) {
   const sd_t b = sd_add(two_r, SD_ONE);            // 2.*ratio + 1.
   const sd_t c = sd_mul(b, b);                     // (..)*(..)
   const sd_t e = sd_mul(sd_ldexp(r, 2), r);        // 4.*ratio*ratio
-  const sd_t g = sd_sqrt(sd_sub(c, e));
+  const sd_t g = sd_sqrt_fast(sd_sub(c, e));
   const sd_t num = sd_sub(b, g);                   // 2.*ratio + 1. - sqrt(..)
   return sd_div(num, two_r);                       // /(2.*ratio)
 }
 
 // Rrec(overdensity, z), user_functions.c:58-65.
 __device__ __forceinline__ sd_t rrec_sd(float od, const PrologueArgs& pa) {
-  const sd_t rec2 = sd_pow(sd_div(sd_from_float(od), pa.r2), pa.r3);
+  const sd_t rec2 = sd_pow(sd_div_c(sd_from_float(od), pa.r2c), pa.r3);
   const sd_t q = sd_div(rec2, sd_add(SD_ONE, rec2));
-  const sd_t rec3 = sd_pow(q, 0x4010000000000000ULL);  // 4.
-  return sd_div(sd_mul(sd_mul(pa.rec1, rec3), pa.dvv), pa.v_norm);
+  const sd_t rec3 = sd_pow4(q);  // pow(.., 4.): exact squaring, correctly rounded like sd_pow
+  return sd_div_c(sd_mul(sd_mul(pa.rec1, rec3), pa.dvv), pa.v_normc);
 }
 
 // Source chain before zeta, left to right as the reference multiplies.

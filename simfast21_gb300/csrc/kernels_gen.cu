@@ -163,14 +163,32 @@ __device__ __forceinline__ void gen_butterfly_t(float2 (&v)[8]) {
     dft2<INV>(v[0], v[1]);
 }
 
+// Per-stage twiddle tables: the stage of span NS and radix R reads
+// w^(k r N / (NS R)) for k < NS, 1 <= r < R from st[NS - 1 + (r - 1) NS + k]
+// (consecutive k on consecutive threads: distinct banks, where the plain
+// table's stride k r N / (NS R) put many k on one bank).  The stage tables
+// fill N - 1 entries in all (the spans telescope: sum (NS R - NS) = N - 1).
+template <int N, int ST, int NS>
+__device__ __forceinline__ void gen_stage_twiddles(float2* st, const float2* __restrict__ gtw) {
+  if constexpr (ST < GenPlanOf<N>::P.nst) {
+    constexpr int R = GenPlanOf<N>::P.radix[ST];
+    constexpr int tstep = N / (NS * R);
+    if constexpr (NS > 1)
+      for (int i = threadIdx.x; i < NS * (R - 1); i += blockDim.x) {
+        const int r = 1 + i / NS, k = i - (r - 1) * NS;
+        st[NS - 1 + i] = gtw[k * r * tstep];
+      }
+    gen_stage_twiddles<N, ST + 1, NS * R>(st, gtw);
+  }
+}
+
 template <bool INV, int N, int ST, int NS>
-__device__ __forceinline__ float2* gen_stages_t(float2* in, float2* out, int L, int ld, const float2* tw) {
+__device__ __forceinline__ float2* gen_stages_t(float2* in, float2* out, int L, int ld, const float2* st) {
   if constexpr (ST >= GenPlanOf<N>::P.nst) {
     return in;
   } else {
     constexpr int R = GenPlanOf<N>::P.radix[ST];
     constexpr int M = N / R;
-    constexpr int tstep = N / (NS * R);
     for (int g = threadIdx.x; g < L * M; g += blockDim.x) {
       const int l = g / M, j = g - l * M;
       const float2* src = in + l * ld;
@@ -182,7 +200,7 @@ __device__ __forceinline__ float2* gen_stages_t(float2* in, float2* out, int L, 
       if constexpr (NS > 1) {
 #pragma unroll
         for (int r = 1; r < R; ++r) {
-          float2 w = tw[k * r * tstep];
+          float2 w = st[NS - 1 + (r - 1) * NS + k];
           if (INV) w.y = -w.y;
           v[r] = cmul(v[r], w);
         }
@@ -193,11 +211,22 @@ __device__ __forceinline__ float2* gen_stages_t(float2* in, float2* out, int L, 
       for (int r = 0; r < R; ++r) dst[base + r * NS] = v[r];
     }
     __syncthreads();
-    return gen_stages_t<INV, N, ST + 1, NS * R>(out, in, L, ld, tw);
+    return gen_stages_t<INV, N, ST + 1, NS * R>(out, in, L, ld, st);
   }
 }
 
-// Line FFT with the plan fixed at compile time (NT > 0) or read at run time.
+// Twiddles into shared memory: the per-stage tables (NT > 0) or the plain
+// table w^t, t < N (plan read at run time).
+template <int NT>
+__device__ __forceinline__ void gen_load_twiddles(float2* tw, int N, const float2* __restrict__ gtw) {
+  if constexpr (NT > 0)
+    gen_stage_twiddles<NT, 0, 1>(tw, gtw);
+  else
+    for (int t = threadIdx.x; t < N; t += blockDim.x) tw[t] = gtw[t];
+}
+
+// Line FFT with the plan fixed at compile time (NT > 0, tw: the stage tables)
+// or read at run time (tw: the plain table).
 template <bool INV, int NT>
 __device__ __forceinline__ float2* gen_lines(float2* x, float2* y, int L, int ld, const GenPlan& p,
                                              const float2* tw) {
@@ -229,7 +258,7 @@ __global__ void __launch_bounds__(GR_THREADS) k_gen_rows(GenRowsArgs ga, GenPlan
   float2* zs = gsm + N;                   // GR_LINES x N: spectrum rows (filter modes)
   float2* b0 = zs + GR_LINES * N;         // GR_LINES x N
   float2* b1 = b0 + GR_LINES * N;         // GR_LINES x N
-  for (int t = threadIdx.x; t < N; t += blockDim.x) tw[t] = gtw[t];
+  gen_load_twiddles<NT>(tw, N, gtw);
   const long row0 = (long)blockIdx.x * GR_LINES;
   const long nrows = (long)N * N;
   const int L = (int)(row0 + GR_LINES <= nrows ? GR_LINES : nrows - row0);
@@ -296,19 +325,22 @@ struct GenColsArgs {
 
 __host__ __device__ __forceinline__ int gen_cw(int N) { return (N <= 600 && N % 16 == 0) ? 16 : 8; }
 
-// Lines in shared memory have the stride N + 1: the transposing load and
-// store (consecutive threads on consecutive columns) then meet distinct banks.
+// Lines in shared memory have a stride ld = 2 (mod 16) float2: the
+// transposing load and store (consecutive threads on CW consecutive columns of
+// a few rows) then meet distinct banks.
+__host__ __device__ __forceinline__ int gen_ld(int N) { return N + ((18 - N % 16) % 16); }
+
 template <int NT, int TH>
 __global__ void __launch_bounds__(TH) k_gen_cols(GenColsArgs ga, GenPlan p, const float2* __restrict__ gtw) {
   extern __shared__ float2 gsm[];
   const int N = NT > 0 ? NT : p.N;
   const int CW = gen_cw(N);
-  const int ld = N + 1;
+  const int ld = gen_ld(N);
   float2* tw = gsm;
   float2* b0 = gsm + N;            // CW lines of N, stride ld
   float2* b1 = b0 + CW * ld;
   uint8_t* hit = reinterpret_cast<uint8_t*>(b1 + CW * ld);  // CW x N (epi 1)
-  for (int t = threadIdx.x; t < N; t += blockDim.x) tw[t] = gtw[t];
+  gen_load_twiddles<NT>(tw, N, gtw);
   const int nblk = N / CW;
   const int outer = blockIdx.x / nblk;
   const int c0 = (blockIdx.x % nblk) * CW;
@@ -398,7 +430,7 @@ GenPlan gen_plan(int N) {
 
 static size_t rows_smem(int N) { return (size_t)(N + 3 * GR_LINES * N) * sizeof(float2); }
 static size_t cols_smem(int N) {
-  return (size_t)(N + 2 * gen_cw(N) * (N + 1)) * sizeof(float2) + (size_t)gen_cw(N) * N;
+  return (size_t)(N + 2 * gen_cw(N) * gen_ld(N)) * sizeof(float2) + (size_t)gen_cw(N) * N;
 }
 
 // Sides with a compile-time plan: the reference's defaults (600, 1200) and the

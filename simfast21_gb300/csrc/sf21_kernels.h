@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include "sf21_device.cuh"
+#include "softdouble.h"
 
 namespace sf21 {
 
@@ -20,6 +21,7 @@ struct PrologueArgs {
   uint64_t v_norm;            // 1e45                           (user_functions.c:38)
   uint64_t src_mul[6];        // source multipliers before zeta (:273 or :258)
   int n_src_mul;
+  sd_divc r2c, v_normc;       // r2 and v_norm as prepared divisors (sd_div_c)
 };
 
 cudaError_t fft_setup(int N);

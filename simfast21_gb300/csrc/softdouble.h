@@ -342,6 +342,54 @@ SD_HD sd_t sd_sqrt(sd_t a) {
   return sd_round_pack(0, e / 2, r | (x != 0));
 }
 
+// sqrt by a fixed-point reciprocal-square-root Newton iteration from a float
+// seed, then an exact integer correction: the same result as the digit-by-
+// digit sd_sqrt, without its 63 iterations on 128-bit values.
+SD_HD uint64_t sd_mulhi64(uint64_t a, uint64_t b) { return (uint64_t)(((sd_u128)a * b) >> 64); }
+
+SD_HD sd_t sd_sqrt_fast(sd_t a) {
+  if (sd_is_zero(a)) return a;
+  if (a >> 63) return SD_QNAN;
+  int ea = (int)((a >> 52) & 0x7FF);
+  if (ea == 0x7FF || ea == 0) return SD_QNAN;
+  uint64_t m = (a & 0xFFFFFFFFFFFFFULL) | (1ULL << 52);
+  int e = ea - 1023;
+  if (e & 1) {
+    m <<= 1;
+    e -= 1;
+  }
+  // x = m << 72 in [2^124, 2^126); X = x / 2^124 = m / 2^52 in [1, 4), Q62: m << 10
+  const uint64_t Xq = m << 10;
+  // y = 1/sqrt(X) in Q63, seeded in float (~24 bits), three Newton steps
+  // y <- y (3 - X y^2) / 2 (each roughly doubles the good bits, to the Q63 limit)
+  const float Xf = (float)m * 2.220446049250313e-16f;  // m / 2^52
+  const float yf = 1.0f / sqrtf(Xf);
+  uint64_t y = yf >= 1.0f ? (1ULL << 63) : (uint64_t)(yf * 9.223372036854775808e18f);
+  for (int it = 0; it < 3; ++it) {
+    const uint64_t y2 = sd_mulhi64(y, y);              // y^2 in Q62 (y^2 <= 1)
+    const uint64_t t = sd_mulhi64(Xq, y2);             // X y^2, Q60
+    const uint64_t u = (3ULL << 60) - t;               // 3 - X y^2, Q60
+    const uint64_t yn = sd_mulhi64(y, u) << 3;         // y u / 2, Q63
+    y = yn;
+  }
+  // r = sqrt(x) = sqrt(X) 2^62 = X y 2^62: mulhi(Xq, y) = X y 2^61
+  uint64_t r = sd_mulhi64(Xq, y) << 1;
+  const sd_u128 x = (sd_u128)m << 72;
+  // exact correction to floor(sqrt(x)): a few units at most; bounded, with
+  // the digit-by-digit routine as the fallback
+  int fix = 0;
+  while ((sd_u128)r * r > x && fix < 64) {
+    --r;
+    ++fix;
+  }
+  while ((sd_u128)(r + 1) * (r + 1) <= x && fix < 64) {
+    ++r;
+    ++fix;
+  }
+  if (fix >= 64) return sd_sqrt(a);
+  return sd_round_pack(0, e / 2, r | ((sd_u128)r * r != x));
+}
+
 // Exact multiplication by 2^k for normal results.
 SD_HD sd_t sd_ldexp(sd_t a, int k) {
   if (sd_is_zero(a)) return a;
@@ -444,6 +492,33 @@ SD_HD sd_t sd_pow(sd_t x, sd_t y) {
   const int ey = (int)((y >> 52) & 0x7FF) - 1023;
   if (ex < -60 || ex > 60 || ey > 5 || ey < -60) return SD_QNAN;
   return sd_exp2_mul(y, sd_log2_q96(x));
+}
+
+// x^4 for x > 0, correctly rounded (the same value as sd_pow(x, 4.0)): the
+// 212-bit integer m^4 of the significand, rounded once.  Exponents outside
+// [-60, 60] take sd_pow's path.
+SD_HD sd_t sd_pow4(sd_t x) {
+  if (sd_is_zero(x) || (x >> 63)) return sd_pow(x, 0x4010000000000000ULL);
+  const int ex = (int)((x >> 52) & 0x7FF) - 1023;
+  if (ex < -60 || ex > 60) return sd_pow(x, 0x4010000000000000ULL);
+  const uint64_t m = (x & 0xFFFFFFFFFFFFFULL) | (1ULL << 52);
+  const sd_u128 m2 = (sd_u128)m * m;  // < 2^106
+  const uint64_t h = (uint64_t)(m2 >> 64), l = (uint64_t)m2;
+  // m^4 = h^2 2^128 + 2 h l 2^64 + l^2 as four 64-bit words w3..w0
+  const sd_u128 ll = (sd_u128)l * l, hl = (sd_u128)h * l, hh = (sd_u128)h * h;
+  uint64_t w0 = (uint64_t)ll;
+  sd_u128 t = (ll >> 64) + ((sd_u128)(uint64_t)hl << 1);
+  uint64_t w1 = (uint64_t)t;
+  t = (t >> 64) + ((hl >> 64) << 1) + ((uint64_t)hl >> 63) + (uint64_t)hh;
+  uint64_t w2 = (uint64_t)t;
+  uint64_t w3 = (uint64_t)(t >> 64) + (uint64_t)(hh >> 64);
+  // leading one at bit L of the 256-bit number (208 <= L <= 211): w3 holds bits 192..255
+  const int L = 255 - sd_clz64(w3);
+  // 63 bits from bit L down (leading one at bit 62), sticky for the rest
+  const int sh = L - 62 - 128;  // shift of (w3:w2) right, 18..21
+  const uint64_t top = (w3 << (64 - sh)) | (w2 >> sh);
+  const uint64_t sticky = ((w2 & ((1ULL << sh) - 1)) | w1 | w0) != 0;
+  return sd_round_pack(0, 4 * ex + (L - 208), top | sticky);
 }
 
 // exp(x) = 2^(x log2 e), correctly rounded for |x| < 2048 with a normal

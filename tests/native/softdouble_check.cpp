@@ -39,8 +39,8 @@ static void acc(Stat& s, uint64_t got, uint64_t want) {
 int main(int argc, char** argv) {
   long n = argc > 1 ? atol(argv[1]) : 1000000;
   rng_state = argc > 2 ? strtoull(argv[2], 0, 10) : 88172645463325252ULL;
-  Stat sa{"add"}, ss{"sub"}, sm{"mul"}, sdv{"div"}, sdc{"div_c"}, sq{"sqrt"}, sf{"to_float"},
-      sff{"from_float"}, sp{"pow"}, sp4{"pow4"}, spf{"pow_then_float"}, se{"exp"}, sp3{"pow3"};
+  Stat sa{"add"}, ss{"sub"}, sm{"mul"}, sdv{"div"}, sdc{"div_c"}, sq{"sqrt"}, sqf{"sqrt_fast"}, sf{"to_float"},
+      sff{"from_float"}, sp{"pow"}, sp4{"pow4"}, sp4x{"pow4_exact"}, spf{"pow_then_float"}, se{"exp"}, sp3{"pow3"};
   for (long i = 0; i < n; i++) {
     double a = rnd_double(-40, 40, true), b = rnd_double(-40, 40, true);
     if (i % 4 == 1) b = rnd_double(-2, 2, true) + a;  // near-cancellation cases
@@ -59,6 +59,14 @@ int main(int argc, char** argv) {
     }
     double pa = std::fabs(a);
     acc(sq, sd_sqrt(d2bits(pa)), d2bits(std::sqrt(pa)));
+    acc(sqf, sd_sqrt_fast(d2bits(pa)), d2bits(std::sqrt(pa)));
+    {  // perfect squares and their neighbours
+      const double r = (double)((rnd64() >> 38) | 1), sqv = r * r;
+      for (int dd = -1; dd <= 1; ++dd) {
+        const double v = bits2d(d2bits(sqv) + dd);
+        acc(sqf, sd_sqrt_fast(d2bits(v)), d2bits(std::sqrt(v)));
+      }
+    }
     double fsrc = rnd_double(-150, 130, true);
     sf.n++;
     if (f2bits(sd_to_float(d2bits(fsrc))) != f2bits((float)fsrc)) sf.bad++;
@@ -70,6 +78,10 @@ int main(int argc, char** argv) {
     acc(sp, sd_pow(d2bits(x), d2bits(y)), d2bits(std::pow(x, y)));
     double x4 = rnd_double(-12, 0, false);
     acc(sp4, sd_pow(d2bits(x4), d2bits(4.0)), d2bits(std::pow(x4, 4.0)));
+    {  // x^4 by exact squaring equals the correctly rounded sd_pow(x, 4)
+      const double xq = (i & 1) ? x4 : rnd_double(-60, 60, false);
+      acc(sp4x, sd_pow4(d2bits(xq)), sd_pow(d2bits(xq), d2bits(4.0)));
+    }
     double xe = -rnd_double(-20, 9, false) * 0.68;  // exp over (-696, 0): normal results
     acc(se, sd_exp(d2bits(xe)), d2bits(std::exp(xe)));
     double x3 = rnd_double(-8, 8, false);
@@ -77,7 +89,7 @@ int main(int argc, char** argv) {
     spf.n++;
     if (f2bits(sd_to_float(sd_pow(d2bits(x), d2bits(y)))) != f2bits((float)std::pow(x, y))) spf.bad++;
   }
-  Stat* all[] = {&sa, &ss, &sm, &sdv, &sdc, &sq, &sf, &sff, &sp, &sp4, &spf, &se, &sp3};
+  Stat* all[] = {&sa, &ss, &sm, &sdv, &sdc, &sq, &sqf, &sf, &sff, &sp, &sp4, &sp4x, &spf, &se, &sp3};
   for (Stat* s : all) printf("%s %ld %ld %ld\n", s->name, s->n, s->bad, s->maxulp);
   return 0;
 }

@@ -25,7 +25,7 @@ def checker(tmp_path_factory):
 def test_basic_ops_bit_exact(checker):
     r = subprocess.run([checker, "300000", "12345"], capture_output=True, text=True, check=True)
     stats = {l.split()[0]: list(map(int, l.split()[1:])) for l in r.stdout.strip().splitlines()}
-    for op in ("add", "sub", "mul", "div", "div_c", "sqrt", "to_float", "from_float"):
+    for op in ("add", "sub", "mul", "div", "div_c", "sqrt", "to_float", "from_float", "pow4_exact", "sqrt_fast"):
         n, bad, _ = stats[op]
         assert n > 0 and bad == 0, (op, stats[op])
     # pow is correctly rounded; libm pow may misround near ties by 1 ulp,
