@@ -277,13 +277,15 @@ def grad_metrics(N, L, z, zeta, rmax, factor, seed, stream, dev, kmax=0):
 
 def halo_metrics(rank: int, with_cpu: bool, N: int = 512, z: float = 7.0, reps: int = 3):
     """Halo finder of get_halos.c on a seeded Gaussian z = 0 density box
-    (P(k) ~ k^-2, rms 4 per cell), L = 100 Mpc, default halo keys with the
-    subgrid cycle on: device time per redshift, end to end with the catalogue
-    copied to host memory, and the CPU restatement at 256^3."""
+    (P(k) ~ k^-2, rms 4 per cell), L = 100 Mpc at 512^3 (the same cell size at
+    other N), default halo keys with the subgrid cycle on: device time per
+    redshift, end to end with the catalogue copied to host memory, and the CPU
+    restatement at 256^3."""
     import ctypes
 
     from simfast21_gb300 import halos
-    w = synth.HaloWorkload(N=N, L_mpc=100.0, sigma=4.0, seed=11, subgrid=True)
+    L_mpc = 100.0 * N / 512
+    w = synth.HaloWorkload(N=N, L_mpc=L_mpc, sigma=4.0, seed=11, subgrid=True)
     ini = synth.halo_ini_text(w, z, z, 1.0)
     d = w.density()
     hf = halos.HaloFinder(halos.config_from_ini(halos.parse_ini(ini)))
@@ -307,7 +309,7 @@ def halo_metrics(rank: int, with_cpu: bool, N: int = 512, z: float = 7.0, reps: 
     counts = hf.counts()
     hf.close()
     ms, ms_e2e = float(np.median(dev)), float(np.median(e2e))
-    res = {"N": N, "L_mpc": 100.0, "z": z, "subgrid": True, "halos": int(n.value),
+    res = {"N": N, "L_mpc": L_mpc, "z": z, "subgrid": True, "halos": int(n.value),
            "excursion_set_halos": int(counts[:-2].sum()), "cell_cycle_halos": int(counts[-2]),
            "subgrid_halos": int(counts[-1]), "set_density_ms": dens_ms, "ms_per_redshift": ms,
            "cells_per_s": N ** 3 / (ms / 1e3), "e2e_ms_per_redshift": ms_e2e,
@@ -315,7 +317,7 @@ def halo_metrics(rank: int, with_cpu: bool, N: int = 512, z: float = 7.0, reps: 
     if rank == 0 and with_cpu:
         from oracle import halo as OH
         Nc = 256
-        wc = synth.HaloWorkload(N=Nc, L_mpc=100.0 * Nc / N, sigma=4.0, seed=11, subgrid=True)
+        wc = synth.HaloWorkload(N=Nc, L_mpc=L_mpc * Nc / N, sigma=4.0, seed=11, subgrid=True)
         pc = OH.params_from_ini(OH.parse_ini(synth.halo_ini_text(wc, z, z, 1.0)))
         dc = wc.density()
         t0 = time.perf_counter()
