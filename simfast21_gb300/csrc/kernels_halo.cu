@@ -10,10 +10,11 @@
 // a float box (float += double each time), so a cell's value depends on the
 // order of its contributions.  Here every contribution is computed in
 // parallel (same float/double steps, integer soft-double for the double
-// ones), tagged with its serial position, grouped by cell with a stable radix
-// sort (the serial order survives inside each cell), and each cell's chain is
-// replayed in that order.  The block average repeats the reference's double
-// sum in its loop order.
+// ones) and written at its serial position, the (cell, weight) entries are
+// grouped by cell with a stable radix sort (the serial order survives inside
+// each cell), and each cell's chain is replayed in that order.  The block
+// average gives the reference's serial double sum (exactly, by an integer sum
+// when no partial sum rounds, else by the soft-double chain).
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_select.cuh>
 #include <cuda_runtime.h>
