@@ -19,6 +19,7 @@
 // The same header compiles as host C++ (g++) so it can be checked against
 // the CPU's native double unit without a GPU.
 #pragma once
+#include <math.h>
 #include <stdint.h>
 
 #if defined(__CUDACC__)
