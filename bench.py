@@ -398,6 +398,50 @@ def sfr_metrics(rank: int, with_cpu: bool, N_halo: int = 1200, N: int = 600, n_h
     return res
 
 
+def hii600_metrics(reps: int = 3):
+    """The HII stage at the reference's default N_smoothed = 600 (2-3-5
+    transforms; workload single600): device time per redshift with CUDA
+    events on the launching stream, per-kernel split, and end to end through
+    sf21_hii_run_z with host boxes."""
+    import torch
+    from simfast21_gb300 import hii
+    w = workload("single600")
+    N = w["N"]
+    delta, sfrd = synth.make_boxes(synth.Workload(N=N, L=w["L"], zs=[w["z"]], seed=w["seed"]), w["z"])
+    fb = hii.FilterBank(N, w["L"], w["hubble"], w["sets"])
+    R = sum(len(fb.radii(s)[0]) for s in range(len(w["sets"])))
+    d_delta = torch.from_numpy(delta).cuda()
+    d_src = torch.from_numpy(sfrd).cuda()
+    d_x = torch.empty((len(w["sets"]), N, N, N), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.Stream()
+    sptr = stream.cuda_stream
+
+    def step():
+        fb.run_z_device(w["z"], d_delta.data_ptr(), d_src.data_ptr(), d_x.data_ptr(), stream=sptr)
+
+    for _ in range(3):
+        step()
+    torch.cuda.synchronize()
+    fb.profile(True)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(reps):
+        step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / reps
+    prof = fb.profile_read()
+    fb.profile(False)
+    t0 = time.perf_counter()
+    fb.run_z(w["z"], delta, sfrd)
+    e2e_ms = (time.perf_counter() - t0) * 1e3
+    fb.close()
+    del d_delta, d_src, d_x
+    return {"workload": describe(w), "radii": R, "ms_per_redshift": ms,
+            "voxel_radii_per_s": N ** 3 * R / (ms / 1e3), "e2e_ms_per_redshift": e2e_ms,
+            "kernels_ms_per_redshift": {k: round(v[0] / reps, 3) for k, v in prof.items() if v[1] > 0}}
+
+
 def run_ours(args, w, rank, world):
     import torch
     from simfast21_gb300 import build as B
@@ -574,6 +618,14 @@ def run_ours(args, w, rank, world):
     if not args.no_halos:
         sfr_res = sfr_metrics(rank, not args.no_cpu_baseline)
 
+    # the HII stage at the reference's default 600^3 (2-3-5 transforms)
+    hii600 = None
+    if not args.no_600:
+        try:
+            hii600 = hii600_metrics()
+        except Exception as e:  # reported in the line, never fatal to the headline measurement
+            hii600 = {"error": str(e)[:300]}
+
     # CPU baseline (rank 0 only)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -613,6 +665,7 @@ def run_ours(args, w, rank, world):
             "t21": t21,
             "halo_finder": halo,
             "sfr": sfr_res,
+            "hii_600": hii600,
             "cpu_baseline": cpu,
         }
         print(json.dumps(out))
@@ -633,6 +686,7 @@ def main():
                     help="skip the halo-finder and star-formation-rate measurements")
     ap.add_argument("--halos-only", type=int, default=0, metavar="N",
                     help="run only the halo-finder measurement at N^3 and print it (profiling entry point)")
+    ap.add_argument("--no-600", action="store_true", help="skip the 600^3 (reference default size) HII measurement")
     ap.add_argument("--sfr-only", action="store_true",
                     help="run only the star-formation-rate measurement and print it (profiling entry point)")
     ap.add_argument("--grad-large", action="store_true", help="also time fwd+bwd at 1024^3 (peak HBM)")
