@@ -8,14 +8,17 @@ full stage pass: prologue, shared forward transform, every set's radius loop,
 dilation, fill and cap, giving 64 xHII boxes.
 
 metric: voxel*radii/s = N^3 * (radii summed over the sets) / step time.
-value : device-resident inputs, CUDA events on the launch stream.
+value : device-resident inputs, CUDA events on the launch stream; the timed
+        steps are the production path (one CUDA graph launch per step); the
+        per-kernel split comes from a separate event-instrumented step.
 e2e   : the same through the host-buffer C-ABI call sf21_hii_run_z (pinned
         host inputs copied in, 64 xHII boxes copied out into pinned host
         memory while the next set computes, neutral fractions summed on the
         host) -- the reference-facing path.
 --impl reference: the CPU restatement of get_HIIbubbles.c (oracle/, FFTW-API
-        shim, OpenMP on all host cores) timed on a bounded sample of the
-        workload (first parameter set, first radii).
+        shim, OpenMP on all host cores) timed on bounded samples of the
+        workload (the front of a redshift and a spread of radii of the median
+        set) and extrapolated to the whole workload (CpuSampler).
 Multi-GPU (torchrun): independent replicas (each rank runs the full
 workload on its GPU; scaling "weak"), barrier + max over ranks.
 """
@@ -40,6 +43,9 @@ from simfast21_gb300 import synth  # noqa: E402
 
 
 # ---------------------------------------------------------------------------
+METRIC = "HII filter-bank voxel*radii/s"
+
+
 def workload(name: str, rank: int = 0):
     """(N, L, z, sets, seed, label) of a named workload.  Under torchrun each
     rank is one replica with its own parameter sets (the batched workloads
@@ -172,43 +178,93 @@ def peaks():
 
 
 # ---------------------------------------------------------------------------
-def cpu_sample(w, n_radii: int, nthreads: int):
-    """CPU restatement on the first parameter set, first n_radii radii."""
-    from oracle import oracle as O
-    O.build()
-    N = w["N"]
-    zt, rmax, nb = w["sets"][0]
-    delta, sfrd = synth.make_boxes(synth.Workload(N=N, L=w["L"], zs=[w["z"]], seed=w["seed"]), w["z"])
-    p = O.params(N, w["L"], w["hubble"], rmax, nb, zt, nthreads=nthreads, max_radii=n_radii)
-    t0 = time.perf_counter()
-    O.run_z_sfr(p, w["z"], delta, sfrd)
-    dt = time.perf_counter() - t0
-    return float(N) ** 3 * n_radii / dt, dt
+class CpuSampler:
+    """The CPU restatement of get_HIIbubbles.c (oracle/, FFTW-API shim with
+    the project's own FFT -- FFTW is absent on both machines -- OpenMP on the
+    host cores) timed on a bounded sample of the workload and extrapolated
+    to all of it.  The sampled set is the one with the median radius count;
+    the sample radii are four of its FFT-branch radii (largest, two middle,
+    smallest) and two of its small-R radii.  Each step times the front of a
+    redshift (prologue, source conversion, fill, both forward transforms)
+    and two of the sample radii in turn.  The reference runs one parameter
+    set per process, so it pays the front per set:
+    t_set = t_front + n_fft(set) * mean t_fft + n_small(set) * mean t_small,
+    and the rate is N^3 * (all radii) / (sum of t_set over the sets)."""
+
+    def __init__(self, w, nthreads: int):
+        from oracle import oracle as O
+        O.build()
+        self.O, self.w, self.nthreads = O, w, nthreads
+        N, dx = w["N"], w["L"] / w["N"]
+        self.counts = []
+        for zt, rmax, nb in w["sets"]:
+            R, nf = P.radii(rmax, dx, nb)
+            self.counts.append((nf, len(R) - nf))
+        order = sorted(range(len(w["sets"])), key=lambda i: sum(self.counts[i]))
+        self.set = order[len(order) // 2]
+        nf, ns = self.counts[self.set]
+        self.idx = [0, nf // 3, (2 * nf) // 3, nf - 1] + ([nf, nf + ns - 1] if ns else [])
+        self.nfft = nf
+        self.delta, self.sfrd = synth.make_boxes(synth.Workload(N=N, L=w["L"], zs=[w["z"]], seed=w["seed"]),
+                                                 w["z"])
+        self.t_front, self.t_r = [], {i: [] for i in self.idx}
+        self.k = 0
+
+    def step(self) -> float:
+        """One bounded sample; returns its wall seconds."""
+        zt, rmax, nb = self.w["sets"][self.set]
+        p = self.O.params(self.w["N"], self.w["L"], self.w["hubble"], rmax, nb, zt, nthreads=self.nthreads)
+        pick = [self.idx[(2 * self.k + j) % len(self.idx)] for j in range(2)]
+        self.k += 1
+        t0 = time.perf_counter()
+        front, tr = self.O.time_radii(p, self.w["z"], self.delta, self.sfrd, pick)
+        dt = time.perf_counter() - t0
+        self.t_front.append(front)
+        for i, t in zip(pick, tr):
+            self.t_r[i].append(t)
+        return dt
+
+    def estimate(self):
+        """(voxel*radii/s of the whole workload, details)."""
+        tf = float(np.mean(self.t_front))
+        fft = [np.mean(v) for i, v in self.t_r.items() if v and i < self.nfft]
+        small = [np.mean(v) for i, v in self.t_r.items() if v and i >= self.nfft]
+        t_fft = float(np.mean(fft))
+        t_small = float(np.mean(small)) if small else t_fft
+        total = sum(tf + nf * t_fft + ns * t_small for nf, ns in self.counts)
+        units = float(self.w["N"]) ** 3 * sum(nf + ns for nf, ns in self.counts)
+        return units / total, {"front_s": tf, "fft_radius_s": t_fft, "small_radius_s": t_small,
+                               "workload_s_extrapolated": total}
+
+    def describe(self, n_steps: int) -> str:
+        nf, ns = self.counts[self.set]
+        return (f"extrapolated: {n_steps} samples of set {self.set} ({nf}+{ns} radii) of the {self.w['N']}^3 "
+                f"workload, each the front of a redshift (prologue, fill, forward transforms) plus two of the "
+                f"radius indices {self.idx}; rate = N^3 * all radii / sum over sets of (front + radii x mean "
+                f"radius time); FFT = the project's FFTW-API shim, not FFTW")
 
 
 def run_reference(args, w, rank):
     if rank != 0:
         return
     ncpu = os.cpu_count() or 1
-    n_radii = 2 if w["N"] >= 512 else 4
+    cs = CpuSampler(w, ncpu)
     for _ in range(args.warmup):
-        cpu_sample(w, n_radii, ncpu)
-    vals, times = [], []
-    for _ in range(args.steps):
-        v, dt = cpu_sample(w, n_radii, ncpu)
-        vals.append(v)
-        times.append(dt)
-    v = float(np.mean(vals))
-    sample = (f"first parameter set, first {n_radii} radii (FFT branch) of the {w['N']}^3 box, "
-              f"prologue and forward transforms included")
+        cs.step()
+    cs.t_front.clear()
+    for v in cs.t_r.values():
+        v.clear()
+    times = [cs.step() for _ in range(max(args.steps, 3))]
+    v, detail = cs.estimate()
     print(json.dumps({
-        "impl": "reference", "metric": "HII filter-bank voxel*radii/s", "value": v,
+        "impl": "reference", "metric": METRIC, "value": v,
         "unit": "voxel*radii/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * float(np.mean(times)), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-        "config": {"workload": describe(w), "flush": "inputs larger than L2"},
+        "config": {"workload": describe(w), "form": "one parameter set per process (reference structure)",
+                   "flush": "inputs larger than L2"},
         "cpu_baseline": {"value": v, "unit": "voxel*radii/s", "cores": ncpu, "kind": "port",
-                         "sample": sample},
+                         "sample": cs.describe(len(times)), **detail},
         "e2e": {"value": v, "unit": "voxel*radii/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
 
@@ -478,7 +534,8 @@ def run_ours(args, w, rank, world):
     torch.cuda.synchronize()
     barrier()
     torch.cuda.synchronize()
-    fb.profile(True)
+    # timed region: the production path (one CUDA graph launch per step, no
+    # per-kernel events)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(dev) as clk:
         ev0.record(stream)
@@ -488,6 +545,13 @@ def run_ours(args, w, rank, world):
         torch.cuda.synchronize()
     barrier()
     ms = ev0.elapsed_time(ev1) / args.steps
+    # per-kernel breakdown from separate, event-instrumented steps (the graph
+    # is bypassed while timing is on)
+    prof_steps = 1
+    fb.profile(True)
+    for _ in range(prof_steps):
+        step()
+    torch.cuda.synchronize()
     prof = fb.profile_read()
     fb.profile(False)
     ms, job_units = reduce_across_ranks(ms, units, "cuda")
@@ -510,7 +574,7 @@ def run_ours(args, w, rank, world):
 
     # roofline of the dominant kernel kind (largest device-time share)
     hbm, peak_kind = peaks()
-    steps = args.steps
+    steps = prof_steps
     kinds = {k: v for k, v in prof.items() if v[1] > 0}
     dom = max(kinds, key=lambda k: kinds[k][0])
     dom_ms, dom_n = kinds[dom]
@@ -560,7 +624,7 @@ def run_ours(args, w, rank, world):
         del d_x
         torch.cuda.synchronize()
         grad = {"box256": grad_metrics(256, 200.0, 8.0, 30.0, 60.0, 1.05, 4321, stream, dev)}
-        if args.grad_large:
+        if not args.no_grad_large:
             grad["box1024"] = grad_metrics(1024, 500.0, 7.0, 30.0, 80.0, 1.12, 5555, stream, dev, kmax=4)
 
     # power spectrum of the density box (tools/power3d_f.c, Bartlett window):
@@ -626,25 +690,27 @@ def run_ours(args, w, rank, world):
         except Exception as e:  # reported in the line, never fatal to the headline measurement
             hii600 = {"error": str(e)[:300]}
 
-    # CPU baseline (rank 0 only)
+    # CPU baseline (rank 0 only): the restatement on the host cores, a
+    # bounded sample extrapolated to the workload
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         ncpu = os.cpu_count() or 1
-        n_radii = 2 if N >= 512 else 4
-        v, dt = cpu_sample(w, n_radii, ncpu)
+        cs = CpuSampler(w, ncpu)
+        n_cpu = 3
+        t_cpu = sum(cs.step() for _ in range(n_cpu))
+        v, detail = cs.estimate()
         cpu = {"value": v, "unit": "voxel*radii/s", "cores": ncpu, "kind": "port",
-               "sample": f"CPU restatement of get_HIIbubbles.c (FFTW-API shim, OpenMP), first parameter "
-                         f"set, first {n_radii} radii of the {N}^3 box incl. prologue+forward FFTs, "
-                         f"{dt:.1f} s"}
+               "sample": cs.describe(n_cpu) + f"; {t_cpu:.1f} s of samples", **detail}
 
     launches = int(sum(v[1] for v in kinds.values()) // steps)
     if rank == 0:
         out = {
-            "metric": "HII filter-bank voxel*radii/s (batched)",
-            "value": value, "unit": "voxel*radii/s", "n_gpus": world, "steps": steps,
+            "metric": METRIC,
+            "value": value, "unit": "voxel*radii/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded lognormal density + SFRD boxes)",
-            "config": {"workload": describe(w), "N": N, "sets": nsets, "radii_total": R_total,
+            "config": {"workload": describe(w), "form": "batched (one shared forward transform, "
+                       "one CUDA graph per step)", "N": N, "sets": nsets, "radii_total": R_total,
                        "pipeline": PIPELINES[path][1],
                        "tuned_batch_ms": {PIPELINES[p][0]: tuned[p] for p in PIPELINES},
                        "flush": "inputs larger than L2 (every box >= 537 MB)"},
@@ -658,6 +724,7 @@ def run_ours(args, w, rank, world):
                          "pipeline_16B_per_voxel_radius_gbs": pipe_gbs,
                          "pipeline_frac": (pipe_gbs / hbm) if pipe_gbs else None},
             "kernels_ms_per_step": {k: round(v[0] / steps, 3) for k, v in kinds.items()},
+            "kernels_source": f"{prof_steps} separate step(s) with CUDA events around each launch",
             "clocks": clk.summary(),
             "plain_gpu": plain,
             "differentiation": grad,
@@ -689,7 +756,7 @@ def main():
     ap.add_argument("--no-600", action="store_true", help="skip the 600^3 (reference default size) HII measurement")
     ap.add_argument("--sfr-only", action="store_true",
                     help="run only the star-formation-rate measurement and print it (profiling entry point)")
-    ap.add_argument("--grad-large", action="store_true", help="also time fwd+bwd at 1024^3 (peak HBM)")
+    ap.add_argument("--no-grad-large", action="store_true", help="skip fwd+bwd at 1024^3 (peak HBM)")
     ap.add_argument("--path", type=int, default=0,
                     help="radius pipeline: 0 = tuned, else one of PIPELINES")
     args = ap.parse_args()

@@ -134,10 +134,12 @@ int sf21_hii_halo_source(sf21_hii_ctx *ctx, double z, long nhalos, const void *h
  * sf21_hii_halo_source.  Its scratch is a fixed 16 MiB array in the
  * library's device image, so N_halo <= 128 and nhalos <= 16384; larger
  * requests return SF21_E_UNSUPPORTED before any GPU work (message in
- * sf21_hii_last_error(NULL)).  The first call on each device (that device
- * current) looks the array up (cudaGetSymbolAddress); make that first call
- * before any stream capture.  Calls that overlap on one device share the
- * array and race: serialise them.  Enqueues on stream (a cudaStream_t, NULL
+ * sf21_hii_last_error(NULL)).  The first call in each CUDA context (the
+ * current device's primary context) looks the array up
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * The address is cached per context, so a call after cudaDeviceReset looks it
+ * up again.  Calls that overlap on one device share the array and race:
+ * serialise them.  Enqueues on stream (a cudaStream_t, NULL
  * = legacy default stream) and returns. */
 int sf21_hii_halo_source_noalloc(double z, long N_halo, long N_smoothed, long nhalos, const void *halos_dev,
                                  float *rion_box_dev, void *stream);
@@ -226,7 +228,7 @@ int sf21_hii_vjp_device(sf21_hii_ctx *ctx, double z, int src_kind, const float *
                         const float *src_dev, int set, const float *dC_dev, float *ddelta_dev,
                         float *dsrc_dev, double *dfesc, void *stream);
 
-/* Radius pipeline in use (1..4, see sf21_hii_config.path); ms_tuned[p-1]
+/* Radius pipeline in use (1..7, see sf21_hii_config.path); ms_tuned[p-1]
  * receives the measured ms of one batch of pipeline p when it was tuned at
  * create (0 if not timed), for p <= cap. */
 int sf21_hii_path(const sf21_hii_ctx *ctx, double *ms_tuned, int cap);
@@ -234,6 +236,23 @@ int sf21_hii_path(const sf21_hii_ctx *ctx, double *ms_tuned, int cap);
 /* Synchronises the context's stream and reports SF21_E_TIMEOUT if a bounded
  * device wait (TMA copy completion) expired since the last check. */
 int sf21_hii_check(sf21_hii_ctx *ctx);
+
+/* Polls per bounded device wait of the TMA-pipelined passes (pipelines 3, 4,
+ * 6 and 7); 0 restores the default (2^26 polls, seconds).  A wait that runs
+ * out makes its block record the error, wait for its own copies in flight
+ * (always with the default bound) and return, so the context stays usable;
+ * the next sf21_hii_check / host-buffer run reports SF21_E_TIMEOUT.  No
+ * reference counterpart (the reference's FFTW calls have no device waits);
+ * lowering it is how the timeout path is exercised without a real stall. */
+int sf21_hii_set_wait_limit(sf21_hii_ctx *ctx, unsigned int polls);
+
+/* Test hook: the n-th device allocation made by any of the library's
+ * contexts after this call (n >= 1) fails with cudaErrorMemoryAllocation,
+ * once; n = 0 disarms it.  The call that met the failure returns
+ * SF21_E_ALLOC and frees what it had allocated (sf21_hii_create leaves
+ * nothing behind).  No reference counterpart: the reference's allocation
+ * checks (get_HIIbubbles.c:102-191) print and exit(1). */
+int sf21_hii_inject_alloc_failure(long n);
 
 /* Measurement hooks.  sf21_hii_profile(ctx, 1) starts recording CUDA events
  * around every kernel the context launches (on its launch stream) and clears

@@ -223,12 +223,109 @@ static void single_cell_fill(work_t *w, const sf21o_params *p) {
   }
 }
 
+/* One radius of the FFT branch (R >= 2 dx, :305-393): filter, both inverse
+ * transforms, centre test and, when there are centres, the FP32 convolution
+ * with the discrete sphere and its threshold into the fill box. */
+static void radius_fft(work_t *w, const sf21o_params *p, double R) {
+  const long N = w->N, N3 = w->N3;
+  const double dx = cell_size(p);
+  const double dx3 = pow(dx, 3);
+  filter_spectra(w, p, R);
+  fftwf_execute(w->i_rec);
+  fftwf_execute(w->i_ion);
+  int any = 0;
+  /* centre test :335-352 */
+#pragma omp parallel for num_threads(p->nthreads) schedule(static) reduction(| : any)
+  for (long i = 0; i < N3; i++) {
+    float h = w->ion[i], d = w->rec[i];
+    float c = 0.0f;
+    if (h > 0.) {
+      if (d > 0.) {
+        if ((double)h / d >= 1.0) c = 1.0f;
+      } else
+        c = 1.0f;
+    }
+    w->bub[i] = c;
+    if (c != 0.0f) any = 1;
+  }
+  if (any) {
+    /* discrete periodic sphere :363-371 (8 image tests) */
+#pragma omp parallel for num_threads(p->nthreads) schedule(static)
+    for (long i = 0; i < N; i++)
+      for (long j = 0; j < N; j++)
+        for (long q = 0; q < N; q++) {
+          long im = i - N, jm = j - N, qm = q - N;
+          int in =
+              sqrt(i * i + j * j + q * q) * dx <= R ||
+              sqrt(i * i + jm * jm + q * q) * dx <= R ||
+              sqrt(i * i + jm * jm + qm * qm) * dx <= R ||
+              sqrt(i * i + qm * qm + j * j) * dx <= R ||
+              sqrt(im * im + j * j + q * q) * dx <= R ||
+              sqrt(im * im + jm * jm + q * q) * dx <= R ||
+              sqrt(im * im + jm * jm + qm * qm) * dx <= R ||
+              sqrt(im * im + j * j + qm * qm) * dx <= R;
+          w->top[i * N * N + j * N + q] = in ? 1.0f : 0.0f;
+        }
+    fftwf_execute(w->f_top); /* :372 */
+    fftwf_execute(w->f_bub); /* :373 */
+    /* complex product :379-381 (float complex *= float complex) */
+    float *bc = (float *)w->bub_c;
+    const float *tc = (const float *)w->top_c;
+#pragma omp parallel for num_threads(p->nthreads) schedule(static)
+    for (long i = 0; i < w->Nh; i++) {
+      float a = bc[2 * i], b = bc[2 * i + 1], c = tc[2 * i], d = tc[2 * i + 1];
+      float ac = a * c, bd = b * d, ad = a * d, bcv = b * c;
+      bc[2 * i] = ac - bd;
+      bc[2 * i + 1] = ad + bcv;
+    }
+    fftwf_execute(w->i_bub); /* :382 */
+    /* threshold :390-393 */
+#pragma omp parallel for num_threads(p->nthreads) schedule(static)
+    for (long i = 0; i < N3; i++) {
+      w->bub[i] = (float)((double)w->bub[i] * dx3 / (double)N3);
+      if ((double)w->bub[i] > dx3 / 100) w->fill[i] = 1.0f;
+    }
+  }
+}
+
+/* One radius of the small-R branch (dx <= R < 2 dx, :406-458): filter, both
+ * inverse transforms and the painting of each centre's ball. */
+static void radius_small(work_t *w, const sf21o_params *p, double R) {
+  const long N = w->N;
+  const double dx = cell_size(p);
+  filter_spectra(w, p, R);
+  fftwf_execute(w->i_rec);
+  fftwf_execute(w->i_ion);
+  const long nc = (long)(R / dx); /* :428 */
+  /* painting :433-458; concurrent writers all store 1.0 */
+#pragma omp parallel for num_threads(p->nthreads) schedule(static)
+  for (long ic = 0; ic < N; ic++)
+    for (long jc = 0; jc < N; jc++)
+      for (long kc = 0; kc < N; kc++) {
+        long c = ic * N * N + jc * N + kc;
+        float h = w->ion[c], d = w->rec[c];
+        if (!(h > 0.)) continue;
+        if (!(!(d > 0.) || ((double)h / d >= 1.0))) continue;
+        for (long a = -(nc + 1); a <= nc + 1; a++) {
+          long ai = wrap_index(ic + a, N);
+          for (long b = -(nc + 1); b <= nc + 1; b++) {
+            if (!(sqrt(a * a + b * b) * dx <= R)) continue;
+            long bi = wrap_index(jc + b, N);
+            for (long e = -(nc + 1); e <= nc + 1; e++) {
+              long ei = wrap_index(kc + e, N);
+              if (sqrt(a * a + b * b + e * e) * dx <= R)
+                w->fill[ai * N * N + bi * N + ei] = 1.0f;
+            }
+          }
+        }
+      }
+}
+
 /* Radius loops (:298-462), cap (:466-471), neutral fraction (:473-477). */
 static void bubble_loops(work_t *w, const sf21o_params *p, float *xhii,
                          double *neutral) {
-  const long N = w->N, N3 = w->N3;
+  const long N3 = w->N3;
   const double dx = cell_size(p), bf = radius_ratio(p);
-  const double dx3 = pow(dx, 3);
   double R = p->Rmax;
 
   int done = 0;
@@ -238,92 +335,12 @@ static void bubble_loops(work_t *w, const sf21o_params *p, float *xhii,
   fftwf_execute(w->f_ion); /* :291 */
 
   while (R >= 2 * dx && done++ < cap) {
-    filter_spectra(w, p, R);
-    fftwf_execute(w->i_rec);
-    fftwf_execute(w->i_ion);
-    int any = 0;
-    /* centre test :335-352 */
-#pragma omp parallel for num_threads(p->nthreads) schedule(static) reduction(| : any)
-    for (long i = 0; i < N3; i++) {
-      float h = w->ion[i], d = w->rec[i];
-      float c = 0.0f;
-      if (h > 0.) {
-        if (d > 0.) {
-          if ((double)h / d >= 1.0) c = 1.0f;
-        } else
-          c = 1.0f;
-      }
-      w->bub[i] = c;
-      if (c != 0.0f) any = 1;
-    }
-    if (any) {
-      /* discrete periodic sphere :363-371 (8 image tests) */
-#pragma omp parallel for num_threads(p->nthreads) schedule(static)
-      for (long i = 0; i < N; i++)
-        for (long j = 0; j < N; j++)
-          for (long q = 0; q < N; q++) {
-            long im = i - N, jm = j - N, qm = q - N;
-            int in =
-                sqrt(i * i + j * j + q * q) * dx <= R ||
-                sqrt(i * i + jm * jm + q * q) * dx <= R ||
-                sqrt(i * i + jm * jm + qm * qm) * dx <= R ||
-                sqrt(i * i + qm * qm + j * j) * dx <= R ||
-                sqrt(im * im + j * j + q * q) * dx <= R ||
-                sqrt(im * im + jm * jm + q * q) * dx <= R ||
-                sqrt(im * im + jm * jm + qm * qm) * dx <= R ||
-                sqrt(im * im + j * j + qm * qm) * dx <= R;
-            w->top[i * N * N + j * N + q] = in ? 1.0f : 0.0f;
-          }
-      fftwf_execute(w->f_top); /* :372 */
-      fftwf_execute(w->f_bub); /* :373 */
-      /* complex product :379-381 (float complex *= float complex) */
-      float *bc = (float *)w->bub_c;
-      const float *tc = (const float *)w->top_c;
-#pragma omp parallel for num_threads(p->nthreads) schedule(static)
-      for (long i = 0; i < w->Nh; i++) {
-        float a = bc[2 * i], b = bc[2 * i + 1], c = tc[2 * i], d = tc[2 * i + 1];
-        float ac = a * c, bd = b * d, ad = a * d, bcv = b * c;
-        bc[2 * i] = ac - bd;
-        bc[2 * i + 1] = ad + bcv;
-      }
-      fftwf_execute(w->i_bub); /* :382 */
-      /* threshold :390-393 */
-#pragma omp parallel for num_threads(p->nthreads) schedule(static)
-      for (long i = 0; i < N3; i++) {
-        w->bub[i] = (float)((double)w->bub[i] * dx3 / (double)N3);
-        if ((double)w->bub[i] > dx3 / 100) w->fill[i] = 1.0f;
-      }
-    }
+    radius_fft(w, p, R);
     R /= bf;
   }
 
   while (R >= dx && done++ < cap) {
-    filter_spectra(w, p, R);
-    fftwf_execute(w->i_rec);
-    fftwf_execute(w->i_ion);
-    const long nc = (long)(R / dx); /* :428 */
-    /* painting :433-458; concurrent writers all store 1.0 */
-#pragma omp parallel for num_threads(p->nthreads) schedule(static)
-    for (long ic = 0; ic < N; ic++)
-      for (long jc = 0; jc < N; jc++)
-        for (long kc = 0; kc < N; kc++) {
-          long c = ic * N * N + jc * N + kc;
-          float h = w->ion[c], d = w->rec[c];
-          if (!(h > 0.)) continue;
-          if (!(!(d > 0.) || ((double)h / d >= 1.0))) continue;
-          for (long a = -(nc + 1); a <= nc + 1; a++) {
-            long ai = wrap_index(ic + a, N);
-            for (long b = -(nc + 1); b <= nc + 1; b++) {
-              if (!(sqrt(a * a + b * b) * dx <= R)) continue;
-              long bi = wrap_index(jc + b, N);
-              for (long e = -(nc + 1); e <= nc + 1; e++) {
-                long ei = wrap_index(kc + e, N);
-                if (sqrt(a * a + b * b + e * e) * dx <= R)
-                  w->fill[ai * N * N + bi * N + ei] = 1.0f;
-              }
-            }
-          }
-        }
+    radius_small(w, p, R);
     R /= bf;
   }
 
@@ -362,7 +379,48 @@ static int run_common(const sf21o_params *p, double z, const float *delta,
   if (rec0) memcpy(rec0, w.rec, sizeof(float) * w.N3);
   if (ion0) memcpy(ion0, w.ion, sizeof(float) * w.N3);
   if (fill0) memcpy(fill0, w.fill, sizeof(float) * w.N3);
-  bubble_loops(&w, p, xhii, neutral);
+  if (p->max_radii < 0)
+    memcpy(xhii, w.fill, sizeof(float) * w.N3);
+  else
+    bubble_loops(&w, p, xhii, neutral);
+  work_free(&w);
+  return 0;
+}
+
+/* CPU-baseline timing sample (SFR branch): the front of one redshift --
+ * prologue, source conversion, single-cell fill and both forward transforms
+ * (:216-291) -- timed once, then the loop body of each listed radius index
+ * on its own (a radius's body depends on the others only through the fill
+ * box, which it only sets), timed one by one.  Wall times in seconds. */
+int sf21o_time_radii(const sf21o_params *p, double z, const float *delta,
+                     const float *sfrd, const int *ridx, int n,
+                     double *t_front, double *t_radius) {
+  double R[512];
+  int n_fft = 0;
+  const int nr = sf21o_radii(p, R, 512, &n_fft);
+  for (int k = 0; k < n; k++)
+    if (ridx[k] < 0 || ridx[k] >= nr || nr > 512) return 2;
+  work_t w;
+  if (work_init(&w, p)) return 1;
+  const double t0 = omp_get_wtime();
+  prologue(&w, p, z, delta);
+  const double dx = cell_size(p);
+  const double q = sf21o_Qion(z);
+#pragma omp parallel for num_threads(p->nthreads) schedule(static)
+  for (long i = 0; i < w.N3; i++)
+    w.ion[i] = (float)(sfrd[i] * dx * dx * dx * q * p->fesc);
+  single_cell_fill(&w, p);
+  fftwf_execute(w.f_rec);
+  fftwf_execute(w.f_ion);
+  *t_front = omp_get_wtime() - t0;
+  for (int k = 0; k < n; k++) {
+    const double t1 = omp_get_wtime();
+    if (ridx[k] < n_fft)
+      radius_fft(&w, p, R[ridx[k]]);
+    else
+      radius_small(&w, p, R[ridx[k]]);
+    t_radius[k] = omp_get_wtime() - t1;
+  }
   work_free(&w);
   return 0;
 }

@@ -28,7 +28,9 @@ typedef struct {
   double fesc;   /* global_fesc (the efficiency zeta) */
   int nthreads;  /* global_nthreads */
   int max_radii; /* 0 = the full radius schedule; n > 0 stops both loops
-                    after the first n radii (a bounded CPU timing sample) */
+                    after the first n radii (a bounded CPU timing sample);
+                    n < 0 runs the prologue, source conversion and
+                    single-cell fill only (xhii = the uncapped fill) */
 } sf21o_params;
 
 /* Mirrors Halo_t (auxiliary.h:13-17). */
@@ -48,6 +50,14 @@ int sf21o_radii(const sf21o_params *p, double *R, int cap, int *n_fft);
  * fill0 (single-cell fill before the radius loops).
  * *neutral receives the mean neutral fraction (:473-477).
  * Returns 0 on success, nonzero on allocation or plan failure. */
+/* CPU-baseline timing sample: the front of one redshift (prologue, source
+ * conversion, fill, forward transforms) and then the loop body of each
+ * radius index ridx[0..n) on its own; wall seconds in *t_front and
+ * t_radius[k]. */
+int sf21o_time_radii(const sf21o_params *p, double z, const float *delta,
+                     const float *sfrd, const int *ridx, int n,
+                     double *t_front, double *t_radius);
+
 int sf21o_run_z_sfr(const sf21o_params *p, double z, const float *delta,
                     const float *sfrd, float *xhii, float *fresid, float *rec0,
                     float *ion0, float *fill0, double *neutral);

@@ -46,6 +46,8 @@ def lib():
                                       ctypes.POINTER(ctypes.c_double)]
         L.sf21o_run_z_rion.argtypes = [ctypes.POINTER(_Params), ctypes.c_double, f, f, f, f, f, f,
                                        ctypes.POINTER(ctypes.c_double)]
+        L.sf21o_time_radii.argtypes = [ctypes.POINTER(_Params), ctypes.c_double, f, f, f, ctypes.c_int,
+                                       ctypes.POINTER(ctypes.c_double), f]
         L.sf21o_filtered.argtypes = [ctypes.POINTER(_Params), f, f, ctypes.c_double, f, f]
         L.sf21o_halo_source.argtypes = [ctypes.POINTER(_Params), ctypes.c_double, ctypes.c_long, f, f]
         L.sf21o_halo_smoothed.argtypes = [ctypes.POINTER(_Params), ctypes.c_double, ctypes.c_long, f, f]
@@ -90,6 +92,22 @@ def run_z_sfr(p: _Params, z: float, delta: np.ndarray, sfrd: np.ndarray, extras:
         for k, e in zip(("fresid", "rec0", "ion0", "fill0"), ex):
             out[k] = e.reshape(shp)
     return out
+
+
+def time_radii(p: _Params, z: float, delta: np.ndarray, sfrd: np.ndarray, ridx):
+    """(front seconds, [seconds per listed radius index]) of the restatement:
+    the prologue, fill and forward transforms once, then each radius's loop
+    body on its own (the CPU-baseline sample)."""
+    delta = np.ascontiguousarray(delta, dtype=np.float32)
+    sfrd = np.ascontiguousarray(sfrd, dtype=np.float32)
+    idx = np.ascontiguousarray(ridx, dtype=np.int32)
+    t = np.zeros(len(idx), np.float64)
+    front = ctypes.c_double(0.0)
+    rc = lib().sf21o_time_radii(ctypes.byref(p), z, _ptr(delta), _ptr(sfrd), _ptr(idx), len(idx),
+                                ctypes.byref(front), _ptr(t))
+    if rc:
+        raise RuntimeError(f"oracle sf21o_time_radii failed ({rc})")
+    return front.value, [float(v) for v in t]
 
 
 def run_z_rion(p: _Params, z: float, delta: np.ndarray, rion_box: np.ndarray):

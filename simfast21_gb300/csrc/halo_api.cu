@@ -635,17 +635,17 @@ extern "C" int sf21_halo_create(const sf21_halo_config* cfg, sf21_halo_ctx** out
     HCREATE(hf_setup(N));
   }
   const size_t box_c = sizeof(float2) * c->n3, bits = sizeof(uint32_t) * c->nwords;
-  HCREATE(cudaMalloc(&c->d_spec, box_c));
-  HCREATE(cudaMalloc(&c->d_work, box_c * c->KP));
-  HCREATE(cudaMalloc(&c->d_delta, sizeof(float) * c->n3));
-  HCREATE(cudaMalloc(&c->d_FL, bits));
-  HCREATE(cudaMalloc(&c->d_UND, bits));
-  HCREATE(cudaMalloc(&c->d_ACC, bits));
-  HCREATE(cudaMalloc(&c->d_bits, bits));
+  HCREATE(dev_malloc(&c->d_spec, box_c));
+  HCREATE(dev_malloc(&c->d_work, box_c * c->KP));
+  HCREATE(dev_malloc(&c->d_delta, sizeof(float) * c->n3));
+  HCREATE(dev_malloc(&c->d_FL, bits));
+  HCREATE(dev_malloc(&c->d_UND, bits));
+  HCREATE(dev_malloc(&c->d_ACC, bits));
+  HCREATE(dev_malloc(&c->d_bits, bits));
   HCREATE(cudaMemset(c->d_UND, 0, bits));
   HCREATE(cudaMemset(c->d_ACC, 0, bits));
-  HCREATE(cudaMalloc(&c->d_chunk, sizeof(uint32_t) * hf_compact_chunks(c->nwords)));
-  HCREATE(cudaMalloc(&c->d_cnt, sizeof(uint32_t) * 4));
+  HCREATE(dev_malloc(&c->d_chunk, sizeof(uint32_t) * hf_compact_chunks(c->nwords)));
+  HCREATE(dev_malloc(&c->d_cnt, sizeof(uint32_t) * 4));
   HCREATE(cudaMallocHost(&c->h_cnt, sizeof(uint32_t) * 4));
   std::vector<float2> tw(N);
   if (c->gen) {  // plain table exp(-2 pi i t / N)
@@ -658,7 +658,7 @@ extern "C" int sf21_halo_create(const sf21_halo_config* cfg, sf21_halo_ctx** out
     twiddle_layout(N, tre.data(), tim.data());
     for (int t = 0; t < N; ++t) tw[t] = make_float2((float)tre[t], (float)tim[t]);
   }
-  HCREATE(cudaMalloc(&c->d_tw, sizeof(float2) * N));
+  HCREATE(dev_malloc(&c->d_tw, sizeof(float2) * N));
   HCREATE(cudaMemcpy(c->d_tw, tw.data(), sizeof(float2) * N, cudaMemcpyHostToDevice));
 #undef HCREATE
   *out = c;
@@ -736,9 +736,9 @@ static int ensure_list(sf21_halo_ctx* c, long n) {
   c->d_list = c->d_list2 = nullptr;
   c->d_status = nullptr;
   c->list_cap = 0;
-  HCTX_CUDA(c, cudaMalloc(&c->d_list, sizeof(uint32_t) * cap));
-  HCTX_CUDA(c, cudaMalloc(&c->d_list2, sizeof(uint32_t) * cap));
-  HCTX_CUDA(c, cudaMalloc(&c->d_status, cap));
+  HCTX_CUDA(c, dev_malloc(&c->d_list, sizeof(uint32_t) * cap));
+  HCTX_CUDA(c, dev_malloc(&c->d_list2, sizeof(uint32_t) * cap));
+  HCTX_CUDA(c, dev_malloc(&c->d_status, cap));
   c->list_cap = cap;
   return SF21_OK;
 }
@@ -747,7 +747,7 @@ static int ensure_cat(sf21_halo_ctx* c, long n) {
   if (n <= c->cat_cap) return SF21_OK;
   const long cap = std::max(n, std::max(2 * c->cat_cap, (long)1 << 16));
   float4* p = nullptr;
-  HCTX_CUDA(c, cudaMalloc(&p, sizeof(float4) * cap));
+  HCTX_CUDA(c, dev_malloc(&p, sizeof(float4) * cap));
   if (c->d_cat) {
     if (c->cat_n) HCTX_CUDA(c, cudaMemcpyAsync(p, c->d_cat, sizeof(float4) * c->cat_n, cudaMemcpyDeviceToDevice,
                                                c->stream));
@@ -829,7 +829,7 @@ static int grow(sf21_halo_ctx* c, T** p, long n, long* cap, bool keep_cap_var = 
   if (n <= *cap && *p) return SF21_OK;
   if (*p) cudaFree(*p);
   *p = nullptr;
-  HCTX_CUDA(c, cudaMalloc(p, sizeof(T) * (size_t)std::max(n, 1L)));
+  HCTX_CUDA(c, dev_malloc(p, sizeof(T) * (size_t)std::max(n, 1L)));
   *cap = std::max(n, 1L);
   return SF21_OK;
 }
@@ -850,12 +850,12 @@ static int sg_tables(sf21_halo_ctx* c) {
       for (int k = 0; k < 32; ++k) loc[((size_t)cc * 32 + k) * SG_LOCAL + i] = acc.col[cc][k];
     acc = taus_mul(t4, acc);
   }
-  HCTX_CUDA(c, cudaMalloc(&c->d_sg_pow2, sizeof(uint32_t) * p2.size()));
-  HCTX_CUDA(c, cudaMalloc(&c->d_sg_local, sizeof(uint32_t) * loc.size()));
+  HCTX_CUDA(c, dev_malloc(&c->d_sg_pow2, sizeof(uint32_t) * p2.size()));
+  HCTX_CUDA(c, dev_malloc(&c->d_sg_local, sizeof(uint32_t) * loc.size()));
   HCTX_CUDA(c, cudaMemcpy(c->d_sg_pow2, p2.data(), sizeof(uint32_t) * p2.size(), cudaMemcpyHostToDevice));
   HCTX_CUDA(c, cudaMemcpy(c->d_sg_local, loc.data(), sizeof(uint32_t) * loc.size(), cudaMemcpyHostToDevice));
-  HCTX_CUDA(c, cudaMalloc(&c->d_sg_u64, sizeof(uint64_t) * 4));
-  HCTX_CUDA(c, cudaMalloc(&c->d_sg_err, sizeof(int) * 3));
+  HCTX_CUDA(c, dev_malloc(&c->d_sg_u64, sizeof(uint64_t) * 4));
+  HCTX_CUDA(c, dev_malloc(&c->d_sg_err, sizeof(int) * 3));
   return SF21_OK;
 }
 
@@ -874,7 +874,7 @@ static int subgrid_cycle(sf21_halo_ctx* c, const Cosmo& cs, double z, double gro
   double R = pow(3 / 4.0 / kPI / rhom * M, 1.0 / 3);
   // unflagged cells: per-word counts -> exclusive prefix (select by binary search)
   long wcap = c->nwords;
-  if (!c->d_sg_wpre) HCTX_CUDA(c, cudaMalloc(&c->d_sg_wpre, sizeof(uint32_t) * c->nwords));
+  if (!c->d_sg_wpre) HCTX_CUDA(c, dev_malloc(&c->d_sg_wpre, sizeof(uint32_t) * c->nwords));
   (void)wcap;
   if ((rc = sg_chunk(c, c->nwords))) return rc;
   HCTX_CUDA(c, launch_sg_free_count(c->d_FL, c->nwords, c->d_sg_wpre, st));
@@ -931,21 +931,21 @@ static int subgrid_cycle(sf21_halo_ctx* c, const Cosmo& cs, double z, double gro
           c->d_sgLB = nullptr;
           c->sg_eb = SgEntryBufs{};
           c->sg_blocks_cap = 0;
-          HCTX_CUDA(c, cudaMalloc(&c->d_sgX, (size_t)nb * SG_LMAX));
-          HCTX_CUDA(c, cudaMalloc(&c->d_sgD, sizeof(uint16_t) * (size_t)nb * SG_LMAX));
-          HCTX_CUDA(c, cudaMalloc(&c->d_sg_cnt, sizeof(uint32_t) * (size_t)nb));
-          HCTX_CUDA(c, cudaMalloc(&c->d_sg_start, sizeof(uint32_t) * 3 * (size_t)nb));
-          HCTX_CUDA(c, cudaMalloc(&c->d_sgLB, sizeof(uint32_t) * (SG_B / 32) * (size_t)nb));
-          HCTX_CUDA(c, cudaMalloc(&c->sg_eb.gx, (size_t)ng * SG_LMAX));
-          HCTX_CUDA(c, cudaMalloc(&c->sg_eb.gd, sizeof(uint32_t) * (size_t)ng * SG_LMAX));
-          HCTX_CUDA(c, cudaMalloc(&c->sg_eb.sx, (size_t)ns * SG_LMAX));
-          HCTX_CUDA(c, cudaMalloc(&c->sg_eb.sd, sizeof(uint32_t) * (size_t)ns * SG_LMAX));
-          HCTX_CUDA(c, cudaMalloc(&c->sg_eb.sentry, (size_t)ns));
-          HCTX_CUDA(c, cudaMalloc(&c->sg_eb.sbase, sizeof(uint64_t) * (size_t)(ns + 1)));
-          HCTX_CUDA(c, cudaMalloc(&c->sg_eb.gentry, (size_t)ng));
-          HCTX_CUDA(c, cudaMalloc(&c->sg_eb.gbase, sizeof(uint64_t) * (size_t)ng));
-          HCTX_CUDA(c, cudaMalloc(&c->sg_eb.bentry, (size_t)nb));
-          HCTX_CUDA(c, cudaMalloc(&c->sg_eb.bbase, sizeof(uint64_t) * (size_t)nb));
+          HCTX_CUDA(c, dev_malloc(&c->d_sgX, (size_t)nb * SG_LMAX));
+          HCTX_CUDA(c, dev_malloc(&c->d_sgD, sizeof(uint16_t) * (size_t)nb * SG_LMAX));
+          HCTX_CUDA(c, dev_malloc(&c->d_sg_cnt, sizeof(uint32_t) * (size_t)nb));
+          HCTX_CUDA(c, dev_malloc(&c->d_sg_start, sizeof(uint32_t) * 3 * (size_t)nb));
+          HCTX_CUDA(c, dev_malloc(&c->d_sgLB, sizeof(uint32_t) * (SG_B / 32) * (size_t)nb));
+          HCTX_CUDA(c, dev_malloc(&c->sg_eb.gx, (size_t)ng * SG_LMAX));
+          HCTX_CUDA(c, dev_malloc(&c->sg_eb.gd, sizeof(uint32_t) * (size_t)ng * SG_LMAX));
+          HCTX_CUDA(c, dev_malloc(&c->sg_eb.sx, (size_t)ns * SG_LMAX));
+          HCTX_CUDA(c, dev_malloc(&c->sg_eb.sd, sizeof(uint32_t) * (size_t)ns * SG_LMAX));
+          HCTX_CUDA(c, dev_malloc(&c->sg_eb.sentry, (size_t)ns));
+          HCTX_CUDA(c, dev_malloc(&c->sg_eb.sbase, sizeof(uint64_t) * (size_t)(ns + 1)));
+          HCTX_CUDA(c, dev_malloc(&c->sg_eb.gentry, (size_t)ng));
+          HCTX_CUDA(c, dev_malloc(&c->sg_eb.gbase, sizeof(uint64_t) * (size_t)ng));
+          HCTX_CUDA(c, dev_malloc(&c->sg_eb.bentry, (size_t)nb));
+          HCTX_CUDA(c, dev_malloc(&c->sg_eb.bbase, sizeof(uint64_t) * (size_t)nb));
           c->sg_blocks_cap = nb;
         }
         HCTX_CUDA(c, cudaMemsetAsync(c->d_sg_err, 0, sizeof(int) * 3, st));
@@ -1093,14 +1093,14 @@ extern "C" int sf21_halo_find_z(sf21_halo_ctx* c, double z, long* nhalos) {
     if (c->d_runs) cudaFree(c->d_runs);
     c->d_runs = nullptr;
     c->runs_cap = 0;
-    HCTX_CUDA(c, cudaMalloc(&c->d_runs, sizeof(int4) * std::max<size_t>(table.size(), 1)));
+    HCTX_CUDA(c, dev_malloc(&c->d_runs, sizeof(int4) * std::max<size_t>(table.size(), 1)));
     c->runs_cap = (long)std::max<size_t>(table.size(), 1);
   }
   if (!table.empty())
     HCTX_CUDA(c, cudaMemcpyAsync(c->d_runs, table.data(), sizeof(int4) * table.size(), cudaMemcpyHostToDevice, st));
   while ((int)c->d_masks.size() < nact) {
     uint32_t* p = nullptr;
-    HCTX_CUDA(c, cudaMalloc(&p, sizeof(uint32_t) * c->nwords));
+    HCTX_CUDA(c, dev_malloc(&p, sizeof(uint32_t) * c->nwords));
     c->d_masks.push_back(p);
   }
   // flags of this redshift (:181-182); the per-mass working sets start empty

@@ -20,6 +20,7 @@
 #include <sys/stat.h>
 #include <stdlib.h>
 
+#include <atomic>
 #include <string>
 #include <thread>
 #include <vector>
@@ -62,6 +63,21 @@ struct SetInfo {
 }  // namespace
 
 namespace sf21 {
+// Allocation-failure injection (sf21_hii_inject_alloc_failure): the n-th
+// device allocation after arming fails once.
+static std::atomic<long> g_fail_alloc_in{0};
+
+cudaError_t dev_malloc(void** p, size_t bytes) {
+  long n = g_fail_alloc_in.load();
+  while (n > 0 && !g_fail_alloc_in.compare_exchange_weak(n, n - 1)) {
+  }
+  if (n == 1) {
+    *p = nullptr;
+    return cudaErrorMemoryAllocation;
+  }
+  return cudaMalloc(p, bytes);
+}
+
 // Qion(z) (user_functions.c:84-88), shared with the star-formation-rate stage.
 double host_Qion(double z) { return pow(10.0, 2.05707274e-02 * z + 5.29944413e+01) / 1.e+45; }
 }  // namespace sf21
@@ -95,6 +111,7 @@ struct sf21_hii_ctx {
   } gkey = {0, -1, nullptr, nullptr, nullptr, nullptr};
   PipeMaps pmaps;
   int* d_err = nullptr;
+  uint32_t wait_limit = 0;  // polls per bounded device wait (0 = the kernels' default)
   int nsm = 0;
   std::vector<SetInfo> sets;
   cudaStream_t stream = nullptr;
@@ -260,12 +277,12 @@ static void tune_cache_store(const std::string& key, const double* ms, int npath
     return (code);                                                \
   } while (0)
 
-#define CTX_CUDA(ctx, call)                                                                  \
-  do {                                                                                       \
-    cudaError_t _e = (call);                                                                 \
-    if (_e != cudaSuccess)                                                                   \
-      CTX_FAIL(ctx, SF21_E_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(_e), \
-               __FILE__, __LINE__);                                                          \
+#define CTX_CUDA(ctx, call)                                                                        \
+  do {                                                                                             \
+    cudaError_t _e = (call);                                                                       \
+    if (_e != cudaSuccess)                                                                         \
+      CTX_FAIL(ctx, _e == cudaErrorMemoryAllocation ? SF21_E_ALLOC : SF21_E_CUDA, "%s failed: %s (%s:%d)", \
+               #call, cudaGetErrorString(_e), __FILE__, __LINE__);                                 \
   } while (0)
 
 static int nmax_of(double R, double dx) {
@@ -426,24 +443,24 @@ extern "C" int sf21_hii_create(const sf21_hii_config* cfg, sf21_hii_ctx** out) {
     CREATE_CUDA(adj_setup((int)N));
   }
   CREATE_CUDA(dt_setup((int)N));
-  CREATE_CUDA(cudaMalloc(&c->d_delta, box_f));
-  CREATE_CUDA(cudaMalloc(&c->d_src, box_f));
-  CREATE_CUDA(cudaMalloc(&c->d_rec0, box_f));
-  CREATE_CUDA(cudaMalloc(&c->d_fres, box_f));
-  CREATE_CUDA(cudaMalloc(&c->d_chain, sizeof(uint64_t) * c->n3));
-  CREATE_CUDA(cudaMalloc(&c->d_om, sizeof(float2) * c->n3));
-  CREATE_CUDA(cudaMalloc(&c->d_xhii, box_f));
-  CREATE_CUDA(cudaMalloc(&c->d_spec, box_c));
-  CREATE_CUDA(cudaMalloc(&c->d_rc, c->n3));
+  CREATE_CUDA(dev_malloc(&c->d_delta, box_f));
+  CREATE_CUDA(dev_malloc(&c->d_src, box_f));
+  CREATE_CUDA(dev_malloc(&c->d_rec0, box_f));
+  CREATE_CUDA(dev_malloc(&c->d_fres, box_f));
+  CREATE_CUDA(dev_malloc(&c->d_chain, sizeof(uint64_t) * c->n3));
+  CREATE_CUDA(dev_malloc(&c->d_om, sizeof(float2) * c->n3));
+  CREATE_CUDA(dev_malloc(&c->d_xhii, box_f));
+  CREATE_CUDA(dev_malloc(&c->d_spec, box_c));
+  CREATE_CUDA(dev_malloc(&c->d_rc, c->n3));
   c->d_work.assign(K, nullptr);
-  CREATE_CUDA(cudaMalloc(&c->d_work_base, box_c * K));
+  CREATE_CUDA(dev_malloc(&c->d_work_base, box_c * K));
   for (int k = 0; k < K; ++k) c->d_work[k] = c->d_work_base + (size_t)k * c->n3;
-  CREATE_CUDA(cudaMalloc(&c->d_err, sizeof(int)));
+  CREATE_CUDA(dev_malloc(&c->d_err, sizeof(int)));
   CREATE_CUDA(cudaMemset(c->d_err, 0, sizeof(int)));
   CREATE_CUDA(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, c->device));
   c->pro_blocks = prologue_blocks(c->n3);
-  CREATE_CUDA(cudaMalloc(&c->d_partials, sizeof(float) * 2 * c->pro_blocks));
-  CREATE_CUDA(cudaMalloc(&c->d_alpha, sizeof(float)));
+  CREATE_CUDA(dev_malloc(&c->d_partials, sizeof(float) * 2 * c->pro_blocks));
+  CREATE_CUDA(dev_malloc(&c->d_alpha, sizeof(float)));
   // twiddles exp(-2 pi i t / N) in double, rounded once (stage layout for the
   // register transforms, plain table for the shared-memory ones)
   std::vector<float2> tw(N);
@@ -457,10 +474,10 @@ extern "C" int sf21_hii_create(const sf21_hii_config* cfg, sf21_hii_ctx** out) {
     twiddle_layout((int)N, tre.data(), tim.data());
     for (long t = 0; t < N; ++t) tw[t] = make_float2((float)tre[t], (float)tim[t]);
   }
-  CREATE_CUDA(cudaMalloc(&c->d_tw, sizeof(float2) * N));
+  CREATE_CUDA(dev_malloc(&c->d_tw, sizeof(float2) * N));
   CREATE_CUDA(cudaMemcpy(c->d_tw, tw.data(), sizeof(float2) * N, cudaMemcpyHostToDevice));
   for (SetInfo& s : c->sets) {
-    CREATE_CUDA(cudaMalloc(&s.d_nmax, sizeof(int) * s.nmax.size()));
+    CREATE_CUDA(dev_malloc(&s.d_nmax, sizeof(int) * s.nmax.size()));
     CREATE_CUDA(cudaMemcpy(s.d_nmax, s.nmax.data(), sizeof(int) * s.nmax.size(), cudaMemcpyHostToDevice));
   }
   // path: explicit, or tuned by timing one K-radius batch of each variant
@@ -640,11 +657,11 @@ static int enqueue_batch(sf21_hii_ctx* c, const Batch& bt, cudaStream_t st) {
       CTX_CUDA(c, launch_cols_b_cb(N, bt, c->d_tw, st));
     else
       CTX_CUDA(c, launch_pipe(N, 0, 1, c->pmaps, bt, c->d_work_base, c->d_rc, c->d_alpha, c->d_tw, c->d_err,
-                              c->nsm, st));
+                              c->nsm, st, c->wait_limit));
     int e2 = mark(c, st);
     if (c->path == 7)
       CTX_CUDA(c, launch_pipe(N, 1, 1, c->pmaps, bt, c->d_work_base, c->d_rc, c->d_alpha, c->d_tw, c->d_err,
-                              c->nsm, st));
+                              c->nsm, st, c->wait_limit));
     else
       CTX_CUDA(c, launch_cols_a_test_cb(N, bt, c->d_rc, c->d_alpha, c->d_tw, c->nsm, st));
     int e3 = mark(c, st);
@@ -658,11 +675,11 @@ static int enqueue_batch(sf21_hii_ctx* c, const Batch& bt, cudaStream_t st) {
     CTX_CUDA(c, x_inv_rows_filter(c, c->d_spec, bt, st));
     int e1 = mark(c, st);
     CTX_CUDA(c, launch_pipe(N, 0, 0, c->pmaps, bt, c->d_work_base, c->d_rc, c->d_alpha, c->d_tw, c->d_err, c->nsm,
-                            st));
+                            st, c->wait_limit));
     int e2 = mark(c, st);
     if (c->path == 4)
       CTX_CUDA(c, launch_pipe(N, 1, 0, c->pmaps, bt, c->d_work_base, c->d_rc, c->d_alpha, c->d_tw, c->d_err,
-                              c->nsm, st));
+                              c->nsm, st, c->wait_limit));
     else
       CTX_CUDA(c, x_cols_a_test(c, bt, st));
     int e3 = mark(c, st);
@@ -805,7 +822,7 @@ static int run_sets_to_host(sf21_hii_ctx* c, cudaStream_t st, float* xhii, doubl
       CTX_CUDA(c, cudaEventCreateWithFlags(&c->ev_copied[i], cudaEventDisableTiming));
     }
   }
-  if (!c->d_xhii2) CTX_CUDA(c, cudaMalloc(&c->d_xhii2, bf));
+  if (!c->d_xhii2) CTX_CUDA(c, dev_malloc(&c->d_xhii2, bf));
   float* stage[2] = {c->d_xhii, c->d_xhii2};
   std::vector<std::thread> sums;
   int status = SF21_OK;
@@ -993,9 +1010,9 @@ extern "C" int sf21_hii_run_z_plain_device(sf21_hii_ctx* c, double z, int kind, 
   cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
   const int N = (int)c->N;
   const long n3 = c->n3;
-  if (!c->d_mask) CTX_CUDA(c, cudaMalloc(&c->d_mask, sizeof(float) * n3));
-  if (!c->d_flag) CTX_CUDA(c, cudaMalloc(&c->d_flag, sizeof(int)));
-  if (!c->d_box2) CTX_CUDA(c, cudaMalloc(&c->d_box2, sizeof(float2) * n3));
+  if (!c->d_mask) CTX_CUDA(c, dev_malloc(&c->d_mask, sizeof(float) * n3));
+  if (!c->d_flag) CTX_CUDA(c, dev_malloc(&c->d_flag, sizeof(int)));
+  if (!c->d_box2) CTX_CUDA(c, dev_malloc(&c->d_box2, sizeof(float2) * n3));
   if ((rc = enqueue_front(c, z, kind, delta_dev, src_dev, st))) return rc;
   const SetInfo& s = c->sets[set];
   // single-cell fill (:281-288) into the output box
@@ -1055,6 +1072,23 @@ static int check_device_flag(sf21_hii_ctx* c) {
   return SF21_OK;
 }
 
+extern "C" int sf21_hii_inject_alloc_failure(long n) {
+  if (n < 0) return SF21_E_ARG;
+  sf21::g_fail_alloc_in.store(n);
+  return SF21_OK;
+}
+
+extern "C" int sf21_hii_set_wait_limit(sf21_hii_ctx* c, unsigned int polls) {
+  if (!c) return SF21_E_ARG;
+  c->wait_limit = polls;
+  // the captured graph holds the old limit in its kernel arguments
+  if (c->gexec) {
+    cudaGraphExecDestroy(c->gexec);
+    c->gexec = nullptr;
+  }
+  return SF21_OK;
+}
+
 extern "C" int sf21_hii_check(sf21_hii_ctx* c) {
   if (!c) return SF21_E_ARG;
   CTX_CUDA(c, cudaSetDevice(c->device));
@@ -1066,8 +1100,8 @@ extern "C" int sf21_hii_check(sf21_hii_ctx* c) {
 static int ensure_adj_buffers(sf21_hii_ctx* c) {
   if (c->gen) CTX_FAIL(c, SF21_E_UNSUPPORTED, "the criterion and its adjoint need a power-of-two box side");
   const long n3 = c->n3;
-  if (!c->d_C) CTX_CUDA(c, cudaMalloc(&c->d_C, sizeof(float) * n3));
-  if (!c->d_A) CTX_CUDA(c, cudaMalloc(&c->d_A, n3));
+  if (!c->d_C) CTX_CUDA(c, dev_malloc(&c->d_C, sizeof(float) * n3));
+  if (!c->d_A) CTX_CUDA(c, dev_malloc(&c->d_A, n3));
   return SF21_OK;
 }
 
@@ -1146,8 +1180,8 @@ extern "C" int sf21_hii_vjp_device(sf21_hii_ctx* c, double z, int kind, const fl
   const int N = (int)c->N;
   const long n3 = c->n3;
   const int nzp = adj_zpart_blocks(N);
-  if (!c->d_acc) CTX_CUDA(c, cudaMalloc(&c->d_acc, sizeof(float2) * n3));
-  if (!c->d_zpart) CTX_CUDA(c, cudaMalloc(&c->d_zpart, sizeof(float) * nzp));
+  if (!c->d_acc) CTX_CUDA(c, dev_malloc(&c->d_acc, sizeof(float2) * n3));
+  if (!c->d_zpart) CTX_CUDA(c, dev_malloc(&c->d_zpart, sizeof(float) * nzp));
   // recompute the spectrum (the checkpoint holds only the argmax index)
   if ((rc = enqueue_front(c, z, kind, delta_dev, src_dev, st))) return rc;
   CTX_CUDA(c, cudaMemsetAsync(c->d_acc, 0, sizeof(float2) * n3, st));
@@ -1217,9 +1251,9 @@ extern "C" int sf21_hii_vjp(sf21_hii_ctx* c, double z, int kind, const float* de
   if (rc) return rc;
   CTX_CUDA(c, cudaSetDevice(c->device));
   const size_t bf = sizeof(float) * c->n3;
-  if (!c->d_g) CTX_CUDA(c, cudaMalloc(&c->d_g, bf));
-  if (ddelta && !c->d_gd) CTX_CUDA(c, cudaMalloc(&c->d_gd, bf));
-  if (dsrc && !c->d_gs) CTX_CUDA(c, cudaMalloc(&c->d_gs, bf));
+  if (!c->d_g) CTX_CUDA(c, dev_malloc(&c->d_g, bf));
+  if (ddelta && !c->d_gd) CTX_CUDA(c, dev_malloc(&c->d_gd, bf));
+  if (dsrc && !c->d_gs) CTX_CUDA(c, dev_malloc(&c->d_gs, bf));
   CTX_CUDA(c, cudaMemcpyAsync(c->d_delta, delta, bf, cudaMemcpyHostToDevice, c->stream));
   CTX_CUDA(c, cudaMemcpyAsync(c->d_src, src, bf, cudaMemcpyHostToDevice, c->stream));
   CTX_CUDA(c, cudaMemcpyAsync(c->d_g, dC, bf, cudaMemcpyHostToDevice, c->stream));
@@ -1239,7 +1273,7 @@ static int enqueue_halo_source(sf21_hii_ctx* c, double z, long nhalos, const voi
   if (c->N_halo < c->N) CTX_FAIL(c, SF21_E_ARG, "N_halo < N_smoothed (smooth_box, auxiliary.c:651-654)");
   if (nhalos >= (1L << 28)) CTX_FAIL(c, SF21_E_UNSUPPORTED, "2^28 halos or more (8 CIC entries each, int count)");
   const long nh3 = c->N_halo * c->N_halo * c->N_halo;
-  if (!c->d_fine) CTX_CUDA(c, cudaMalloc(&c->d_fine, sizeof(float) * nh3));
+  if (!c->d_fine) CTX_CUDA(c, dev_malloc(&c->d_fine, sizeof(float) * nh3));
   if (nhalos > c->halo_cap) {
     if (c->d_halos) cudaFree(c->d_halos);
     if (c->d_hscratch) cudaFree(c->d_hscratch);
@@ -1247,9 +1281,9 @@ static int enqueue_halo_source(sf21_hii_ctx* c, double z, long nhalos, const voi
     c->d_hscratch = nullptr;
     c->halo_cap = 0;
     const long cap = nhalos + nhalos / 4 + 1024;
-    CTX_CUDA(c, cudaMalloc(&c->d_halos, (size_t)cap * 16));
+    CTX_CUDA(c, dev_malloc(&c->d_halos, (size_t)cap * 16));
     c->hscratch_bytes = halo_scratch_bytes(cap);
-    CTX_CUDA(c, cudaMalloc(&c->d_hscratch, c->hscratch_bytes));
+    CTX_CUDA(c, dev_malloc(&c->d_hscratch, c->hscratch_bytes));
     c->halo_cap = cap;
   }
   if (nhalos > 0)
@@ -1298,10 +1332,10 @@ static int power_spectrum_device(sf21_hii_ctx* c, const float* box_dev, int flag
   const int N = (int)c->N;
   const int nk = pk_nbins(N);
   const int grid = pk_bin_grid(N);
-  if (!c->d_pk) CTX_CUDA(c, cudaMalloc(&c->d_pk, sizeof(float2) * c->n3));
-  if (!c->d_pk_w) CTX_CUDA(c, cudaMalloc(&c->d_pk_w, sizeof(float) * N));
-  if (!c->d_pk_part) CTX_CUDA(c, cudaMalloc(&c->d_pk_part, sizeof(float) * (size_t)grid * nk));
-  if (!c->d_pk_cnt) CTX_CUDA(c, cudaMalloc(&c->d_pk_cnt, sizeof(unsigned long long) * nk));
+  if (!c->d_pk) CTX_CUDA(c, dev_malloc(&c->d_pk, sizeof(float2) * c->n3));
+  if (!c->d_pk_w) CTX_CUDA(c, dev_malloc(&c->d_pk_w, sizeof(float) * N));
+  if (!c->d_pk_part) CTX_CUDA(c, dev_malloc(&c->d_pk_part, sizeof(float) * (size_t)grid * nk));
+  if (!c->d_pk_cnt) CTX_CUDA(c, dev_malloc(&c->d_pk_cnt, sizeof(unsigned long long) * nk));
   std::vector<float> wax(N);
   double s1 = 0.;
   for (int x = 0; x < N; ++x) {
@@ -1400,9 +1434,9 @@ extern "C" int sf21_t21_run_z(sf21_hii_ctx* c, const sf21_t21_cosmo* cosmo, doub
   const int N = (int)c->N;
   const size_t bf = sizeof(float) * n3;
   const int nb = t21_blocks(n3);
-  if (!c->d_pk) CTX_CUDA(c, cudaMalloc(&c->d_pk, sizeof(float2) * n3));
-  if (!c->d_t21) CTX_CUDA(c, cudaMalloc(&c->d_t21, 4 * bf));
-  if (!c->d_t21_part) CTX_CUDA(c, cudaMalloc(&c->d_t21_part, sizeof(float) * 2 * nb));
+  if (!c->d_pk) CTX_CUDA(c, dev_malloc(&c->d_pk, sizeof(float2) * n3));
+  if (!c->d_t21) CTX_CUDA(c, dev_malloc(&c->d_t21, 4 * bf));
+  if (!c->d_t21_part) CTX_CUDA(c, dev_malloc(&c->d_t21_part, sizeof(float) * 2 * nb));
   float* d_xc = c->d_t21;
   float* d_xa = d_xc + n3;
   float* d_tk = d_xa + n3;

@@ -480,30 +480,71 @@ cudaError_t launch_halo_source(long nh, const void* halos_dev, double z, long N_
 // which caps the sizes (kNoAllocMaxNHalo, kNoAllocMaxHalos).  One array per
 // device: calls that overlap on the same device (two streams, two threads)
 // share it and race; the caller serialises them.
+//
+// The array's device address belongs to the CUDA context the module is loaded
+// in.  It is looked up with cudaGetSymbolAddress once per context (the first
+// call in a context does it, so that call should come before any stream
+// capture) and cached under the context's process-unique id (cuCtxGetId):
+// after cudaDeviceReset, or under another context, the next call looks it up
+// again instead of reusing a stale address.
 constexpr size_t kNoAllocScratchBytes = (size_t)16 << 20;  // 16 MiB
 constexpr long kNoAllocMaxNHalo = 128;                     // fine grid <= 8 MiB
 constexpr long kNoAllocMaxHalos = 16384;                   // 131072 CIC entries, 4 MiB
-constexpr int kNoAllocMaxDevices = 64;
+constexpr int kNoAllocCacheSlots = 64;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
 static std::mutex g_noalloc_mu;
-static void* g_noalloc_ptr[kNoAllocMaxDevices];
+static struct {
+  unsigned long long ctx_id;
+  void* ptr;
+} g_noalloc_cache[kNoAllocCacheSlots];
+static int g_noalloc_next = 0;
 
-// Set-up, once per device with that device current: the device address of
+// Process-unique id of the current context (driver entry points, so the
+// library needs no link against libcuda).
+static cudaError_t current_context_id(unsigned long long* id) {
+  typedef int (*CtxGetCurrent)(void**);
+  typedef int (*CtxGetId)(void*, unsigned long long*);
+  static CtxGetCurrent get_current = nullptr;
+  static CtxGetId get_id = nullptr;
+  if (!get_current || !get_id) {
+    void* f = nullptr;
+    void* g = nullptr;
+    cudaDriverEntryPointQueryResult q1, q2;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q1) != cudaSuccess ||
+        q1 != cudaDriverEntryPointSuccess ||
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &g, 12000, cudaEnableDefault, &q2) != cudaSuccess ||
+        q2 != cudaDriverEntryPointSuccess)
+      return cudaErrorNotSupported;
+    get_current = (CtxGetCurrent)f;
+    get_id = (CtxGetId)g;
+  }
+  void* ctx = nullptr;
+  if (get_current(&ctx) != 0 || !ctx) return cudaErrorDeviceUninitialized;
+  return get_id(ctx, id) == 0 ? cudaSuccess : cudaErrorDeviceUninitialized;
+}
+
+// Set-up, once per context with its device current: the device address of
 // the array.  Nothing is allocated (the array belongs to the loaded module).
 static cudaError_t noalloc_scratch(void** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaSetDevice(dev);  // makes the device's primary context current
+  unsigned long long id = 0;
+  if (e == cudaSuccess) e = current_context_id(&id);
   if (e != cudaSuccess) return e;
-  if (dev < 0 || dev >= kNoAllocMaxDevices) return cudaErrorInvalidDevice;
   std::lock_guard<std::mutex> lk(g_noalloc_mu);
-  if (!g_noalloc_ptr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) return e;
-    g_noalloc_ptr[dev] = p;
-  }
-  *out = g_noalloc_ptr[dev];
+  for (int i = 0; i < kNoAllocCacheSlots; ++i)
+    if (g_noalloc_cache[i].ptr && g_noalloc_cache[i].ctx_id == id) {
+      *out = g_noalloc_cache[i].ptr;
+      return cudaSuccess;
+    }
+  void* p = nullptr;
+  e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess) return e;
+  g_noalloc_cache[g_noalloc_next] = {id, p};
+  g_noalloc_next = (g_noalloc_next + 1) % kNoAllocCacheSlots;
+  *out = p;
   return cudaSuccess;
 }
 
@@ -527,9 +568,14 @@ int halo_source_noalloc(double z, long N_halo, long N_smooth, long nh, const voi
   const long ne = 8 * nh;
   const long Nh3 = N_halo * N_halo * N_halo;
   size_t sort_tmp = 0;
-  if (ne > 0)
-    cub::DeviceRadixSort::SortPairs(nullptr, sort_tmp, (uint32_t*)nullptr, (uint32_t*)nullptr, (sd_t*)nullptr,
-                                    (sd_t*)nullptr, (int)ne);
+  if (ne > 0) {
+    const cudaError_t q = cub::DeviceRadixSort::SortPairs(nullptr, sort_tmp, (uint32_t*)nullptr, (uint32_t*)nullptr,
+                                                          (sd_t*)nullptr, (sd_t*)nullptr, (int)ne);
+    if (q != cudaSuccess) {
+      snprintf(err, errlen, "no-alloc halo source: sort size query failed: %s", cudaGetErrorString(q));
+      return SF21_E_CUDA;
+    }
+  }
   // layout: fine | k0 | k1 | v0 | v1 | CUB temp, each 256-byte aligned (N_halo <= 128: 32-bit keys)
   const size_t o_k0 = align256(sizeof(float) * Nh3);
   const size_t o_k1 = o_k0 + align256(ne * sizeof(uint32_t));

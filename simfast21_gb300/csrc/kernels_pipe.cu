@@ -10,9 +10,12 @@
 // centre test and the first-hit update (kx pass; the filtered fields never
 // return to HBM).
 //
-// Every mbarrier wait is bounded: after SF21_SPIN_LIMIT polls the CTA gives
-// up, records the error in *err, waits (bounded again) for its own copy in
-// flight and returns; the host reads *err and reports SF21_E_TIMEOUT.
+// Every mbarrier wait is bounded: after spin_limit polls (a launch argument,
+// SF21_SPIN_LIMIT by default; the context can lower it) the CTA gives up,
+// records the error in *err, waits for its own copies in flight (bounded by
+// SF21_SPIN_LIMIT, whatever spin_limit is, so that no copy can still be
+// writing into the CTA's shared memory when it exits) and returns; the host
+// reads *err and reports SF21_E_TIMEOUT.
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -43,9 +46,27 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
-  for (uint32_t it = 0; it < SF21_SPIN_LIMIT; ++it)
-    if (mbar_try_wait(bar, parity)) return true;
+__device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, uint32_t parity) {  // never suspends
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// At the default limit each poll is a try_wait (the thread may sleep until
+// the phase completes or a system time limit passes); a lowered limit polls
+// with test_wait, which returns at once, so the limit counts polls, not
+// sleeps.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint32_t limit) {
+  if (limit >= SF21_SPIN_LIMIT) {
+    for (uint32_t it = 0; it < limit; ++it)
+      if (mbar_try_wait(bar, parity)) return true;
+  } else {
+    for (uint32_t it = 0; it < limit; ++it)
+      if (mbar_test_wait(bar, parity)) return true;
+  }
   return false;
 }
 __device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y, int z,
@@ -83,7 +104,7 @@ template <int N, int MODE, int LAYOUT>
 __global__ void __launch_bounds__(PipeGeom<N>::THREADS, 1)
 k_pipe(const __grid_constant__ CUtensorMap tmap, Batch bt, float2* __restrict__ work0, long box_stride,
        uint8_t* __restrict__ rc, const float* __restrict__ alpha_ptr, const float2* __restrict__ gtw,
-       int* __restrict__ err) {
+       int* __restrict__ err, uint32_t spin_limit) {
   using G = PipeGeom<N>;
   extern __shared__ __align__(1024) unsigned char pipe_smem_raw[];
   unsigned char* base_ptr =
@@ -168,7 +189,7 @@ k_pipe(const __grid_constant__ CUtensorMap tmap, Batch bt, float2* __restrict__ 
       fence_proxy_async();
       issue(li + 1);
     }
-    const bool ok = mbar_wait_bounded(&full[li & 1], (uint32_t)((li >> 1) & 1));
+    const bool ok = mbar_wait_bounded(&full[li & 1], (uint32_t)((li >> 1) & 1), spin_limit);
     if (__syncthreads_or(!ok)) {
       failed_at = li;
       break;
@@ -216,9 +237,10 @@ k_pipe(const __grid_constant__ CUtensorMap tmap, Batch bt, float2* __restrict__ 
     atomicExch(err, 1);
     // drain this CTA's copies that may still be in flight (loads failed_at and
     // failed_at + 1) before its shared memory is released; bounded again
-    (void)mbar_wait_bounded(&full[failed_at & 1], (uint32_t)((failed_at >> 1) & 1));
+    (void)mbar_wait_bounded(&full[failed_at & 1], (uint32_t)((failed_at >> 1) & 1), SF21_SPIN_LIMIT);
     if (failed_at + 1 < nloads)
-      (void)mbar_wait_bounded(&full[(failed_at + 1) & 1], (uint32_t)(((failed_at + 1) >> 1) & 1));
+      (void)mbar_wait_bounded(&full[(failed_at + 1) & 1], (uint32_t)(((failed_at + 1) >> 1) & 1),
+                              SF21_SPIN_LIMIT);
   }
 }
 
@@ -286,16 +308,17 @@ struct PipeLaunch {
     return make_map(&pm->a_rows_cb, N, K, base, G::CW, G::BOX, true, 1);
   }
   static cudaError_t launch(int mode, int layout, const PipeMaps& pm, const Batch& bt, float2* work0, uint8_t* rc,
-                            const float* alpha, const float2* tw, int* err, int nsm, cudaStream_t st) {
+                            const float* alpha, const float2* tw, int* err, int nsm, uint32_t lim,
+                            cudaStream_t st) {
     const long box_stride = (long)N * N * N;
     if (mode == 0 && layout == 0)
-      k_pipe<N, 0, 0><<<nsm, G::THREADS, G::SMEM, st>>>(pm.b_rows, bt, work0, box_stride, rc, alpha, tw, err);
+      k_pipe<N, 0, 0><<<nsm, G::THREADS, G::SMEM, st>>>(pm.b_rows, bt, work0, box_stride, rc, alpha, tw, err, lim);
     else if (mode == 1 && layout == 0)
-      k_pipe<N, 1, 0><<<nsm, G::THREADS, G::SMEM, st>>>(pm.a_rows, bt, work0, box_stride, rc, alpha, tw, err);
+      k_pipe<N, 1, 0><<<nsm, G::THREADS, G::SMEM, st>>>(pm.a_rows, bt, work0, box_stride, rc, alpha, tw, err, lim);
     else if (mode == 0)
-      k_pipe<N, 0, 1><<<nsm, G::THREADS, G::SMEM, st>>>(pm.b_rows_cb, bt, work0, box_stride, rc, alpha, tw, err);
+      k_pipe<N, 0, 1><<<nsm, G::THREADS, G::SMEM, st>>>(pm.b_rows_cb, bt, work0, box_stride, rc, alpha, tw, err, lim);
     else
-      k_pipe<N, 1, 1><<<nsm, G::THREADS, G::SMEM, st>>>(pm.a_rows_cb, bt, work0, box_stride, rc, alpha, tw, err);
+      k_pipe<N, 1, 1><<<nsm, G::THREADS, G::SMEM, st>>>(pm.a_rows_cb, bt, work0, box_stride, rc, alpha, tw, err, lim);
     return cudaGetLastError();
   }
 };
@@ -325,13 +348,15 @@ cudaError_t pipe_make_maps(int N, PipeMaps* pm, int K, void* work_base) {
 }
 
 cudaError_t launch_pipe(int N, int mode, int layout, const PipeMaps& pm, const Batch& bt, float2* work0,
-                        uint8_t* rc, const float* alpha, const float2* tw, int* err, int nsm, cudaStream_t st) {
+                        uint8_t* rc, const float* alpha, const float2* tw, int* err, int nsm, cudaStream_t st,
+                        uint32_t spin_limit) {
+  const uint32_t lim = spin_limit ? spin_limit : SF21_SPIN_LIMIT;
   switch (N) {
-    case 64: return PipeLaunch<64>::launch(mode, layout, pm, bt, work0, rc, alpha, tw, err, nsm, st);
-    case 128: return PipeLaunch<128>::launch(mode, layout, pm, bt, work0, rc, alpha, tw, err, nsm, st);
-    case 256: return PipeLaunch<256>::launch(mode, layout, pm, bt, work0, rc, alpha, tw, err, nsm, st);
-    case 512: return PipeLaunch<512>::launch(mode, layout, pm, bt, work0, rc, alpha, tw, err, nsm, st);
-    case 1024: return PipeLaunch<1024>::launch(mode, layout, pm, bt, work0, rc, alpha, tw, err, nsm, st);
+    case 64: return PipeLaunch<64>::launch(mode, layout, pm, bt, work0, rc, alpha, tw, err, nsm, lim, st);
+    case 128: return PipeLaunch<128>::launch(mode, layout, pm, bt, work0, rc, alpha, tw, err, nsm, lim, st);
+    case 256: return PipeLaunch<256>::launch(mode, layout, pm, bt, work0, rc, alpha, tw, err, nsm, lim, st);
+    case 512: return PipeLaunch<512>::launch(mode, layout, pm, bt, work0, rc, alpha, tw, err, nsm, lim, st);
+    case 1024: return PipeLaunch<1024>::launch(mode, layout, pm, bt, work0, rc, alpha, tw, err, nsm, lim, st);
     default: return cudaErrorInvalidValue;
   }
 }

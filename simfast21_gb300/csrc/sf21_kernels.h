@@ -9,6 +9,16 @@
 
 namespace sf21 {
 
+// Device allocations of the library's contexts (HII, halo finder, SFR
+// stage) go through dev_malloc, where sf21_hii_inject_alloc_failure can make
+// a chosen one fail with cudaErrorMemoryAllocation (a test hook; off unless
+// armed).
+cudaError_t dev_malloc(void** p, size_t bytes);
+template <class T>
+inline cudaError_t dev_malloc(T** p, size_t bytes) {
+  return dev_malloc(reinterpret_cast<void**>(p), bytes);
+}
+
 // Per-redshift scalars of the prologue, as IEEE double bit patterns computed
 // on the host exactly as the reference evaluates them.
 struct PrologueArgs {
@@ -81,8 +91,10 @@ cudaError_t pipe_make_maps(int N, PipeMaps* pm, int K, void* work_base);
 // mode 0: ky inverse pass in place over the batch's boxes; mode 1: kx inverse
 // pass + centre test + first-hit update.  layout 0: natural work boxes,
 // 1: column-block major (kernels_cb.cu).  nsm = persistent CTAs.
+// spin_limit: polls per bounded mbarrier wait (0 = the default, 2^26).
 cudaError_t launch_pipe(int N, int mode, int layout, const PipeMaps& pm, const Batch& bt, float2* work0,
-                        uint8_t* rc, const float* alpha, const float2* tw, int* err, int nsm, cudaStream_t st);
+                        uint8_t* rc, const float* alpha, const float2* tw, int* err, int nsm, cudaStream_t st,
+                        uint32_t spin_limit = 0);
 
 // Radius pipeline over column-block-major work boxes (kernels_cb.cu):
 // c-axis filter pass, in-place b-axis pass, a-axis pass + centre test.

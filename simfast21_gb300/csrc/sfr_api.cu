@@ -90,8 +90,8 @@ extern "C" int sf21_sfr_create(const sf21_sfr_config* cfg, sf21_sfr_ctx** out) {
   } while (0)
   SCREATE(cudaSetDevice(cfg->device));
   SCREATE(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
-  SCREATE(cudaMalloc(&c->d_fine, sizeof(float) * c->n3_halo));
-  SCREATE(cudaMalloc(&c->d_out, sizeof(float) * c->n3));
+  SCREATE(dev_malloc(&c->d_fine, sizeof(float) * c->n3_halo));
+  SCREATE(dev_malloc(&c->d_out, sizeof(float) * c->n3));
 #undef SCREATE
   *out = c;
   return SF21_OK;
@@ -111,9 +111,9 @@ static int ensure_halo_cap(sf21_sfr_ctx* c, long nhalos) {
   c->halo_cap = 0;
   long cap = nhalos + nhalos / 4 + 1024;
   if (cap >= (1L << 28)) cap = (1L << 28) - 1;
-  SCTX_CUDA(c, cudaMalloc(&c->d_halos, (size_t)cap * 16));
+  SCTX_CUDA(c, dev_malloc(&c->d_halos, (size_t)cap * 16));
   c->scratch_bytes = halo_scratch_bytes(cap);
-  SCTX_CUDA(c, cudaMalloc(&c->d_scratch, c->scratch_bytes));
+  SCTX_CUDA(c, dev_malloc(&c->d_scratch, c->scratch_bytes));
   c->halo_cap = cap;
   return SF21_OK;
 }

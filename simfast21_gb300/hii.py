@@ -31,7 +31,7 @@ EXPORTS = [
     "sf21_hii_vjp", "sf21_hii_vjp_device", "sf21_hii_path", "sf21_hii_check", "sf21_hii_halo_source",
     "sf21_hii_run_z_halos", "sf21_hii_profile", "sf21_hii_profile_read", "sf21_hii_profile_name",
     "sf21_hii_halo_source_noalloc", "sf21_hii_power_spectrum", "sf21_hii_power_spectrum_device",
-    "sf21_t21_run_z",
+    "sf21_t21_run_z", "sf21_hii_set_wait_limit", "sf21_hii_inject_alloc_failure",
 ]
 
 
@@ -97,6 +97,8 @@ def load_library(path: str = LIB_PATH):
     L.sf21_hii_power_spectrum_device.argtypes = [vp, vp, ctypes.c_int, ctypes.c_double, dp, dp, ctypes.c_int, vp]
     L.sf21_t21_run_z.argtypes = [vp, ctypes.POINTER(T21Cosmo), ctypes.c_double, fp, fp, fp, fp, fp, fp, dp, dp]
     L.sf21_hii_check.argtypes = [vp]
+    L.sf21_hii_set_wait_limit.argtypes = [vp, ctypes.c_uint]
+    L.sf21_hii_inject_alloc_failure.argtypes = [ctypes.c_long]
     L.sf21_hii_profile.argtypes = [vp, ctypes.c_int]
     L.sf21_hii_profile_read.argtypes = [vp, dp, ctypes.POINTER(ctypes.c_long), ctypes.c_int]
     L.sf21_hii_profile_name.argtypes = [ctypes.c_int]
@@ -114,6 +116,14 @@ def _f32(a, n3):
     if a.size != n3:
         raise ValueError(f"box has {a.size} elements, expected {n3}")
     return a
+
+
+def inject_alloc_failure(n: int) -> None:
+    """Test hook: the n-th device allocation of any context from now fails
+    once (0 disarms)."""
+    rc = load_library().sf21_hii_inject_alloc_failure(int(n))
+    if rc != 0:
+        raise HIIError(rc, "bad count")
 
 
 def halo_source_noalloc(z: float, N_halo: int, N_smoothed: int, nhalos: int, halos_ptr: int, out_ptr: int,
@@ -180,6 +190,11 @@ class FilterBank:
     def check(self):
         """Raise if a bounded device wait expired since the last check."""
         self._check(self._lib.sf21_hii_check(self._h))
+
+    def set_wait_limit(self, polls: int):
+        """Polls per bounded device wait of the TMA-pipelined passes (0 =
+        default); lowering it makes the waits run out on an ordinary launch."""
+        self._check(self._lib.sf21_hii_set_wait_limit(self._h, int(polls)))
 
     def radii(self, s: int = 0):
         buf = (ctypes.c_double * 512)()

@@ -51,3 +51,28 @@ def test_nmax_definition():
     for R in (0.7, 1.0, 1.39, 2.1, 7.77, 30.0):
         n = P.nmax(R, dx)
         assert np.sqrt(float(n)) * dx <= R and not (np.sqrt(float(n + 1)) * dx <= R)
+
+
+def test_torch_bands_equal_numpy_bands(oracle_lib):
+    """The torch form of the bands (run on the GPU at the measured box sizes)
+    gives the numpy form's first-hit bounds, dilations and finished boxes, here
+    on the CPU with torch's float64 FFT."""
+    import torch
+    from oracle import fp64_torch as T
+    O = oracle_lib
+    g = load_golden("hii_n32_sfr.npz")
+    sp = g["params"]
+    out = O.run_z_sfr(oracle_params(O, sp), float(g["zs"][0]), g["delta_0"], g["sfrd_0"], extras=True)
+    radii, _ = P.radii(sp.Rmax, sp.dx, sp.Nbins)
+    want = F.bands(out["rec0"], out["ion0"], radii, sp.dx, sp.dk)
+    got = T.Bands(out["rec0"], out["ion0"], sp.dk, device="cpu").bands(radii, sp.dx)
+    for k in ("rc_lo", "rc_hi", "ionised_lo", "ionised_hi"):
+        assert np.array_equal(got[k].numpy(), want[k]), k
+    assert got["n_band"] == want["n_band"]
+    for k in ("ionised_lo", "ionised_hi"):
+        x_np = F.finish(want[k], out["fill0"], out["fresid"])
+        x_t = T.finish(got[k], out["fill0"], out["fresid"]).numpy()
+        assert np.array_equal(x_np.view(np.uint32), x_t.view(np.uint32))
+    v = torch.full((12, 12, 12), -1, dtype=torch.int32)
+    v[1, 2, 3], v[7, 11, 0] = 9, 20
+    assert np.array_equal(T.dilate(v).numpy(), F.dilate(v.numpy().astype(np.int64)))

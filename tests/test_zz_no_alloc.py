@@ -28,14 +28,22 @@ def test_noalloc_matches_context_entry_on_consecutive_calls(hii):
     import torch
     fb = hii.FilterBank(N, L, 0.71, [(0.5, L / 2, 20)], N_halo=NH)
     cats = [_catalogue(55), _catalogue(77), _catalogue(55)]
+    free_after = []
     for cat in cats:
         want = fb.halo_source(Z, cat)
         d_cat = _device(cat)
         out = torch.full((N, N, N), float("nan"), device="cuda")
+        torch.cuda.synchronize()
+        free_before = torch.cuda.mem_get_info()[0]
         hii.halo_source_noalloc(Z, NH, N, len(cat), d_cat.data_ptr(), out.data_ptr())
         torch.cuda.synchronize()
+        free_after.append((free_before, torch.cuda.mem_get_info()[0]))
         got = out.cpu().numpy()
         assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    # nothing allocated on the device by the calls after the first (the first
+    # may load the library's module image, which holds the array)
+    for before, after in free_after[1:]:
+        assert after == before
     # an empty catalogue leaves a zero box (the fine grid is cleared per call)
     out = torch.full((N, N, N), float("nan"), device="cuda")
     hii.halo_source_noalloc(Z, NH, N, 0, 0, out.data_ptr())
