@@ -278,6 +278,7 @@ PIPELINES = {
     5: ("cb_three_pass", "column-block-major work boxes, three axis passes"),
     6: ("cb_tma_ky", "column-block-major work boxes, ky pass TMA-pipelined"),
     7: ("cb_tma_ky_kx", "column-block-major work boxes, ky and kx passes TMA-pipelined"),
+    8: ("cb_fused_l2", "column-block-major work boxes, c-axis pass + one persistent ky/kx launch through L2"),
 }
 
 
@@ -580,12 +581,13 @@ def run_ours(args, w, rank, world):
     dom_ms, dom_n = kinds[dom]
     per_launch_ms = dom_ms / dom_n
     # algorithmic bytes per launch (complex64 boxes: 8 B per voxel)
-    nbatch = kinds.get("inv_cols_a_test", (0, 1))[1] / steps
+    nbatch = kinds.get("inv_cols_a_test", kinds.get("inv_cols_ba_fused", (0, 1)))[1] / steps
     K_avg = R_total / nbatch
     alg = {
         "inv_rows_filter": n3 * 8.0 * (1 + K_avg),      # spectrum read once, K boxes written
         "inv_cols_b": n3 * 16.0 * K_avg,                 # K boxes read + written
         "inv_cols_a_test": n3 * (8.0 * K_avg + 2.0),     # K boxes read, first-hit byte r/w
+        "inv_cols_ba_fused": n3 * (8.0 * K_avg + 2.0),   # K boxes read from DRAM (ky), kx through L2
         "inv_plane_filter": n3 * 8.0 * (1 + K_avg),      # spectrum read once, K boxes written
     }.get(dom, None)
     achieved = alg / (per_launch_ms / 1e3) / 1e9 if alg else None
@@ -596,7 +598,7 @@ def run_ours(args, w, rank, world):
     traffic = traffic_b * n3 * K_avg if (traffic_b and path >= 5) else None
     # whole radius pipeline against the 16 B per voxel*radius algorithmic traffic
     pipe_ms = sum(kinds.get(k, (0, 0))[0] for k in ("inv_rows_filter", "inv_cols_b", "inv_cols_a_test",
-                                                     "inv_plane_filter"))
+                                                     "inv_plane_filter", "inv_cols_ba_fused"))
     pipe_gbs = 16.0 * units * steps / (pipe_ms / 1e3) / 1e9 if pipe_ms else None
 
     # the plain one-radius-per-launch form on one parameter set (same box)

@@ -58,10 +58,12 @@ typedef struct {
   int device;        /* CUDA device ordinal                                 */
   int nsets;         /* parameter sets sharing each forward transform (>=1) */
   const sf21_hii_set *sets;
-  int kmax;          /* radii per spectrum read (0 = automatic, <= 8)       */
+  int kmax;          /* radii per spectrum read (0 = automatic: the
+                        autotuner picks 8, 6 or 4; else fixed, <= 8)       */
   int path;          /* radius pipeline: 0 = tuned at create (times one batch
-                        of each available one and keeps the fastest; the
-                        timings are cached per device, N and kmax in
+                        of each available one at each candidate batch size
+                        and keeps the least time per radius; the timings
+                        are cached per device, N and batch size in
                         $SF21_TUNE_CACHE or ~/.cache/simfast21_gb300/
                         tune.jsonl and reused, SF21_RETUNE=1 times again),
                         1 = three axis passes, 2 = plane passes on
@@ -69,7 +71,10 @@ typedef struct {
                         passes with the ky pass TMA-pipelined and
                         persistent, 4 = ky and kx passes TMA-pipelined
                         (3 and 4: N 64..1024), 5-7 = the same over
-                        column-block-major work boxes */
+                        column-block-major work boxes, 8 = column-block-
+                        major c-axis pass + one persistent launch running
+                        the ky and kx passes slab by slab through L2
+                        (N 64..512) */
   int graph;         /* 0 = sf21_hii_run_z_device captures its per-redshift
                         schedule as a CUDA graph and replays it while z, the
                         kind, the buffers and the stream stay the same;
@@ -228,10 +233,15 @@ int sf21_hii_vjp_device(sf21_hii_ctx *ctx, double z, int src_kind, const float *
                         const float *src_dev, int set, const float *dC_dev, float *ddelta_dev,
                         float *dsrc_dev, double *dfesc, void *stream);
 
-/* Radius pipeline in use (1..7, see sf21_hii_config.path); ms_tuned[p-1]
+/* Radius pipeline in use (1..8, see sf21_hii_config.path); ms_tuned[p-1]
  * receives the measured ms of one batch of pipeline p when it was tuned at
  * create (0 if not timed), for p <= cap. */
 int sf21_hii_path(const sf21_hii_ctx *ctx, double *ms_tuned, int cap);
+
+/* Radii per spectrum read (batch size K) in use: kmax when the config fixed
+ * it, else the autotuner's choice among kmax (<= 8), 6 and 4 (least time per
+ * radius together with the pipeline).  No reference counterpart. */
+int sf21_hii_batch_radii(const sf21_hii_ctx *ctx);
 
 /* Synchronises the context's stream and reports SF21_E_TIMEOUT if a bounded
  * device wait (TMA copy completion) expired since the last check. */

@@ -84,8 +84,9 @@ double host_Qion(double z) { return pow(10.0, 2.05707274e-02 * z + 5.29944413e+0
 
 // Radius pipelines: 1 three axis passes, 2 plane clusters + kx pass,
 // 3 TMA ky + kx pass, 4 TMA ky + TMA kx, and over column-block-major work
-// boxes: 5 three axis passes, 6 TMA ky + kx pass, 7 TMA ky + TMA kx.
-constexpr int NPATH = 7;
+// boxes: 5 three axis passes, 6 TMA ky + kx pass, 7 TMA ky + TMA kx,
+// 8 c-axis pass + one persistent ky/kx launch handing each slab over in L2.
+constexpr int NPATH = 8;
 
 struct sf21_hii_ctx {
   int device = 0;
@@ -111,6 +112,7 @@ struct sf21_hii_ctx {
   } gkey = {0, -1, nullptr, nullptr, nullptr, nullptr};
   PipeMaps pmaps;
   int* d_err = nullptr;
+  int* d_ctl = nullptr;     // work-queue control block of pipeline 8
   uint32_t wait_limit = 0;  // polls per bounded device wait (0 = the kernels' default)
   int nsm = 0;
   std::vector<SetInfo> sets;
@@ -171,9 +173,9 @@ static const char* kKindNames[] = {"prologue", "alpha", "fwd_rows", "fwd_cols_b"
                                    "inv_rows_filter", "inv_cols_b", "inv_cols_a_test", "dt_a",
                                    "dt_b", "dt_c_finish", "inv_plane_filter", "crit_cols_a",
                                    "adj_cols_a", "adj_cols_b_fwd", "adj_rows_acc", "adj_final",
-                                   "finish_prep"};
+                                   "finish_prep", "inv_cols_ba_fused"};
 enum { KD_PRO, KD_ALPHA, KD_FROWS, KD_FCB, KD_FCA, KD_IROWS, KD_ICB, KD_ICA, KD_DTR, KD_DTB, KD_DTA, KD_PLANE,
-       KD_CRIT, KD_ADJA, KD_ADJB, KD_ADJR, KD_ADJF, KD_PREP, KD_COUNT };
+       KD_CRIT, KD_ADJA, KD_ADJB, KD_ADJR, KD_ADJF, KD_PREP, KD_FUSED, KD_COUNT };
 
 // Records an event on st when timing is on; returns its index (or -1).
 static int mark(sf21_hii_ctx* c, cudaStream_t st) {
@@ -327,6 +329,7 @@ static void free_ctx(sf21_hii_ctx* c) {
     if (p) cudaFree(p);
   if (c->d_work_base) cudaFree(c->d_work_base);
   if (c->d_err) cudaFree(c->d_err);
+  if (c->d_ctl) cudaFree(c->d_ctl);
   for (SetInfo& s : c->sets)
     if (s.d_nmax) cudaFree(s.d_nmax);
   for (cudaEvent_t e : c->ev) cudaEventDestroy(e);
@@ -487,9 +490,14 @@ extern "C" int sf21_hii_create(const sf21_hii_config* cfg, sf21_hii_ctx** out) {
   if (!c->gen && pipe_supported((int)N) && pipe_setup((int)N) == cudaSuccess &&
       pipe_make_maps((int)N, &c->pmaps, K, c->d_work_base) == cudaSuccess)
     can_pipe = true;
+  bool can_fused = false;
+  if (!c->gen && fused_supported((int)N) && fused_setup((int)N) == cudaSuccess &&
+      dev_malloc(&c->d_ctl, sizeof(int) * fused_ctl_ints((int)N)) == cudaSuccess)
+    can_fused = true;
   cudaGetLastError();
   const int want = cfg->path;
   if ((want == 2 && !can_plane) || ((want == 3 || want == 4 || want == 6 || want == 7) && !can_pipe) ||
+      (want == 8 && !can_fused) ||
       (c->gen && want > 1) || want < 0 || want > NPATH) {
     g_create_err = "requested radius pipeline not available for this box on this device";
     free_ctx(c);
@@ -497,60 +505,92 @@ extern "C" int sf21_hii_create(const sf21_hii_config* cfg, sf21_hii_ctx** out) {
   }
   c->path = want ? want : 1;
   // a tuning result cached for this device, box size and batch size skips the timing
-  const std::string tkey = tune_key(c->device, N, K);
-  if (want == 0 && (can_plane || can_pipe) && tune_cache_lookup(tkey, c->tune_ms, NPATH)) {
-    for (int p = 2; p <= NPATH; ++p)
-      if (c->tune_ms[p] < c->tune_ms[c->path]) c->path = p;
-    if ((c->path == 2 && !can_plane) || ((c->path == 3 || c->path == 4 || c->path == 6 || c->path == 7) && !can_pipe))
-      c->path = 1;
-  } else if (want == 0 && (can_plane || can_pipe)) {
-    CREATE_CUDA(cudaMemsetAsync(c->d_spec, 0, box_c, c->stream));
-    CREATE_CUDA(cudaMemsetAsync(c->d_alpha, 0, sizeof(float), c->stream));
-    Batch bt;
-    memset(&bt, 0, sizeof(bt));
-    bt.K = K;
-    bt.zmul = 1.0f;
-    for (int k = 0; k < K; ++k) {
-      bt.r[k].dkR = (float)(c->dk * c->dx * (2.0 + k));
-      bt.r[k].ridx = k;
-      bt.r[k].work = c->d_work[k];
-    }
-    cudaEvent_t t0, t1;
-    CREATE_CUDA(cudaEventCreate(&t0));
-    CREATE_CUDA(cudaEventCreate(&t1));
-    double best[NPATH + 1];
-    for (int p = 0; p <= NPATH; ++p) best[p] = 1e30;
-    for (int p = 1; p <= NPATH; ++p) {
-      if ((p == 2 && !can_plane) || ((p == 3 || p == 4 || p == 6 || p == 7) && !can_pipe)) continue;
-      c->path = p;
-      for (int rep = 0; rep < 4; ++rep) {
-        CREATE_CUDA(cudaEventRecord(t0, c->stream));
-        if (enqueue_batch(c, bt, c->stream) != SF21_OK) {
-          g_create_err = c->err;
-          free_ctx(c);
-          return SF21_E_CUDA;
+  // Autotuner: the radius pipeline and the radii per spectrum read K.  For
+  // each candidate K (the cap, and 6 and 4 below it unless the caller fixed
+  // kmax) one K-radius batch of every available pipeline is timed (or the
+  // timings are read from the per-device cache); the (pipeline, K) with the
+  // least time per radius wins.
+  auto available = [&](int p) {
+    return !((p == 2 && !can_plane) || ((p == 3 || p == 4 || p == 6 || p == 7) && !can_pipe) ||
+             (p == 8 && !can_fused));
+  };
+  if (want == 0 && (can_plane || can_pipe || can_fused)) {
+    std::vector<int> kcands = {K};
+    if (cfg->kmax <= 0)
+      for (int kc : {6, 4})
+        if (kc < K) kcands.push_back(kc);
+    double best_per_radius = 1e30;
+    int best_path = 1, best_K = K;
+    double best_ms[NPATH + 1];
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    bool zeroed = false;
+    for (int Kc : kcands) {
+      double ms_p[NPATH + 1];
+      for (int p = 0; p <= NPATH; ++p) ms_p[p] = 1e30;
+      const std::string tkey = tune_key(c->device, N, Kc);
+      if (!tune_cache_lookup(tkey, ms_p, NPATH)) {
+        if (!zeroed) {
+          CREATE_CUDA(cudaMemsetAsync(c->d_spec, 0, box_c, c->stream));
+          CREATE_CUDA(cudaMemsetAsync(c->d_alpha, 0, sizeof(float), c->stream));
+          CREATE_CUDA(cudaEventCreate(&t0));
+          CREATE_CUDA(cudaEventCreate(&t1));
+          zeroed = true;
         }
-        CREATE_CUDA(cudaEventRecord(t1, c->stream));
-        CREATE_CUDA(cudaEventSynchronize(t1));
-        float ms = 0.f;
-        CREATE_CUDA(cudaEventElapsedTime(&ms, t0, t1));
-        if (rep > 0 && ms < best[p]) best[p] = ms;  // the first run warms up
+        Batch bt;
+        memset(&bt, 0, sizeof(bt));
+        bt.K = Kc;
+        bt.zmul = 1.0f;
+        for (int k = 0; k < Kc; ++k) {
+          bt.r[k].dkR = (float)(c->dk * c->dx * (2.0 + k));
+          bt.r[k].ridx = k;
+          bt.r[k].work = c->d_work[k];
+        }
+        for (int p = 1; p <= NPATH; ++p) {
+          if (!available(p)) continue;
+          c->path = p;
+          for (int rep = 0; rep < 4; ++rep) {
+            CREATE_CUDA(cudaEventRecord(t0, c->stream));
+            if (enqueue_batch(c, bt, c->stream) != SF21_OK) {
+              g_create_err = c->err;
+              cudaEventDestroy(t0);
+              cudaEventDestroy(t1);
+              free_ctx(c);
+              return SF21_E_CUDA;
+            }
+            CREATE_CUDA(cudaEventRecord(t1, c->stream));
+            CREATE_CUDA(cudaEventSynchronize(t1));
+            float ms = 0.f;
+            CREATE_CUDA(cudaEventElapsedTime(&ms, t0, t1));
+            if (rep > 0 && ms < ms_p[p]) ms_p[p] = ms;  // the first run warms up
+          }
+        }
+        int err_flag = 0;
+        CREATE_CUDA(cudaMemcpy(&err_flag, c->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+        if (err_flag) {
+          g_create_err = "a bounded device wait expired while tuning";
+          if (t0) cudaEventDestroy(t0);
+          if (t1) cudaEventDestroy(t1);
+          free_ctx(c);
+          return SF21_E_TIMEOUT;
+        }
+        tune_cache_store(tkey, ms_p, NPATH);
       }
-      c->tune_ms[p] = best[p];
+      for (int p = 1; p <= NPATH; ++p) {
+        if (!available(p) || !(ms_p[p] < 1e29)) continue;
+        if (ms_p[p] / Kc < best_per_radius) {
+          best_per_radius = ms_p[p] / Kc;
+          best_path = p;
+          best_K = Kc;
+          for (int q = 0; q <= NPATH; ++q) best_ms[q] = ms_p[q];
+        }
+      }
     }
-    cudaEventDestroy(t0);
-    cudaEventDestroy(t1);
-    int err_flag = 0;
-    CREATE_CUDA(cudaMemcpy(&err_flag, c->d_err, sizeof(int), cudaMemcpyDeviceToHost));
-    if (err_flag) {
-      g_create_err = "a bounded device wait expired while tuning";
-      free_ctx(c);
-      return SF21_E_TIMEOUT;
-    }
-    c->path = 1;
-    for (int p = 2; p <= NPATH; ++p)
-      if (best[p] < best[c->path]) c->path = p;
-    tune_cache_store(tkey, c->tune_ms, NPATH);
+    if (t0) cudaEventDestroy(t0);
+    if (t1) cudaEventDestroy(t1);
+    c->path = best_path;
+    c->K = best_K;
+    if (best_per_radius < 1e29)
+      for (int p = 0; p <= NPATH; ++p) c->tune_ms[p] = best_ms[p];
   }
 #undef CREATE_CUDA
   *out = c;
@@ -647,6 +687,17 @@ static int enqueue_batch(sf21_hii_ctx* c, const Batch& bt, cudaStream_t st) {
     int e2 = mark(c, st);
     span(c, KD_PLANE, e0, e1);
     span(c, KD_ICA, e1, e2);
+    return SF21_OK;
+  }
+  if (c->path == 8) {  // column-block-major work boxes, ky and kx in one launch
+    int e0 = mark(c, st);
+    CTX_CUDA(c, launch_rows_filter_cb(N, c->d_spec, bt, c->d_tw, st));
+    int e1 = mark(c, st);
+    CTX_CUDA(c, launch_cols_ba_fused(N, bt, c->d_rc, c->d_alpha, c->d_tw, c->d_ctl, c->d_err, c->nsm, st,
+                                     c->wait_limit));
+    int e2 = mark(c, st);
+    span(c, KD_IROWS, e0, e1);
+    span(c, KD_FUSED, e1, e2);
     return SF21_OK;
   }
   if (c->path >= 5) {  // column-block-major work boxes
@@ -1089,6 +1140,8 @@ extern "C" int sf21_hii_set_wait_limit(sf21_hii_ctx* c, unsigned int polls) {
   return SF21_OK;
 }
 
+extern "C" int sf21_hii_batch_radii(const sf21_hii_ctx* c) { return c ? c->K : -SF21_E_ARG; }
+
 extern "C" int sf21_hii_check(sf21_hii_ctx* c) {
   if (!c) return SF21_E_ARG;
   CTX_CUDA(c, cudaSetDevice(c->device));
@@ -1098,7 +1151,6 @@ extern "C" int sf21_hii_check(sf21_hii_ctx* c) {
 
 // ---- criterion C(x) = max_R ion_R / rec_R and its vector-Jacobian product ----
 static int ensure_adj_buffers(sf21_hii_ctx* c) {
-  if (c->gen) CTX_FAIL(c, SF21_E_UNSUPPORTED, "the criterion and its adjoint need a power-of-two box side");
   const long n3 = c->n3;
   if (!c->d_C) CTX_CUDA(c, dev_malloc(&c->d_C, sizeof(float) * n3));
   if (!c->d_A) CTX_CUDA(c, dev_malloc(&c->d_A, n3));
@@ -1155,7 +1207,12 @@ extern "C" int sf21_hii_criterion_device(sf21_hii_ctx* c, double z, int kind, co
     Batch bt = make_batch(c, set, k0, nr);
     if ((rc = enqueue_recompute(c, bt, st))) return rc;
     int e0 = mark(c, st);
-    CTX_CUDA(c, launch_cols_a_crit(N, bt, c->d_C, c->d_A, c->d_alpha, c->d_tw, st));
+    if (c->gen) {  // shared-memory transforms: whole a-axis pass, then the per-element rule
+      CTX_CUDA(c, x_cols(c, nullptr, bt, bt.K, 0, true, st));
+      CTX_CUDA(c, launch_crit_elem(c->n3, bt, c->d_C, c->d_A, c->d_alpha, st));
+    } else {
+      CTX_CUDA(c, launch_cols_a_crit(N, bt, c->d_C, c->d_A, c->d_alpha, c->d_tw, st));
+    }
     span(c, KD_CRIT, e0, mark(c, st));
   }
   CTX_CUDA(c, launch_crit_finalize(c->n3, c->d_C, c->d_A, st));
@@ -1179,7 +1236,7 @@ extern "C" int sf21_hii_vjp_device(sf21_hii_ctx* c, double z, int kind, const fl
   cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
   const int N = (int)c->N;
   const long n3 = c->n3;
-  const int nzp = adj_zpart_blocks(N);
+  const int nzp = c->gen ? adj_elem_blocks() : adj_zpart_blocks(N);
   if (!c->d_acc) CTX_CUDA(c, dev_malloc(&c->d_acc, sizeof(float2) * n3));
   if (!c->d_zpart) CTX_CUDA(c, dev_malloc(&c->d_zpart, sizeof(float) * nzp));
   // recompute the spectrum (the checkpoint holds only the argmax index)
@@ -1193,11 +1250,23 @@ extern "C" int sf21_hii_vjp_device(sf21_hii_ctx* c, double z, int kind, const fl
     Batch bt = make_batch(c, set, k0, nr);
     if ((rc = enqueue_recompute(c, bt, st))) return rc;
     int e0 = mark(c, st);
-    CTX_CUDA(c, launch_cols_a_adj(N, bt, dC_dev, c->d_A, c->d_alpha, c->d_zpart, c->d_tw, st));
+    if (c->gen) {  // a-axis inverse, cotangents, a-axis forward as whole-box passes
+      CTX_CUDA(c, x_cols(c, nullptr, bt, bt.K, 0, true, st));
+      CTX_CUDA(c, launch_adj_elem(n3, bt, dC_dev, c->d_A, c->d_alpha, c->d_zpart, st));
+      CTX_CUDA(c, x_cols(c, nullptr, bt, bt.K, 0, false, st));
+    } else {
+      CTX_CUDA(c, launch_cols_a_adj(N, bt, dC_dev, c->d_A, c->d_alpha, c->d_zpart, c->d_tw, st));
+    }
     int e1 = mark(c, st);
     CTX_CUDA(c, x_cols(c, nullptr, bt, bt.K, 1, false, st));
     int e2 = mark(c, st);
-    CTX_CUDA(c, launch_rows_adj_acc(N, bt, c->d_acc, c->d_tw, st));
+    if (c->gen) {  // c-axis forward of each box, then W and the sum over the batch
+      for (int k = 0; k < bt.K; ++k)
+        CTX_CUDA(c, launch_gen_fwd_rows(c->gp, bt.r[k].work, bt.r[k].work, nullptr, c->d_tw, st));
+      CTX_CUDA(c, launch_acc_elem(N, bt, c->d_acc, st));
+    } else {
+      CTX_CUDA(c, launch_rows_adj_acc(N, bt, c->d_acc, c->d_tw, st));
+    }
     int e3 = mark(c, st);
     span(c, KD_ADJA, e0, e1);
     span(c, KD_ADJB, e1, e2);

@@ -241,6 +241,107 @@ __global__ void k_crit_finalize(long n3, float* __restrict__ C, const uint8_t* _
     if (A[i] == RC_NONE) C[i] = 0.0f;
 }
 
+// ---- any box side (the shared-memory transform family): the same per-element
+// rules over natural-layout work boxes, after whole-box transforms --------
+constexpr int kAdjElemBlocks = 152 * 8;  // fixed grid: deterministic zeta partials
+
+// Forward: running max of the ratio over the batch's fully inverse-transformed
+// boxes (the rule of k_cols_a_crit).
+__global__ void k_crit_elem(long n3, Batch bt, float* __restrict__ Cbuf, uint8_t* __restrict__ Abuf,
+                            const float* __restrict__ alpha_ptr) {
+  const float alpha = fabsf(*alpha_ptr);
+  const float zmul = *alpha_ptr > 0.0f ? bt.zmul : 0.0f;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += (long)gridDim.x * blockDim.x) {
+    float best = -INFINITY;
+    int arg = RC_NONE;
+    for (int k = 0; k < bt.K; ++k) {
+      const float2 v = bt.r[k].work[i];
+      const float den = v.x * alpha;
+      if (den > 0.0f) {
+        const float ratio = __fdiv_rn(v.y * zmul, den);
+        if (ratio > best) {
+          best = ratio;
+          arg = bt.r[k].ridx;
+        }
+      }
+    }
+    if (arg != RC_NONE && best > Cbuf[i]) {
+      Cbuf[i] = best;
+      Abuf[i] = (uint8_t)arg;
+    }
+  }
+}
+
+// Backward: fields -> masked cotangents in place (the rule of k_cols_a_adj),
+// per-block partial sums of g C / zeta.
+__global__ void k_adj_elem(long n3, Batch bt, const float* __restrict__ g, const uint8_t* __restrict__ Abuf,
+                           const float* __restrict__ alpha_ptr, float* __restrict__ zpart) {
+  __shared__ float red[32];
+  const float alpha = fabsf(*alpha_ptr);
+  const float inv_alpha = 1.0f / alpha;  // exact: alpha is a power of two
+  float zacc = 0.0f;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += (long)gridDim.x * blockDim.x) {
+    const int a = Abuf[i];
+    for (int k = 0; k < bt.K; ++k) {
+      float2 q = make_float2(0.0f, 0.0f);
+      if (a == bt.r[k].ridx) {
+        const float2 v = bt.r[k].work[i];
+        const float rec = v.x;
+        const float h = v.y * inv_alpha;
+        const float C = __fdiv_rn(bt.zmul * h, rec);
+        const float gg = g[i];
+        const float ginv = __fdiv_rn(gg, rec);
+        q = make_float2(-ginv * C, ginv * bt.zmul * inv_alpha);
+        zacc += gg * __fdiv_rn(C, bt.zmul);
+      }
+      bt.r[k].work[i] = q;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) zacc += __shfl_xor_sync(0xffffffffu, zacc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = zacc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float s = 0.0f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
+    zpart[blockIdx.x] += s;
+  }
+}
+
+// Backward: acc += sum_k W(dk R_k |k|) box_k over the batch's forward-
+// transformed cotangent boxes (the accumulation of k_rows_adj_acc).
+__global__ void k_acc_elem(int N, Batch bt, float2* __restrict__ acc) {
+  const long n3 = (long)N * N * N;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += (long)gridDim.x * blockDim.x) {
+    const int c = (int)(i % N), b = (int)((i / N) % N), a = (int)(i / ((long)N * N));
+    const int ka = kfreq(a, N), kb = kfreq(b, N), kc = kfreq(c, N);
+    const float kmag = sqrtf((float)(ka * ka + kb * kb + kc * kc));
+    float2 sum = make_float2(0.0f, 0.0f);
+    for (int k = 0; k < bt.K; ++k) {
+      const float w = w_tophat(bt.r[k].dkR * kmag);
+      const float2 v = bt.r[k].work[i];
+      sum.x = fmaf(w, v.x, sum.x);
+      sum.y = fmaf(w, v.y, sum.y);
+    }
+    const float2 o = acc[i];
+    acc[i] = make_float2(o.x + sum.x, o.y + sum.y);
+  }
+}
+
+int adj_elem_blocks() { return kAdjElemBlocks; }
+cudaError_t launch_crit_elem(long n3, const Batch& bt, float* C, uint8_t* A, const float* alpha, cudaStream_t st) {
+  k_crit_elem<<<kAdjElemBlocks, 256, 0, st>>>(n3, bt, C, A, alpha);
+  return cudaGetLastError();
+}
+cudaError_t launch_adj_elem(long n3, const Batch& bt, const float* g, const uint8_t* A, const float* alpha,
+                            float* zpart, cudaStream_t st) {
+  k_adj_elem<<<kAdjElemBlocks, 256, 0, st>>>(n3, bt, g, A, alpha, zpart);
+  return cudaGetLastError();
+}
+cudaError_t launch_acc_elem(int N, const Batch& bt, float2* acc, cudaStream_t st) {
+  k_acc_elem<<<kAdjElemBlocks, 256, 0, st>>>(N, bt, acc);
+  return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------------------
 template <int N>
 struct AdjLaunch {

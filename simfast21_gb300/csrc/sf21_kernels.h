@@ -104,6 +104,15 @@ cudaError_t launch_cols_b_cb(int N, const Batch& bt, const float2* tw, cudaStrea
 cudaError_t launch_cols_a_test_cb(int N, const Batch& bt, uint8_t* rc, const float* alpha, const float2* tw, int nsm,
                                   cudaStream_t st);
 
+// b- and a-axis passes of a batch in one persistent launch through L2
+// (kernels_fused.cu, radius pipeline 8; column-block-major work boxes).
+// ctl: fused_ctl_ints(N) ints of device memory (zeroed by the launch).
+bool fused_supported(int N);
+size_t fused_ctl_ints(int N);
+cudaError_t fused_setup(int N);
+cudaError_t launch_cols_ba_fused(int N, const Batch& bt, uint8_t* rc, const float* alpha, const float2* tw, int* ctl,
+                                 int* err, int nsm, cudaStream_t st, uint32_t spin_limit = 0);
+
 // Criterion and adjoint (kernels_adj.cu).
 cudaError_t adj_setup(int N);
 int adj_zpart_blocks(int N);
@@ -112,6 +121,13 @@ cudaError_t launch_cols_a_crit(int N, const Batch& bt, float* C, uint8_t* A, con
 cudaError_t launch_cols_a_adj(int N, const Batch& bt, const float* g, const uint8_t* A, const float* alpha,
                               float* zpart, const float2* tw, cudaStream_t st);
 cudaError_t launch_rows_adj_acc(int N, const Batch& bt, float2* acc, const float2* tw, cudaStream_t st);
+// The same rules for any box side, as per-element passes over natural-layout
+// work boxes after whole-box transforms (the shared-memory transform family).
+int adj_elem_blocks();
+cudaError_t launch_crit_elem(long n3, const Batch& bt, float* C, uint8_t* A, const float* alpha, cudaStream_t st);
+cudaError_t launch_adj_elem(long n3, const Batch& bt, const float* g, const uint8_t* A, const float* alpha,
+                            float* zpart, cudaStream_t st);
+cudaError_t launch_acc_elem(int N, const Batch& bt, float2* acc, cudaStream_t st);
 cudaError_t launch_grad_finish(long n3, const float2* G, const float* alpha, const float* delta, const float* rec0,
                                float r2, float r3, float src_mul, float* gdelta, float* gsrc, cudaStream_t st);
 cudaError_t launch_crit_init(long n3, float* C, uint8_t* A, cudaStream_t st);

@@ -31,11 +31,11 @@ EXPORTS = [
     "sf21_hii_vjp", "sf21_hii_vjp_device", "sf21_hii_path", "sf21_hii_check", "sf21_hii_halo_source",
     "sf21_hii_run_z_halos", "sf21_hii_profile", "sf21_hii_profile_read", "sf21_hii_profile_name",
     "sf21_hii_halo_source_noalloc", "sf21_hii_power_spectrum", "sf21_hii_power_spectrum_device",
-    "sf21_t21_run_z", "sf21_hii_set_wait_limit", "sf21_hii_inject_alloc_failure",
+    "sf21_t21_run_z", "sf21_hii_set_wait_limit", "sf21_hii_inject_alloc_failure", "sf21_hii_batch_radii",
 ]
 
 
-NPATH = 7  # radius pipelines (FilterBank.path)
+NPATH = 8  # radius pipelines (FilterBank.path)
 
 
 class HIIError(RuntimeError):
@@ -99,6 +99,7 @@ def load_library(path: str = LIB_PATH):
     L.sf21_hii_check.argtypes = [vp]
     L.sf21_hii_set_wait_limit.argtypes = [vp, ctypes.c_uint]
     L.sf21_hii_inject_alloc_failure.argtypes = [ctypes.c_long]
+    L.sf21_hii_batch_radii.argtypes = [vp]
     L.sf21_hii_profile.argtypes = [vp, ctypes.c_int]
     L.sf21_hii_profile_read.argtypes = [vp, dp, ctypes.POINTER(ctypes.c_long), ctypes.c_int]
     L.sf21_hii_profile_name.argtypes = [ctypes.c_int]
@@ -182,10 +183,15 @@ class FilterBank:
         """(pipeline in use: 1 = three axis passes, 2 = plane clusters,
         3 = TMA-pipelined ky pass, 4 = TMA-pipelined ky and kx passes, and over
         column-block-major work boxes 5 = three axis passes, 6 = TMA ky pass,
-        7 = TMA ky and kx passes; {pipeline: tuned ms of one batch})."""
+        7 = TMA ky and kx passes, 8 = c-axis pass + one persistent ky/kx
+        launch through L2; {pipeline: tuned ms of one batch})."""
         ms = (ctypes.c_double * NPATH)()
         p = self._lib.sf21_hii_path(self._h, ms, NPATH)
         return p, {i + 1: ms[i] for i in range(NPATH)}
+
+    def batch_radii(self) -> int:
+        """Radii per spectrum read (K) in use (fixed by kmax or tuned)."""
+        return int(self._lib.sf21_hii_batch_radii(self._h))
 
     def check(self):
         """Raise if a bounded device wait expired since the last check."""

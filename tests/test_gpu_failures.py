@@ -31,7 +31,7 @@ def _boxes(N, L, seed=5):
     return synth.make_boxes(w, 7.5)
 
 
-@pytest.mark.parametrize("path", [6, 7, 3])
+@pytest.mark.parametrize("path", [6, 7, 3, 8])
 def test_wait_timeout_is_reported_and_the_context_recovers(hii, path):
     N, L = 128, 80.0
     sets = [(40.0, 20.0, 30)]

@@ -1,0 +1,153 @@
+"""The criterion and its hand-written adjoint on box sides that are not powers
+of two (the shared-memory 2-3-5 transform family; the reference's defaults
+are N_smoothed = 600 and N_halo = 1200).
+
+* 120^3 (L = 90 Mpc/h, z = 8, zeta = 30, Rmax = 20 Mpc/h, factor 1.05): the
+  VJP of the loss sum_x w(x) C(x) (w ~ U[0,1], seeded) with respect to
+  density, source and zeta against float64 central finite differences
+  (h = 1e-3 relative) at 200 voxels away from argmax ties, on the whole box.
+* 600^3 (L = 106.5 Mpc/h, z = 7, zeta = 30, Rmax = 35.5 Mpc/h): the criterion
+  against float64 on the whole box, and the VJP against the finite
+  differences of a 32^3-window loss at 40 voxels.
+
+Float64 on the GPU is used here only, as the checker.
+"""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from simfast21_gb300 import params as P, synth
+
+pytestmark = pytest.mark.gpu
+
+H_REL = 1e-3
+
+
+def _w_filter(x):
+    small = x < 0.03
+    xs = torch.where(small, torch.ones_like(x), x)
+    big = 3.0 * (-(torch.cos(xs) - (torch.sin(xs) / xs)) / xs / xs)
+    return torch.where(small, 3.0 * (1.0 / 3.0 - x * x / 30.0), big)
+
+
+def _rrec64(od, z, L, N, hubble=0.71):
+    """Rrec (user_functions.c:58-65) in float64 without the float rounding."""
+    rec1 = 1.e-24 * 9.84815696 * (1.0 + z) ** 5.06773134
+    rec2 = (od / 1.76105133) ** 0.81722878
+    rec3 = (rec2 / (1. + rec2)) ** 4.
+    dvv = (L * 3.0857e24 / N / hubble / (1. + z)) ** 3.0
+    return rec1 * rec3 * dvv / 1.e45
+
+
+def _run(hii, N, L, z, zeta, rmax, factor, seed, win0, win, nvox):
+    dev = torch.device("cuda")
+    w = synth.Workload(N=N, L=L, zs=[z], zeta=zeta, Rmax=rmax, factor=factor, seed=seed)
+    delta, sfrd = synth.make_boxes(w, z)
+    fb = hii.FilterBank(N, L, 0.71, [(zeta, rmax, w.Nbins)])
+    radii, nf = fb.radii()
+    d = torch.from_numpy(delta).to(dev)
+    s = torch.from_numpy(sfrd).to(dev)
+    C = torch.empty_like(d)
+    A = torch.empty(d.shape, dtype=torch.uint8, device=dev)
+    sl = tuple(slice(o, o + win) for o in win0)
+    wts = torch.from_numpy(np.random.default_rng(99).random((win,) * 3)).to(dev)
+    g = torch.zeros_like(d)
+    g[sl] = wts.float()
+    gd, gs = torch.empty_like(d), torch.empty_like(d)
+    fb.criterion_device(z, d.data_ptr(), s.data_ptr(), C.data_ptr(), A.data_ptr())
+    gz = fb.vjp_device(z, d.data_ptr(), s.data_ptr(), g.data_ptr(), gd.data_ptr(), gs.data_ptr())
+    torch.cuda.synchronize()
+    fb.check()
+    rec0, _, _ = fb.prologue(z, delta, sfrd)
+    fb.close()
+    # float64 fields on the window and the kernels on its offsets
+    dx = L / N
+    m = dx ** 3 * synth.qion(z)
+    h1 = (sfrd.astype(np.float64) * m).astype(np.float32)
+    dk = 2 * P.PI / L
+    f = torch.fft.fftfreq(N, d=1.0 / N, device=dev, dtype=torch.float64)
+    hh = torch.arange(N // 2 + 1, device=dev, dtype=torch.float64)
+    kmag = dk * torch.sqrt(f[:, None, None] ** 2 + f[None, :, None] ** 2 + hh[None, None, :] ** 2)
+    R0 = torch.fft.rfftn(torch.from_numpy(rec0).to(dev, torch.float64))
+    H0 = torch.fft.rfftn(torch.from_numpy(h1).to(dev, torch.float64))
+    n3 = float(N) ** 3
+    D = win - 1
+    kidx = torch.from_numpy(np.r_[N - D:N, 0:D + 1] % N).to(dev)
+    best = torch.full((N,) * 3, -math.inf, dtype=torch.float64, device=dev)
+    recs, hs, ks = [], [], []
+    for R in radii[:nf]:
+        W = _w_filter(kmag * R)
+        r = torch.fft.irfftn(R0 * W, s=(N, N, N)) * n3
+        h = torch.fft.irfftn(H0 * W, s=(N, N, N)) * n3
+        best = torch.maximum(best, torch.where(r > 0, zeta * h / r, torch.full_like(r, -math.inf)))
+        recs.append(r[sl].clone())
+        hs.append(h[sl].clone())
+        kf = torch.fft.irfftn(W.to(torch.complex128), s=(N, N, N)) * n3
+        ks.append(kf.index_select(0, kidx).index_select(1, kidx).index_select(2, kidx).clone())
+        del W, r, h, kf
+    C64 = torch.where(torch.isinf(best), torch.zeros_like(best), best)
+    dC = (C64 - C.double()).abs()
+    print(f"{N}^3: criterion max |C| {float(C64.abs().max()):.4g}, max |C32 - C64| {float(dC.max()):.3e}")
+    assert float(dC.max()) <= 1e-4 * float(C64.abs().max())
+
+    def crit(v=None, drec=0.0, dh=0.0):
+        b = torch.full((win,) * 3, -math.inf, dtype=torch.float64, device=dev)
+        t2 = torch.full_like(b, -math.inf)
+        for i in range(nf):
+            r, h = recs[i], hs[i]
+            if v is not None:
+                o = [D - (v[a] - win0[a]) for a in range(3)]
+                kr = ks[i][o[0]:o[0] + win, o[1]:o[1] + win, o[2]:o[2] + win]
+                r = r + drec * kr
+                h = h + dh * kr
+            ratio = torch.where(r > 0, zeta * h / r, torch.full_like(r, -math.inf))
+            t2 = torch.maximum(t2, torch.minimum(b, ratio))
+            b = torch.maximum(b, ratio)
+        return torch.where(torch.isinf(b), torch.zeros_like(b), b), t2
+
+    Cw, top2 = crit()
+    loss = lambda Cx: float((wts * Cx).sum())
+    gap = ((Cw - top2) / Cw.abs().clamp(min=1e-30)).cpu().numpy()
+    cand = np.argwhere(gap > 0.02)
+    picks = cand[np.random.default_rng(7).choice(len(cand), size=nvox, replace=False)]
+    gd_h, gs_h = gd.cpu(), gs.cpu()
+    rel_d, rel_s = [], []
+    for p in picks:
+        v = tuple(int(p[a]) + win0[a] for a in range(3))
+        dv = float(delta[v])
+        hstep = H_REL * max(abs(dv), 1e-3)
+        base = _rrec64(1.0 + dv, z, L, N)
+        Lp = loss(crit(v, drec=_rrec64(1.0 + dv + hstep, z, L, N) - base)[0])
+        Lm = loss(crit(v, drec=_rrec64(1.0 + dv - hstep, z, L, N) - base)[0])
+        rel_d.append((float(gd_h[v]), (Lp - Lm) / (2 * hstep)))
+        sv = float(sfrd[v])
+        sstep = H_REL * max(abs(sv), float(np.abs(sfrd[sl]).mean()))
+        Lp = loss(crit(v, dh=sstep * m)[0])
+        Lm = loss(crit(v, dh=-sstep * m)[0])
+        rel_s.append((float(gs_h[v]), (Lp - Lm) / (2 * sstep)))
+    fdz = loss(Cw) / zeta
+
+    def stats(pairs):
+        a = np.array(pairs)
+        scale = np.abs(a[:, 1]).max()
+        err = np.abs(a[:, 0] - a[:, 1]) / (np.abs(a[:, 1]) + 1e-3 * scale)
+        return np.median(err), np.quantile(err, 0.95)
+
+    md, q95d = stats(rel_d)
+    ms, q95s = stats(rel_s)
+    print(f"{N}^3: delta median {md:.2e} q95 {q95d:.2e}; src median {ms:.2e} q95 {q95s:.2e}; "
+          f"zeta adj {gz:.6e} fd {fdz:.6e}")
+    assert md < 1e-3 and q95d < 2e-2
+    assert ms < 1e-3 and q95s < 2e-2
+    assert abs(gz - fdz) <= 1e-3 * abs(fdz)
+
+
+def test_vjp_120_whole_box(hii):
+    # the window is the whole box: offsets wrap (kernel indices taken mod N)
+    _run(hii, 120, 90.0, 8.0, 30.0, 20.0, 1.05, 4321, (0, 0, 0), 120, 200)
+
+
+def test_criterion_and_vjp_600(hii):
+    _run(hii, 600, 106.5, 7.0, 30.0, 35.5, 1.05, 4242, (280, 100, 440), 32, 40)
