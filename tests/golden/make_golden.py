@@ -32,8 +32,9 @@ recipe on any machine and are not stored.
 
 Each holds the ini values, the input boxes per redshift, the xHII boxes the
 reference wrote, and its x_HI text output.  Needs the reference sources (only
-in the build container); the GPU tests read the committed .npz files.
-Usage: python tests/golden/make_golden.py [case-prefix ...]   (default: all)
+in the build container): REF_DIR or SF21_REF_DIR names their tree, as for
+``make -C oracle ref``; the GPU tests read the committed .npz files.
+Usage: SF21_REF_DIR=<tree> python tests/golden/make_golden.py [case-prefix ...]   (default: all)
 """
 from __future__ import annotations
 
