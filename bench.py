@@ -724,7 +724,8 @@ def run_ours(args, w, rank, world):
                          "peak_source": peak_kind, "traffic": traffic,
                          "traffic_source": "ncu capture, 512^3 K=8, scaled per launch" if traffic else None,
                          "pipeline_16B_per_voxel_radius_gbs": pipe_gbs,
-                         "pipeline_frac": (pipe_gbs / hbm) if pipe_gbs else None},
+                         "pipeline_frac": (pipe_gbs / hbm) if pipe_gbs else None,
+                         "step_16B_per_voxel_radius_frac": value / world * 16.0 / (hbm * 1e9)},
             "kernels_ms_per_step": {k: round(v[0] / steps, 3) for k, v in kinds.items()},
             "kernels_source": f"{prof_steps} separate step(s) with CUDA events around each launch",
             "clocks": clk.summary(),

@@ -7,8 +7,11 @@ are N_smoothed = 600 and N_halo = 1200).
   density, source and zeta against float64 central finite differences
   (h = 1e-3 relative) at 200 voxels away from argmax ties, on the whole box.
 * 600^3 (L = 106.5 Mpc/h, z = 7, zeta = 30, Rmax = 35.5 Mpc/h): the criterion
-  against float64 on the whole box, and the VJP against the finite
-  differences of a 32^3-window loss at 40 voxels.
+  against float64 on the whole box (each voxel within the error an FP32
+  field error of 2e-5 of the field's max can make of zeta h / r at its
+  argmax radius), and the VJP against the finite differences of a
+  32^3-window loss at 40 voxels.
+At 120^3 the criterion is held to the same bound.
 
 Float64 on the GPU is used here only, as the checker.
 """
@@ -23,6 +26,7 @@ from simfast21_gb300 import params as P, synth
 pytestmark = pytest.mark.gpu
 
 H_REL = 1e-3
+EPS_FIELD = 2e-5  # FP32 filtered-field error bound, relative to the field's max |value| (measured <= 2e-6)
 
 
 def _w_filter(x):
@@ -76,12 +80,20 @@ def _run(hii, N, L, z, zeta, rmax, factor, seed, win0, win, nvox):
     D = win - 1
     kidx = torch.from_numpy(np.r_[N - D:N, 0:D + 1] % N).to(dev)
     best = torch.full((N,) * 3, -math.inf, dtype=torch.float64, device=dev)
+    cond = torch.zeros_like(best)  # relative sensitivity of C to an FP32-sized field error
+    amb = torch.zeros(best.shape, dtype=torch.bool, device=dev)  # a radius whose rec_R sign FP32 may flip
     recs, hs, ks = [], [], []
     for R in radii[:nf]:
         W = _w_filter(kmag * R)
         r = torch.fft.irfftn(R0 * W, s=(N, N, N)) * n3
         h = torch.fft.irfftn(H0 * W, s=(N, N, N)) * n3
-        best = torch.maximum(best, torch.where(r > 0, zeta * h / r, torch.full_like(r, -math.inf)))
+        ratio = torch.where(r > 0, zeta * h / r, torch.full_like(r, -math.inf))
+        upd = ratio > best
+        best = torch.where(upd, ratio, best)
+        rmx = float(r.abs().max())
+        cond = torch.where(upd, EPS_FIELD * (rmx / r.abs() + float(h.abs().max()) / h.abs()), cond)
+        amb |= r.abs() <= EPS_FIELD * rmx
+        del ratio, upd
         recs.append(r[sl].clone())
         hs.append(h[sl].clone())
         kf = torch.fft.irfftn(W.to(torch.complex128), s=(N, N, N)) * n3
@@ -89,8 +101,20 @@ def _run(hii, N, L, z, zeta, rmax, factor, seed, win0, win, nvox):
         del W, r, h, kf
     C64 = torch.where(torch.isinf(best), torch.zeros_like(best), best)
     dC = (C64 - C.double()).abs()
-    print(f"{N}^3: criterion max |C| {float(C64.abs().max()):.4g}, max |C32 - C64| {float(dC.max()):.3e}")
-    assert float(dC.max()) <= 1e-4 * float(C64.abs().max())
+    # C = zeta h / r at the argmax radius: an error e max|field| in the FP32
+    # fields moves it by C (e max|r|/|r| + e max|h|/|h|); where the filtered
+    # recombination rate is near zero (top-hat ringing at the smallest radii)
+    # the ratio is ill-conditioned and a plain max-error bound does not apply
+    # (voxels where the sign of some rec_R is within that error of zero are
+    # left out: either ratio is admissible there; they are counted)
+    tol = C64.abs() * cond + 1e-7 * float(C64.abs().max())
+    bad = int(((dC > tol) & ~amb).sum())
+    n_amb = int(amb.sum())
+    print(f"{N}^3: criterion max |C| {float(C64.abs().max()):.4g}, max |C32 - C64| {float(dC.max()):.3e}, "
+          f"median relative {float((dC / C64.abs().clamp(min=1e-30)).median()):.2e}, "
+          f"sign-ambiguous voxels {n_amb}, outside the conditioning bound {bad}")
+    assert bad == 0
+    assert n_amb <= 1e-3 * N ** 3
 
     def crit(v=None, drec=0.0, dh=0.0):
         b = torch.full((win,) * 3, -math.inf, dtype=torch.float64, device=dev)
