@@ -113,6 +113,7 @@ struct sf21_hii_ctx {
   PipeMaps pmaps;
   int* d_err = nullptr;
   int* d_ctl = nullptr;     // work-queue control block of pipeline 8
+  unsigned int* d_rc32 = nullptr;  // pipeline 8: 32-bit first-hit box (atomicMin), folded into d_rc per set
   uint32_t wait_limit = 0;  // polls per bounded device wait (0 = the kernels' default)
   int nsm = 0;
   std::vector<SetInfo> sets;
@@ -330,6 +331,7 @@ static void free_ctx(sf21_hii_ctx* c) {
   if (c->d_work_base) cudaFree(c->d_work_base);
   if (c->d_err) cudaFree(c->d_err);
   if (c->d_ctl) cudaFree(c->d_ctl);
+  if (c->d_rc32) cudaFree(c->d_rc32);
   for (SetInfo& s : c->sets)
     if (s.d_nmax) cudaFree(s.d_nmax);
   for (cudaEvent_t e : c->ev) cudaEventDestroy(e);
@@ -492,7 +494,8 @@ extern "C" int sf21_hii_create(const sf21_hii_config* cfg, sf21_hii_ctx** out) {
     can_pipe = true;
   bool can_fused = false;
   if (!c->gen && fused_supported((int)N) && fused_setup((int)N) == cudaSuccess &&
-      dev_malloc(&c->d_ctl, sizeof(int) * fused_ctl_ints((int)N)) == cudaSuccess)
+      dev_malloc(&c->d_ctl, sizeof(int) * fused_ctl_ints((int)N)) == cudaSuccess &&
+      dev_malloc(&c->d_rc32, sizeof(unsigned int) * c->n3) == cudaSuccess)
     can_fused = true;
   cudaGetLastError();
   const int want = cfg->path;
@@ -693,7 +696,7 @@ static int enqueue_batch(sf21_hii_ctx* c, const Batch& bt, cudaStream_t st) {
     int e0 = mark(c, st);
     CTX_CUDA(c, launch_rows_filter_cb(N, c->d_spec, bt, c->d_tw, st));
     int e1 = mark(c, st);
-    CTX_CUDA(c, launch_cols_ba_fused(N, bt, c->d_rc, c->d_alpha, c->d_tw, c->d_ctl, c->d_err, c->nsm, st,
+    CTX_CUDA(c, launch_cols_ba_fused(N, bt, c->d_rc32, c->d_alpha, c->d_tw, c->d_ctl, c->d_err, c->nsm, st,
                                      c->wait_limit));
     int e2 = mark(c, st);
     span(c, KD_IROWS, e0, e1);
@@ -756,6 +759,7 @@ static int enqueue_radii(sf21_hii_ctx* c, int set, cudaStream_t st) {
   const SetInfo& s = c->sets[set];
   int rc;
   CTX_CUDA(c, cudaMemsetAsync(c->d_rc, RC_NONE, c->n3, st));
+  if (c->path == 8) CTX_CUDA(c, cudaMemsetAsync(c->d_rc32, 0xFF, sizeof(unsigned int) * c->n3, st));
   const int nr = (int)s.R.size();
   for (int k0 = 0; k0 < nr; k0 += c->K) {
     Batch bt;
@@ -770,6 +774,7 @@ static int enqueue_radii(sf21_hii_ctx* c, int set, cudaStream_t st) {
     }
     if ((rc = enqueue_batch(c, bt, st))) return rc;
   }
+  if (c->path == 8) CTX_CUDA(c, launch_rc32_to_rc(c->n3, c->d_rc32, c->d_rc, st));
   return SF21_OK;
 }
 

@@ -110,8 +110,10 @@ cudaError_t launch_cols_a_test_cb(int N, const Batch& bt, uint8_t* rc, const flo
 bool fused_supported(int N);
 size_t fused_ctl_ints(int N);
 cudaError_t fused_setup(int N);
-cudaError_t launch_cols_ba_fused(int N, const Batch& bt, uint8_t* rc, const float* alpha, const float2* tw, int* ctl,
-                                 int* err, int nsm, cudaStream_t st, uint32_t spin_limit = 0);
+// rc32: 32-bit first-hit box (all bits set = never), folded into the byte box by launch_rc32_to_rc
+cudaError_t launch_cols_ba_fused(int N, const Batch& bt, unsigned int* rc32, const float* alpha, const float2* tw,
+                                 int* ctl, int* err, int nsm, cudaStream_t st, uint32_t spin_limit = 0);
+cudaError_t launch_rc32_to_rc(long n3, const unsigned int* rc32, uint8_t* rc, cudaStream_t st);
 
 // Criterion and adjoint (kernels_adj.cu).
 cudaError_t adj_setup(int N);

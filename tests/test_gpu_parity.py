@@ -164,7 +164,7 @@ def test_plain_form_matches_reference(hii, oracle_lib, name):
     assert np.all((x == lo) | (x == hi))
 
 
-@pytest.mark.parametrize("N,L", [(64, 50.0), (128, 100.0)])
+@pytest.mark.parametrize("N,L", [(64, 50.0), (128, 100.0), (256, 150.0)])
 def test_radius_pipelines_agree(hii, N, L):
     """The radius pipelines -- three axis passes, the cluster plane pass
     (filter + kz + ky in distributed shared memory), the TMA-pipelined
