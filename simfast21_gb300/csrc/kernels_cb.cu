@@ -52,7 +52,7 @@ __device__ __forceinline__ void rows_filter_row(const float2* __restrict__ spec,
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
       const float w = w_tophat(dkR * kmag[r]);
-      v[r] = make_float2(z[r].x * w, z[r].y * w);
+      v[r] = filter_mul(z[r], w);
     }
     if (FftPP<N>::CALL_SYNC) __syncthreads();
     fft_line_pp<N, true>(v, s0, s1, stw, j);

@@ -91,7 +91,7 @@ k_inv_rows_filter(const float2* __restrict__ spec, Batch bt, const float2* __res
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
       const float w = w_tophat(dkR * kmag[r]);
-      v[r] = make_float2(z[r].x * w, z[r].y * w);
+      v[r] = filter_mul(z[r], w);
     }
     fft_line<N, true>(v, sbuf + row_in_cta * L::LS, stw, j);
     float2* dst = bt.r[k].work + row * N;

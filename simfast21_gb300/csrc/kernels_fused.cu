@@ -68,7 +68,7 @@ __device__ __forceinline__ void discard_l2_line(const void* p) {
 // already met when it is taken.
 template <int N>
 struct FusedGeom {
-  static constexpr int G = 4;       // tiles per queue item
+  static constexpr int G = 4;       // tiles per queue item (even: processed in pairs)
   static constexpr int NG = N / G;  // groups per unit and kind
 };
 
@@ -207,19 +207,11 @@ k_cols_ba_fused(Batch bt, unsigned int* __restrict__ rc32, const float* __restri
     bool next_loaded = false;
     const int k = u / NBLK, cb = u % NBLK;
     const unsigned int ridx = (unsigned int)bt.r[k].ridx;
-#pragma unroll 1
-    for (int g = 0; g < F::G; ++g) {
-      const int t = t0 + g;
-      // prefetch: the group's next tile, or the next item's first tile
-      if (g + 1 < F::G) {
-        load(vb, kind, u, t + 1);
-      } else if (next_ready) {
-        load(vb, nkind, nu, nt0);
-        next_loaded = true;
-      }
+    // transform + store (b axis) or centre test (a axis) of tile t held in v
+    auto process = [&](float2 (&v)[8], int t, bool first) {
       if (FftPP<N>::CALL_SYNC) __syncthreads();
-      fft_line_pp<N, true>(va, s0, s1, stw, j);
-      if (g == 0 && threadIdx.x == 0) {
+      fft_line_pp<N, true>(v, s0, s1, stw, j);
+      if (first && threadIdx.x == 0) {
         publish();  // the previous group (every thread's stores precede the transform's barriers)
         if (has_next) {
           s_pos[safter] = pafter;
@@ -229,7 +221,7 @@ k_cols_ba_fused(Batch bt, unsigned int* __restrict__ rc32, const float* __restri
       float2* p = tile_ptr(kind, u, t);
       if (kind == 0) {
 #pragma unroll
-        for (int r = 0; r < 8; ++r) p[(j + r * (N / 8)) * CW] = va[r];
+        for (int r = 0; r < 8; ++r) p[(j + r * (N / 8)) * CW] = v[r];
       } else {
         // every thread has read the tile's N lines of CW values (the
         // transform's exchanges are behind barriers): drop them from L2
@@ -238,13 +230,24 @@ k_cols_ba_fused(Batch bt, unsigned int* __restrict__ rc32, const float* __restri
         const int c = cb * CW + col;
 #pragma unroll
         for (int r = 0; r < 8; ++r) {
-          if (is_centre(va[r], alpha, zmul)) atomicMin(rc32 + ((long)(j + r * (N / 8)) * N + t) * N + c, ridx);
+          if (is_centre(v[r], alpha, zmul)) atomicMin(rc32 + ((long)(j + r * (N / 8)) * N + t) * N + c, ridx);
         }
       }
-      if (g + 1 < F::G || next_loaded) {
-#pragma unroll
-        for (int r = 0; r < 8; ++r) va[r] = vb[r];
+    };
+    // the group's tiles in pairs, the two register sets in turn (no copies):
+    // each set's next tile -- or the next item's first tile -- is loaded
+    // before the other set's transform
+#pragma unroll 1
+    for (int g = 0; g < F::G; g += 2) {
+      load(vb, kind, u, t0 + g + 1);
+      process(va, t0 + g, g == 0);
+      if (g + 2 < F::G) {
+        load(va, kind, u, t0 + g + 2);
+      } else if (next_ready) {
+        load(va, nkind, nu, nt0);
+        next_loaded = true;
       }
+      process(vb, t0 + g + 1, false);
     }
     // group done: every thread's stores are in; the release goes out later
     __syncthreads();

@@ -290,7 +290,7 @@ __global__ void __launch_bounds__(GR_THREADS) k_gen_rows(GenRowsArgs ga, GenPlan
       const float2 z = zs[l * N + c];
       if (ga.mode == 2) {
         const float w = w_tophat(ga.bt.r[k].dkR * kmag);
-        b0[l * N + c] = make_float2(z.x * w, z.y * w);
+        b0[l * N + c] = filter_mul(z, w);
       } else {
         const HfPair& pr = ga.hb.p[k];
         const float wa = ga.hb.scale * w_tophat(pr.dkRa * kmag);

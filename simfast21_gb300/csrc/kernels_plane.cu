@@ -70,7 +70,7 @@ k_plane_filter(const float2* __restrict__ spec, Batch bt, const float2* __restri
           const int kc = kfreq(c, N);
           const float w = w_tophat(dkR * sqrtf((float)(kab + kc * kc)));
           const float2 zz = src[c];
-          v[r] = make_float2(zz.x * w, zz.y * w);
+          v[r] = filter_mul(zz, w);
         }
         float2* s = slice + bl * G::LS;
         fft_line<N, true>(v, s, stw, j);

@@ -61,8 +61,19 @@ __device__ __forceinline__ float w_tophat(float x) {
 // v.y > 0 && v.y * zeta >= v.x * alpha (alpha a power of two: exact scaling).
 // The one difference, a NaN rec, does not arise from finite boxes.
 // alpha <= 0 marks an ionisation box that is zero everywhere: no centre.
+// Both products are rounded explicitly (__fmul_rn): left to the compiler,
+// the comparison may become one fused multiply-add in one kernel and two
+// rounded products in another, and the radius pipelines would then disagree
+// on centres within an ulp of the threshold.
 __device__ __forceinline__ bool is_centre(float2 v, float alpha, float zeta) {
-  return (alpha > 0.0f) && (v.y > 0.0f) && (v.y * zeta >= v.x * alpha);
+  return (alpha > 0.0f) && (v.y > 0.0f) && (__fmul_rn(v.y, zeta) >= __fmul_rn(v.x, alpha));
+}
+
+// The top-hat filter applied to a spectrum value, rounded as two products
+// (no contraction into the transform's first additions, so every pipeline
+// filters with the same bits).
+__device__ __forceinline__ float2 filter_mul(float2 z, float w) {
+  return make_float2(__fmul_rn(z.x, w), __fmul_rn(z.y, w));
 }
 
 // Signed frequency index of position i on an N-point axis (:309-311).
