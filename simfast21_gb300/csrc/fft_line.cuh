@@ -62,8 +62,13 @@ __device__ __forceinline__ void load_twiddles(float2* stw, const float2* __restr
 
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+// Every product that feeds an addition in the line transforms is written as
+// an explicit fused multiply-add (the other product rounded on its own):
+// left to the compiler, the contraction may differ between two kernels that
+// inline the same transform, and their outputs would then differ in the last
+// bit.  Written out, every kernel built on these transforms gets the same bits.
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
-  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+  return make_float2(fmaf(a.x, b.x, -__fmul_rn(a.y, b.y)), fmaf(a.x, b.y, __fmul_rn(a.y, b.x)));
 }
 // multiply by -i (forward) or +i (inverse)
 template <bool INV>
@@ -89,25 +94,26 @@ __device__ __forceinline__ void dft8(float2 (&v)[8]) {
   float2 o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
   dft4<INV>(e0, e1, e2, e3);
   dft4<INV>(o0, o1, o2, o3);
-  // twiddles w8^k, w8 = exp(-/+ i pi/4)
-  float2 w1o, w2o, w3o;
+  // twiddles w8^k, w8 = exp(-/+ i pi/4): w8 o = h s with s a sum of the
+  // parts of o, applied as e + h s and e - h s (explicit fused multiply-adds)
+  float2 s1, s3, w2o;
   if (!INV) {
-    w1o = make_float2(h * (o1.x + o1.y), h * (o1.y - o1.x));
+    s1 = make_float2(o1.x + o1.y, o1.y - o1.x);
     w2o = make_float2(o2.y, -o2.x);
-    w3o = make_float2(h * (o3.y - o3.x), -h * (o3.x + o3.y));
+    s3 = make_float2(o3.y - o3.x, -(o3.x + o3.y));
   } else {
-    w1o = make_float2(h * (o1.x - o1.y), h * (o1.x + o1.y));
+    s1 = make_float2(o1.x - o1.y, o1.x + o1.y);
     w2o = make_float2(-o2.y, o2.x);
-    w3o = make_float2(-h * (o3.x + o3.y), h * (o3.x - o3.y));
+    s3 = make_float2(-(o3.x + o3.y), o3.x - o3.y);
   }
   v[0] = cadd(e0, o0);
   v[4] = csub(e0, o0);
-  v[1] = cadd(e1, w1o);
-  v[5] = csub(e1, w1o);
+  v[1] = make_float2(fmaf(h, s1.x, e1.x), fmaf(h, s1.y, e1.y));
+  v[5] = make_float2(fmaf(-h, s1.x, e1.x), fmaf(-h, s1.y, e1.y));
   v[2] = cadd(e2, w2o);
   v[6] = csub(e2, w2o);
-  v[3] = cadd(e3, w3o);
-  v[7] = csub(e3, w3o);
+  v[3] = make_float2(fmaf(h, s3.x, e3.x), fmaf(h, s3.y, e3.y));
+  v[7] = make_float2(fmaf(-h, s3.x, e3.x), fmaf(-h, s3.y, e3.y));
 }
 
 // Offset of the twiddles of radix-8 stage st (st >= 1) in the table.
