@@ -713,7 +713,7 @@ def run_ours(args, w, rank, world):
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded lognormal density + SFRD boxes)",
             "config": {"workload": describe(w), "form": "batched (one shared forward transform, "
                        "one CUDA graph per step)", "N": N, "sets": nsets, "radii_total": R_total,
-                       "pipeline": PIPELINES[path][1],
+                       "pipeline": PIPELINES[path][1], "batch_radii": fb.batch_radii(),
                        "tuned_batch_ms": {PIPELINES[p][0]: tuned[p] for p in PIPELINES},
                        "flush": "inputs larger than L2 (every box >= 537 MB)"},
             "e2e": {"value": e2e_val, "unit": "voxel*radii/s",
