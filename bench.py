@@ -619,7 +619,7 @@ def run_ours(args, w, rank, world):
     del d_plain
 
     # differentiation: criterion forward and hand-written VJP (bwd/fwd),
-    # 256^3 (L=200, z=8, zeta=30, Rmax=60, factor 1.05) and, with --grad-large,
+    # 256^3 (L=200, z=8, zeta=30, Rmax=60, factor 1.05) and, unless --no-grad-large,
     # 1024^3 (L=500, z=7, Rmax=80, factor 1.12) with peak HBM
     grad = None
     if not args.no_grad:
