@@ -29,7 +29,7 @@ SFR_DRIVER = os.path.join(HERE, "sf21_get_SFR")  # drop-in for get_SFR.x
 SFR_DRIVER_SRC = [os.path.join(HERE, "driver", f) for f in ("sf21_get_SFR_main.c", "sf21_stage.c")]
 SOURCES = ["kernels_fft.cu", "kernels_plane.cu", "kernels_pipe.cu", "kernels_adj.cu", "kernels_elem.cu",
            "kernels_plain.cu", "kernels_halo.cu", "kernels_cb.cu", "kernels_dt.cu", "kernels_pk.cu", "kernels_t21.cu",
-           "kernels_hf.cu", "kernels_sg.cu", "kernels_gen.cu", "kernels_fused.cu", "hii_api.cu", "halo_api.cu", "sfr_api.cu"]
+           "kernels_hf.cu", "kernels_sg.cu", "kernels_gen.cu", "kernels_fused.cu", "kernels_gen600.cu", "hii_api.cu", "halo_api.cu", "sfr_api.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3"]
 

@@ -442,6 +442,7 @@ extern "C" int sf21_hii_create(const sf21_hii_config* cfg, sf21_hii_ctx** out) {
   if (c->gen) {
     c->gp = gen_plan((int)N);
     CREATE_CUDA(gen_setup((int)N));
+    if (gen600_supported((int)N)) CREATE_CUDA(gen600_setup());
   } else {
     CREATE_CUDA(fft_setup((int)N));
     CREATE_CUDA(cb_setup((int)N));
@@ -640,9 +641,11 @@ static cudaError_t x_cols(sf21_hii_ctx* c, float2* box, const Batch& bt, int nbo
                           cudaStream_t st) {
   if (!c->gen) return launch_cols((int)c->N, box, bt, nbox, axis, inverse, c->d_tw, st);
   if (!box && nbox != bt.K) return cudaErrorInvalidValue;
+  if (gen600_supported((int)c->N)) return launch_gen600_cols(box, bt, axis, inverse, c->d_tw, st);
   return launch_gen_cols(c->gp, box, bt, axis, inverse, c->d_tw, st);
 }
 static cudaError_t x_cols_a_test(sf21_hii_ctx* c, const Batch& bt, cudaStream_t st) {
+  if (c->gen && gen600_supported((int)c->N)) return launch_gen600_cols_a_test(bt, c->d_rc, c->d_alpha, c->d_tw, st);
   return c->gen ? launch_gen_cols_a_test(c->gp, bt, c->d_rc, c->d_alpha, c->d_tw, st)
                 : launch_cols_a_test((int)c->N, bt, c->d_rc, c->d_alpha, c->d_tw, st);
 }

@@ -272,6 +272,16 @@ struct GenPlan {
   int nst;        // stages
   int radix[16];  // radix of each stage (8, 4, 2, 3 or 5)
 };
+// Register-resident b- and a-axis passes for N = 600 (kernels_gen600.cu):
+// 600 = 24 x 25, one shared-memory exchange per line.  Same arguments and
+// results (to rounding) as launch_gen_cols / launch_gen_cols_a_test; twiddles:
+// the plain table of the shared-memory family.
+bool gen600_supported(int N);
+cudaError_t gen600_setup();
+cudaError_t launch_gen600_cols(float2* box0, const Batch& bt, int axis, bool inverse, const float2* tw,
+                               cudaStream_t st);
+cudaError_t launch_gen600_cols_a_test(const Batch& bt, uint8_t* rc, const float* alpha, const float2* tw,
+                                      cudaStream_t st);
 bool gen_supported(int N);
 GenPlan gen_plan(int N);
 cudaError_t gen_setup(int N);

@@ -183,3 +183,22 @@ def test_xhii_256_every_redshift(hii, oracle_lib):
             print(f"z={z:.3f}: differences from the full restatement {n_ref}")
         print(f"z={z:.3f}: neutral {nf[0]:.6f}, band voxels {n_band}, differences from the low bound {n_diff}")
     fb.close()
+
+
+def test_xhii_600_matches_oracle(hii, oracle_lib):
+    """The reference's default side N_smoothed = 600 (the 2-3-5 transform
+    family: shared-memory row passes and the register-resident 24 x 25
+    column passes), one parameter set at L = 106.5 Mpc/h, z = 7: xHII
+    bit-identical with the oracle outside the band, the first hit within the
+    FP64 bounds."""
+    N, L, z, h = 600, 106.5, 7.0, 0.71
+    st = (30.0, 35.5, 109)
+    delta, sfrd = synth.make_boxes(synth.Workload(N=N, L=L, zs=[z], seed=4242), z)
+    fb = hii.FilterBank(N, L, h, [st])
+    x, _ = fb.run_z(z, delta, sfrd)
+    radii, nf = fb.radii()
+    rc = fb.first_hit(z, delta, sfrd)
+    ex = _prologue(oracle_lib, N, L, h, st, z, delta, sfrd)
+    n_band, n_diff, _ = _check(torch.from_numpy(x[0]).cuda(), ex, radii, L / N, 2 * P.PI / L, rc)
+    print(f"600^3: {len(radii)} radii ({nf} FFT), band voxels {n_band}, differences from the low bound {n_diff}")
+    fb.close()
