@@ -626,13 +626,20 @@ extern "C" int sf21_hii_radii(const sf21_hii_ctx* ctx, int set, double* R, int c
 // ---- transform passes: register kernels (power-of-two sides) or shared-memory
 // kernels (other sides), same arguments ------------------------------------
 static cudaError_t x_fwd_rows(sf21_hii_ctx* c, const float2* in, float2* out, const float* alpha, cudaStream_t st) {
+  Batch none;
+  memset(&none, 0, sizeof(none));
+  if (c->gen && gen600_supported((int)c->N)) return launch_gen600_rows(0, in, out, none, alpha, c->d_tw, st);
   return c->gen ? launch_gen_fwd_rows(c->gp, in, out, alpha, c->d_tw, st)
                 : launch_fwd_rows((int)c->N, in, out, alpha, c->d_tw, st);
 }
 static cudaError_t x_inv_rows_plain(sf21_hii_ctx* c, float2* box, cudaStream_t st) {
+  Batch none;
+  memset(&none, 0, sizeof(none));
+  if (c->gen && gen600_supported((int)c->N)) return launch_gen600_rows(1, box, box, none, nullptr, c->d_tw, st);
   return c->gen ? launch_gen_inv_rows_plain(c->gp, box, c->d_tw, st) : launch_inv_rows_plain((int)c->N, box, c->d_tw, st);
 }
 static cudaError_t x_inv_rows_filter(sf21_hii_ctx* c, const float2* spec, const Batch& bt, cudaStream_t st) {
+  if (c->gen && gen600_supported((int)c->N)) return launch_gen600_rows(2, spec, nullptr, bt, nullptr, c->d_tw, st);
   return c->gen ? launch_gen_inv_rows_filter(c->gp, spec, bt, c->d_tw, st)
                 : launch_inv_rows_filter((int)c->N, spec, bt, c->d_tw, st);
 }
@@ -1270,7 +1277,7 @@ extern "C" int sf21_hii_vjp_device(sf21_hii_ctx* c, double z, int kind, const fl
     int e2 = mark(c, st);
     if (c->gen) {  // c-axis forward of each box, then W and the sum over the batch
       for (int k = 0; k < bt.K; ++k)
-        CTX_CUDA(c, launch_gen_fwd_rows(c->gp, bt.r[k].work, bt.r[k].work, nullptr, c->d_tw, st));
+        CTX_CUDA(c, x_fwd_rows(c, bt.r[k].work, bt.r[k].work, nullptr, st));
       CTX_CUDA(c, launch_acc_elem(N, bt, c->d_acc, st));
     } else {
       CTX_CUDA(c, launch_rows_adj_acc(N, bt, c->d_acc, c->d_tw, st));

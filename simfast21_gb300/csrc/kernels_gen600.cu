@@ -199,6 +199,91 @@ __global__ void __launch_bounds__(g600::THREADS, 3) k_gen600_cols(float2* box0, 
 
 bool gen600_supported(int N) { return N == g600::N; }
 
+// ---- c-axis (rows) pass: one warp per row ---------------------------------
+// Lane n1 < 24 holds x[n1 + 24 n2] (for fixed n2 the 24 lanes read 24
+// consecutive values: coalesced); lane k2 < 25 holds the outputs 25 k1 + k2
+// (for fixed k1, 25 consecutive values: coalesced stores).  The exchange is
+// the warp's own shared-memory block (stride 25 float2 per k2: the reads by
+// k2 meet distinct banks), so a row needs no CTA barrier.
+// MODE 0: forward, imaginary part times |alpha| (the packed prologue box);
+// MODE 1: inverse in place; MODE 2: inverse of the spectrum row times the
+// top-hat filter of each of the batch's K radii, into the K work boxes.
+namespace g600 {
+constexpr int RW = 8;                      // rows (warps) per CTA
+constexpr int RTHREADS = 32 * RW;
+constexpr int XS = N2 * N2;                // exchange float2 per warp (25 k2 x stride 25)
+constexpr size_t RSMEM = (size_t)(N + RW * (XS + N)) * sizeof(float2);  // twiddles, exchange + spectrum row per warp
+}  // namespace g600
+
+template <int MODE>
+__global__ void __launch_bounds__(g600::RTHREADS, 2) k_gen600_rows(const float2* in, float2* out, Batch bt,
+                                                                  const float* __restrict__ alpha_ptr,
+                                                                  const float2* __restrict__ gtw) {
+  using namespace g600;
+  constexpr bool INV = MODE != 0;
+  extern __shared__ float2 gsm[];
+  float2* tw = gsm;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  float2* ex = gsm + N + w * (XS + N);
+  float2* zrow = ex + XS;
+  for (int t = threadIdx.x; t < N; t += RTHREADS) tw[t] = gtw[t];
+  __syncthreads();
+  const long row = (long)blockIdx.x * RW + w;
+  const float2* src = in + row * N;
+  const int nout = MODE == 2 ? bt.K : 1;
+  float alpha = 1.0f;
+  if (MODE == 0 && alpha_ptr) alpha = fabsf(*alpha_ptr);
+  int kab = 0;
+  if (MODE == 2) {
+    const int a = (int)(row / N), b = (int)(row % N);
+    const int ka = kfreq(a, N), kb = kfreq(b, N);
+    kab = ka * ka + kb * kb;
+    for (int c = lane; c < N; c += 32) zrow[c] = src[c];
+    __syncwarp();
+  }
+  for (int k = 0; k < nout; ++k) {
+    if (lane < N1) {
+      float2 y[25];
+#pragma unroll
+      for (int n2 = 0; n2 < 25; ++n2) {
+        const int c = lane + N1 * n2;
+        if (MODE == 2) {
+          const int kc = kfreq(c, N);
+          const float kmag = sqrtf((float)(kab + kc * kc));
+          y[n2] = filter_mul(zrow[c], w_tophat(bt.r[k].dkR * kmag));
+        } else {
+          float2 v = src[c];
+          if (MODE == 0) v.y *= alpha;
+          y[n2] = v;
+        }
+      }
+      dft25<INV>(y, tw);
+#pragma unroll
+      for (int l1 = 0; l1 < 5; ++l1)
+#pragma unroll
+        for (int l2 = 0; l2 < 5; ++l2) {
+          const int k2 = l1 + 5 * l2;
+          float2 v = y[5 * l1 + l2];
+          if (k2 > 0 && lane > 0) v = cmul(v, twc<INV>(tw, lane * k2));  // w600^(n1 k2)
+          ex[k2 * N2 + lane] = v;
+        }
+    }
+    __syncwarp();
+    if (lane < N2) {
+      float2 u[24];
+#pragma unroll
+      for (int n1 = 0; n1 < 24; ++n1) u[n1] = ex[lane * N2 + n1];
+      dft24<INV>(u, tw);
+      float2* dst = (MODE == 2 ? bt.r[k].work : out) + row * N + lane;
+#pragma unroll
+      for (int q1 = 0; q1 < 8; ++q1)
+#pragma unroll
+        for (int q2 = 0; q2 < 3; ++q2) dst[25 * (q1 + 8 * q2)] = u[3 * q1 + q2];
+    }
+    __syncwarp();  // the exchange is free for the next radius
+  }
+}
+
 template <bool INV, int EPI, int AXIS>
 static cudaError_t g600_attr() {
   return cudaFuncSetAttribute(k_gen600_cols<INV, EPI, AXIS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -210,7 +295,24 @@ cudaError_t gen600_setup() {
   if ((e = g600_attr<true, 0, 0>()) || (e = g600_attr<true, 0, 1>()) || (e = g600_attr<false, 0, 0>()) ||
       (e = g600_attr<false, 0, 1>()))
     return e;
-  return g600_attr<true, 1, 0>();
+  if ((e = g600_attr<true, 1, 0>())) return e;
+  for (auto f : {k_gen600_rows<0>, k_gen600_rows<1>, k_gen600_rows<2>})
+    if ((e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g600::RSMEM))) return e;
+  return cudaSuccess;
+}
+
+cudaError_t launch_gen600_rows(int mode, const float2* in, float2* out, const Batch& bt, const float* alpha,
+                               const float2* tw, cudaStream_t st) {
+  const unsigned grid = (unsigned)((long)g600::N * g600::N / g600::RW);
+  const int T = g600::RTHREADS;
+  const size_t S = g600::RSMEM;
+  if (mode == 0)
+    k_gen600_rows<0><<<grid, T, S, st>>>(in, out, bt, alpha, tw);
+  else if (mode == 1)
+    k_gen600_rows<1><<<grid, T, S, st>>>(in, out, bt, nullptr, tw);
+  else
+    k_gen600_rows<2><<<grid, T, S, st>>>(in, nullptr, bt, nullptr, tw);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_gen600_cols(float2* box0, const Batch& bt, int axis, bool inverse, const float2* tw,

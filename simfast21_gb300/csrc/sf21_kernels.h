@@ -280,6 +280,11 @@ bool gen600_supported(int N);
 cudaError_t gen600_setup();
 cudaError_t launch_gen600_cols(float2* box0, const Batch& bt, int axis, bool inverse, const float2* tw,
                                cudaStream_t st);
+// rows: mode 0 forward (in -> out, imaginary part times |*alpha|), 1 inverse
+// in place (in == out), 2 inverse of the spectrum times the batch's filters
+// (in = spectrum -> bt.r[k].work)
+cudaError_t launch_gen600_rows(int mode, const float2* in, float2* out, const Batch& bt, const float* alpha,
+                               const float2* tw, cudaStream_t st);
 cudaError_t launch_gen600_cols_a_test(const Batch& bt, uint8_t* rc, const float* alpha, const float2* tw,
                                       cudaStream_t st);
 bool gen_supported(int N);
