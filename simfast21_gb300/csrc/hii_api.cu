@@ -628,27 +628,29 @@ extern "C" int sf21_hii_radii(const sf21_hii_ctx* ctx, int set, double* R, int c
 static cudaError_t x_fwd_rows(sf21_hii_ctx* c, const float2* in, float2* out, const float* alpha, cudaStream_t st) {
   Batch none;
   memset(&none, 0, sizeof(none));
-  if (c->gen && gen600_supported((int)c->N)) return launch_gen600_rows(0, in, out, none, alpha, c->d_tw, st);
+  if (c->gen && gen600_supported((int)c->N)) return launch_gen600_rows(0, in, out, none, alpha, c->d_tw, false, st);
   return c->gen ? launch_gen_fwd_rows(c->gp, in, out, alpha, c->d_tw, st)
                 : launch_fwd_rows((int)c->N, in, out, alpha, c->d_tw, st);
 }
 static cudaError_t x_inv_rows_plain(sf21_hii_ctx* c, float2* box, cudaStream_t st) {
   Batch none;
   memset(&none, 0, sizeof(none));
-  if (c->gen && gen600_supported((int)c->N)) return launch_gen600_rows(1, box, box, none, nullptr, c->d_tw, st);
+  if (c->gen && gen600_supported((int)c->N)) return launch_gen600_rows(1, box, box, none, nullptr, c->d_tw, false, st);
   return c->gen ? launch_gen_inv_rows_plain(c->gp, box, c->d_tw, st) : launch_inv_rows_plain((int)c->N, box, c->d_tw, st);
 }
-static cudaError_t x_inv_rows_filter(sf21_hii_ctx* c, const float2* spec, const Batch& bt, cudaStream_t st) {
-  if (c->gen && gen600_supported((int)c->N)) return launch_gen600_rows(2, spec, nullptr, bt, nullptr, c->d_tw, st);
+// cb: the radius pipeline's batch in the column-block-major layout (N = 600 only)
+static cudaError_t x_inv_rows_filter(sf21_hii_ctx* c, const float2* spec, const Batch& bt, cudaStream_t st,
+                                     bool cb = false) {
+  if (c->gen && gen600_supported((int)c->N)) return launch_gen600_rows(2, spec, nullptr, bt, nullptr, c->d_tw, cb, st);
   return c->gen ? launch_gen_inv_rows_filter(c->gp, spec, bt, c->d_tw, st)
                 : launch_inv_rows_filter((int)c->N, spec, bt, c->d_tw, st);
 }
 // box, or (box null) the batch's nbox = bt.K boxes
 static cudaError_t x_cols(sf21_hii_ctx* c, float2* box, const Batch& bt, int nbox, int axis, bool inverse,
-                          cudaStream_t st) {
+                          cudaStream_t st, bool cb = false) {
   if (!c->gen) return launch_cols((int)c->N, box, bt, nbox, axis, inverse, c->d_tw, st);
   if (!box && nbox != bt.K) return cudaErrorInvalidValue;
-  if (gen600_supported((int)c->N)) return launch_gen600_cols(box, bt, axis, inverse, c->d_tw, st);
+  if (gen600_supported((int)c->N)) return launch_gen600_cols(box, bt, axis, inverse, cb, c->d_tw, st);
   return launch_gen_cols(c->gp, box, bt, axis, inverse, c->d_tw, st);
 }
 static cudaError_t x_cols_a_test(sf21_hii_ctx* c, const Batch& bt, cudaStream_t st) {
@@ -752,10 +754,12 @@ static int enqueue_batch(sf21_hii_ctx* c, const Batch& bt, cudaStream_t st) {
     span(c, KD_ICA, e2, e3);
     return SF21_OK;
   }
+  // at N = 600 the batch's boxes are column-block major (the a-axis test pass reads them so)
+  const bool cb600 = c->gen && gen600_supported(N);
   int e0 = mark(c, st);
-  CTX_CUDA(c, x_inv_rows_filter(c, c->d_spec, bt, st));
+  CTX_CUDA(c, x_inv_rows_filter(c, c->d_spec, bt, st, cb600));
   int e1 = mark(c, st);
-  CTX_CUDA(c, x_cols(c, nullptr, bt, bt.K, 1, true, st));
+  CTX_CUDA(c, x_cols(c, nullptr, bt, bt.K, 1, true, st, cb600));
   int e2 = mark(c, st);
   CTX_CUDA(c, x_cols_a_test(c, bt, st));
   int e3 = mark(c, st);

@@ -27,7 +27,7 @@ namespace g600 {
 constexpr int N = 600, N1 = 24, N2 = 25, CW = 8, ROWS = 28;
 constexpr int THREADS = CW * ROWS;       // 224: step 1 uses rows 0..23, step 2 rows 0..24
 constexpr int EXS = N1 * CW + CW;        // float2 per k2 slab of the exchange (padded)
-constexpr size_t SMEM = (size_t)(N + N2 * EXS) * sizeof(float2) + (size_t)N * CW;  // twiddles, exchange, hits
+constexpr size_t SMEM = (size_t)(N + N2 * EXS) * sizeof(float2);  // twiddles, exchange
 }  // namespace g600
 
 template <bool INV>
@@ -117,8 +117,12 @@ __device__ __forceinline__ void dft24(float2 (&u)[24], const float2* tw) {
 
 // EPI 0: transform in place (box0, or the batch's K boxes); EPI 1: inverse,
 // centre test and first-hit update of the batch's K boxes (the transform is
-// not stored).  AXIS 1: lines along b (stride N); AXIS 0: along a (N^2).
-template <bool INV, int EPI, int AXIS>
+// not stored).  AXIS 1: lines along b; AXIS 0: along a.  LAYOUT 0: natural
+// boxes (a N^2 + b N + c: a-axis rows N^2 apart, 600 rows of a tile on 600
+// pages); LAYOUT 1: the radius batch's work boxes column-block major,
+// ((c / 8) N + a) N + b) 8 + c mod 8, where a b-axis tile is one contiguous
+// run and an a-axis tile stays inside one 23 MB slab.
+template <bool INV, int EPI, int AXIS, int LAYOUT>
 __global__ void __launch_bounds__(g600::THREADS, 3) k_gen600_cols(float2* box0, Batch bt, uint8_t* rc,
                                                                const float* __restrict__ alpha_ptr,
                                                                const float2* __restrict__ gtw) {
@@ -126,20 +130,23 @@ __global__ void __launch_bounds__(g600::THREADS, 3) k_gen600_cols(float2* box0, 
   extern __shared__ float2 gsm[];
   float2* tw = gsm;
   float2* ex = gsm + N;
-  uint8_t* hit = reinterpret_cast<uint8_t*>(ex + N2 * EXS);  // [row][col]
   for (int t = threadIdx.x; t < N; t += THREADS) tw[t] = gtw[t];
   const int col = threadIdx.x % CW, r = threadIdx.x / CW;
   const int nblk = N / CW;
   const int outer = blockIdx.x / nblk;
   const int c0 = (blockIdx.x % nblk) * CW;
-  constexpr long stride = AXIS == 1 ? (long)N : (long)N * N;
-  const long base = (AXIS == 1 ? (long)outer * N * N : (long)outer * N) + c0 + col;
+  constexpr long stride = LAYOUT == 1 ? (AXIS == 1 ? (long)CW : (long)N * CW) : (AXIS == 1 ? (long)N : (long)N * N);
+  const long cbk = c0 / CW;
+  const long base = LAYOUT == 1 ? (AXIS == 1 ? (cbk * N + outer) * N * CW : (cbk * N * N + outer) * CW) + col
+                                : (AXIS == 1 ? (long)outer * N * N : (long)outer * N) + c0 + col;
   const int nbox = box0 ? 1 : bt.K;
   float alpha = 1.0f;
-  if (EPI == 1) {
-    alpha = *alpha_ptr;
-    for (int t = threadIdx.x; t < N * CW; t += THREADS) hit[t] = RC_NONE;
-  }
+  if (EPI == 1) alpha = *alpha_ptr;
+  // EPI 1: first hits of this thread's 24 outputs (rows 25 k1 + r), over the
+  // batch's radii in increasing index order: bit e of hmask says output e has
+  // one, its radius index is byte e of hbyte (24 bytes in 6 words)
+  uint32_t hmask = 0u;
+  uint32_t hbyte[6] = {0u, 0u, 0u, 0u, 0u, 0u};
   for (int k = 0; k < nbox; ++k) {
     float2* box = box0 ? box0 : bt.r[k].work;
     __syncthreads();  // twiddles (k = 0); the previous box's step 2 is done with the exchange
@@ -172,25 +179,26 @@ __global__ void __launch_bounds__(g600::THREADS, 3) k_gen600_cols(float2* box0, 
 #pragma unroll
           for (int q2 = 0; q2 < 3; ++q2) dst[(long)25 * (q1 + 8 * q2) * stride] = u[3 * q1 + q2];
       } else {
-        const int ridx = bt.r[k].ridx;
+        const uint32_t ridx = (uint32_t)bt.r[k].ridx;
 #pragma unroll
-        for (int q1 = 0; q1 < 8; ++q1)
-#pragma unroll
-          for (int q2 = 0; q2 < 3; ++q2) {
-            const int row = 25 * (q1 + 8 * q2) + r;
-            if (is_centre(u[3 * q1 + q2], alpha, bt.zmul) && ridx < hit[row * CW + col])
-              hit[row * CW + col] = (uint8_t)ridx;
+        for (int e = 0; e < 24; ++e) {
+          if (is_centre(u[e], alpha, bt.zmul) && !((hmask >> e) & 1u)) {
+            hmask |= 1u << e;
+            hbyte[e >> 2] |= ridx << (8 * (e & 3));
           }
+        }
       }
     }
   }
-  if (EPI == 1) {
-    __syncthreads();
-    for (int t = threadIdx.x; t < N * CW; t += THREADS) {
-      const int row = t / CW, cc = t % CW;
-      const uint8_t h = hit[t];
-      if (h != RC_NONE) {
-        const long idx = base - col + cc + (long)row * stride;
+  if (EPI == 1 && r < N2 && hmask) {
+    // rc is in the natural layout (AXIS 0: row = a, outer = b); output e =
+    // 3 q1 + q2 is row 25 (q1 + 8 q2) + r
+#pragma unroll
+    for (int e = 0; e < 24; ++e) {
+      if ((hmask >> e) & 1u) {
+        const int row = 25 * (e / 3 + 8 * (e % 3)) + r;
+        const uint8_t h = (uint8_t)(hbyte[e >> 2] >> (8 * (e & 3)));
+        const long idx = ((long)row * N + outer) * N + c0 + col;
         if (h < rc[idx]) rc[idx] = h;
       }
     }
@@ -215,7 +223,7 @@ constexpr int XS = N2 * N2;                // exchange float2 per warp (25 k2 x 
 constexpr size_t RSMEM = (size_t)(N + RW * (XS + N)) * sizeof(float2);  // twiddles, exchange + spectrum row per warp
 }  // namespace g600
 
-template <int MODE>
+template <int MODE, int LAYOUT>
 __global__ void __launch_bounds__(g600::RTHREADS, 2) k_gen600_rows(const float2* in, float2* out, Batch bt,
                                                                   const float* __restrict__ alpha_ptr,
                                                                   const float2* __restrict__ gtw) {
@@ -274,67 +282,83 @@ __global__ void __launch_bounds__(g600::RTHREADS, 2) k_gen600_rows(const float2*
 #pragma unroll
       for (int n1 = 0; n1 < 24; ++n1) u[n1] = ex[lane * N2 + n1];
       dft24<INV>(u, tw);
-      float2* dst = (MODE == 2 ? bt.r[k].work : out) + row * N + lane;
+      if (LAYOUT == 0) {
+        float2* dst = (MODE == 2 ? bt.r[k].work : out) + row * N + lane;
 #pragma unroll
-      for (int q1 = 0; q1 < 8; ++q1)
+        for (int q1 = 0; q1 < 8; ++q1)
 #pragma unroll
-        for (int q2 = 0; q2 < 3; ++q2) dst[25 * (q1 + 8 * q2)] = u[3 * q1 + q2];
+          for (int q2 = 0; q2 < 3; ++q2) dst[25 * (q1 + 8 * q2)] = u[3 * q1 + q2];
+      } else {  // column-block major: (a, b, c) at ((c / 8) N^2 + a N + b) 8 + c mod 8, row = a N + b
+        float2* dst = (MODE == 2 ? bt.r[k].work : out) + row * CW;
+#pragma unroll
+        for (int q1 = 0; q1 < 8; ++q1)
+#pragma unroll
+          for (int q2 = 0; q2 < 3; ++q2) {
+            const int c = 25 * (q1 + 8 * q2) + lane;
+            dst[(long)(c / CW) * N * N * CW + c % CW] = u[3 * q1 + q2];
+          }
+      }
     }
     __syncwarp();  // the exchange is free for the next radius
   }
 }
 
-template <bool INV, int EPI, int AXIS>
+template <bool INV, int EPI, int AXIS, int LAYOUT>
 static cudaError_t g600_attr() {
-  return cudaFuncSetAttribute(k_gen600_cols<INV, EPI, AXIS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  return cudaFuncSetAttribute(k_gen600_cols<INV, EPI, AXIS, LAYOUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)g600::SMEM);
 }
 
 cudaError_t gen600_setup() {
   cudaError_t e;
-  if ((e = g600_attr<true, 0, 0>()) || (e = g600_attr<true, 0, 1>()) || (e = g600_attr<false, 0, 0>()) ||
-      (e = g600_attr<false, 0, 1>()))
+  if ((e = g600_attr<true, 0, 0, 0>()) || (e = g600_attr<true, 0, 1, 0>()) || (e = g600_attr<false, 0, 0, 0>()) ||
+      (e = g600_attr<false, 0, 1, 0>()) || (e = g600_attr<true, 0, 1, 1>()) || (e = g600_attr<true, 1, 0, 1>()))
     return e;
-  if ((e = g600_attr<true, 1, 0>())) return e;
-  for (auto f : {k_gen600_rows<0>, k_gen600_rows<1>, k_gen600_rows<2>})
+  for (auto f : {k_gen600_rows<0, 0>, k_gen600_rows<1, 0>, k_gen600_rows<2, 0>, k_gen600_rows<2, 1>})
     if ((e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g600::RSMEM))) return e;
   return cudaSuccess;
 }
 
 cudaError_t launch_gen600_rows(int mode, const float2* in, float2* out, const Batch& bt, const float* alpha,
-                               const float2* tw, cudaStream_t st) {
+                               const float2* tw, bool cb, cudaStream_t st) {
   const unsigned grid = (unsigned)((long)g600::N * g600::N / g600::RW);
   const int T = g600::RTHREADS;
   const size_t S = g600::RSMEM;
   if (mode == 0)
-    k_gen600_rows<0><<<grid, T, S, st>>>(in, out, bt, alpha, tw);
+    k_gen600_rows<0, 0><<<grid, T, S, st>>>(in, out, bt, alpha, tw);
   else if (mode == 1)
-    k_gen600_rows<1><<<grid, T, S, st>>>(in, out, bt, nullptr, tw);
+    k_gen600_rows<1, 0><<<grid, T, S, st>>>(in, out, bt, nullptr, tw);
+  else if (cb)
+    k_gen600_rows<2, 1><<<grid, T, S, st>>>(in, nullptr, bt, nullptr, tw);
   else
-    k_gen600_rows<2><<<grid, T, S, st>>>(in, nullptr, bt, nullptr, tw);
+    k_gen600_rows<2, 0><<<grid, T, S, st>>>(in, nullptr, bt, nullptr, tw);
   return cudaGetLastError();
 }
 
-cudaError_t launch_gen600_cols(float2* box0, const Batch& bt, int axis, bool inverse, const float2* tw,
+cudaError_t launch_gen600_cols(float2* box0, const Batch& bt, int axis, bool inverse, bool cb, const float2* tw,
                                cudaStream_t st) {
   const unsigned grid = (unsigned)(g600::N * (g600::N / g600::CW));
   const int T = g600::THREADS;
   const size_t S = g600::SMEM;
-  if (inverse && axis == 1)
-    k_gen600_cols<true, 0, 1><<<grid, T, S, st>>>(box0, bt, nullptr, nullptr, tw);
-  else if (inverse)
-    k_gen600_cols<true, 0, 0><<<grid, T, S, st>>>(box0, bt, nullptr, nullptr, tw);
-  else if (axis == 1)
-    k_gen600_cols<false, 0, 1><<<grid, T, S, st>>>(box0, bt, nullptr, nullptr, tw);
-  else
-    k_gen600_cols<false, 0, 0><<<grid, T, S, st>>>(box0, bt, nullptr, nullptr, tw);
+  if (cb) {  // the radius batch's b-axis inverse
+    if (box0 || axis != 1 || !inverse) return cudaErrorInvalidValue;
+    k_gen600_cols<true, 0, 1, 1><<<grid, T, S, st>>>(nullptr, bt, nullptr, nullptr, tw);
+  } else if (inverse && axis == 1) {
+    k_gen600_cols<true, 0, 1, 0><<<grid, T, S, st>>>(box0, bt, nullptr, nullptr, tw);
+  } else if (inverse) {
+    k_gen600_cols<true, 0, 0, 0><<<grid, T, S, st>>>(box0, bt, nullptr, nullptr, tw);
+  } else if (axis == 1) {
+    k_gen600_cols<false, 0, 1, 0><<<grid, T, S, st>>>(box0, bt, nullptr, nullptr, tw);
+  } else {
+    k_gen600_cols<false, 0, 0, 0><<<grid, T, S, st>>>(box0, bt, nullptr, nullptr, tw);
+  }
   return cudaGetLastError();
 }
 
 cudaError_t launch_gen600_cols_a_test(const Batch& bt, uint8_t* rc, const float* alpha, const float2* tw,
                                       cudaStream_t st) {
   const unsigned grid = (unsigned)(g600::N * (g600::N / g600::CW));
-  k_gen600_cols<true, 1, 0><<<grid, g600::THREADS, g600::SMEM, st>>>(nullptr, bt, rc, alpha, tw);
+  k_gen600_cols<true, 1, 0, 1><<<grid, g600::THREADS, g600::SMEM, st>>>(nullptr, bt, rc, alpha, tw);
   return cudaGetLastError();
 }
 

@@ -272,19 +272,21 @@ struct GenPlan {
   int nst;        // stages
   int radix[16];  // radix of each stage (8, 4, 2, 3 or 5)
 };
-// Register-resident b- and a-axis passes for N = 600 (kernels_gen600.cu):
-// 600 = 24 x 25, one shared-memory exchange per line.  Same arguments and
-// results (to rounding) as launch_gen_cols / launch_gen_cols_a_test; twiddles:
-// the plain table of the shared-memory family.
+// Register-resident passes for N = 600 (kernels_gen600.cu): 600 = 24 x 25,
+// one shared-memory exchange per line; twiddles: the plain table of the
+// shared-memory family.  cb: the radius batch's work boxes in the
+// column-block-major layout ((c / 8) N + a) N + b) 8 + c mod 8 (rows mode 2
+// writes it, the b-axis inverse and the a-axis test pass read it); otherwise
+// natural boxes.  launch_gen600_cols_a_test reads the batch in that layout.
 bool gen600_supported(int N);
 cudaError_t gen600_setup();
-cudaError_t launch_gen600_cols(float2* box0, const Batch& bt, int axis, bool inverse, const float2* tw,
+cudaError_t launch_gen600_cols(float2* box0, const Batch& bt, int axis, bool inverse, bool cb, const float2* tw,
                                cudaStream_t st);
 // rows: mode 0 forward (in -> out, imaginary part times |*alpha|), 1 inverse
 // in place (in == out), 2 inverse of the spectrum times the batch's filters
 // (in = spectrum -> bt.r[k].work)
 cudaError_t launch_gen600_rows(int mode, const float2* in, float2* out, const Batch& bt, const float* alpha,
-                               const float2* tw, cudaStream_t st);
+                               const float2* tw, bool cb, cudaStream_t st);
 cudaError_t launch_gen600_cols_a_test(const Batch& bt, uint8_t* rc, const float* alpha, const float2* tw,
                                       cudaStream_t st);
 bool gen_supported(int N);
