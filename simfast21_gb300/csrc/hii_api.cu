@@ -370,6 +370,10 @@ static int prologue_args(sf21_hii_ctx* c, double z, int kind, PrologueArgs* pa) 
   } else {
     CTX_FAIL(c, SF21_E_ARG, "unknown src_kind %d", kind);
   }
+  pa->rf = rrec_fast_prepare(pa->rec1, pa->dvv, pa->v_norm, pa->r2, pa->r3);
+  const sd_t resid[3] = {pa->c_resid, pa->one_plus_z_cubed, pa->g_h};
+  pa->pf_resid = prod_fast_prepare(resid, 3);
+  pa->pf_src = prod_fast_prepare(pa->src_mul, pa->n_src_mul);
   return SF21_OK;
 }
 

@@ -14,26 +14,6 @@ namespace sf21 {
 
 #define SD_ONE (0x3FF0000000000000ULL)
 
-// XHI(ratio), user_functions.c:101-106, operation by operation.
-__device__ __forceinline__ sd_t xhi_sd(sd_t r) {
-  if (sd_is_zero(r)) return 0;
-  const sd_t two_r = sd_ldexp(r, 1);               // 2.*ratio (exact)
-  const sd_t b = sd_add(two_r, SD_ONE);            // 2.*ratio + 1.
-  const sd_t c = sd_mul(b, b);                     // (..)*(..)
-  const sd_t e = sd_mul(sd_ldexp(r, 2), r);        // 4.*ratio*ratio
-  const sd_t g = sd_sqrt_fast(sd_sub(c, e));
-  const sd_t num = sd_sub(b, g);                   // 2.*ratio + 1. - sqrt(..)
-  return sd_div(num, two_r);                       // /(2.*ratio)
-}
-
-// Rrec(overdensity, z), user_functions.c:58-65.
-__device__ __forceinline__ sd_t rrec_sd(float od, const PrologueArgs& pa) {
-  const sd_t rec2 = sd_pow(sd_div_c(sd_from_float(od), pa.r2c), pa.r3);
-  const sd_t q = sd_div(rec2, sd_add(SD_ONE, rec2));
-  const sd_t rec3 = sd_pow4(q);  // pow(.., 4.): exact squaring, correctly rounded like sd_pow
-  return sd_div_c(sd_mul(sd_mul(pa.rec1, rec3), pa.dvv), pa.v_normc);
-}
-
 // Source chain before zeta, left to right as the reference multiplies.
 __device__ __forceinline__ sd_t src_chain(float s, const PrologueArgs& pa) {
   sd_t t = sd_from_float(s);
@@ -52,15 +32,23 @@ k_prologue(long n3, const float* __restrict__ delta, const float* __restrict__ s
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += (long)gridDim.x * blockDim.x) {
     const float d = delta[i];
     const sd_t one_d = sd_add(SD_ONE, sd_from_float(d));  // 1. + density_map[i]
+    // Each quantity takes its fast path (prologue_fast.h), which returns the
+    // exact chain's float for all but about one voxel in 2^21; those voxels
+    // evaluate the exact chain.
     // fresid = XHI((float)((1+d) * 1.881e-7 * pow(1+z,3) * G_H(z)))      (:220-221)
-    sd_t t = sd_mul(one_d, pa.c_resid);
-    t = sd_mul(t, pa.one_plus_z_cubed);
-    t = sd_mul(t, pa.g_h);
-    const float fr = sd_to_float(t);
-    const float fx = sd_to_float(xhi_sd(sd_from_float(fr)));
+    float fr;
+    if (!prod_fast(one_d, pa.pf_resid, &fr))
+      fr = sd_to_float(sd_mul(sd_mul(sd_mul(one_d, pa.c_resid), pa.one_plus_z_cubed), pa.g_h));
+    const float fx = xhi_float(fr);
     // density_map = (float)Rrec((float)(1 + d), z)                          (:222)
-    const float rr = sd_to_float(rrec_sd(sd_to_float(one_d), pa));
-    const float h1 = sd_to_float(src_chain(src[i], pa));
+    const float od = sd_to_float(one_d);
+    float rr;
+    if (!rrec_fast(od, pa.rf, &rr))
+      rr = sd_to_float(rrec_exact(od, pa.r2c, pa.r3, pa.rec1, pa.dvv, pa.v_normc));
+    // source before zeta                                                   (:272-274)
+    const float s = src[i];
+    float h1;
+    if (!prod_fast(sd_from_float(s), pa.pf_src, &h1)) h1 = sd_to_float(src_chain(s, pa));
     rec0[i] = rr;
     fres[i] = fx;
     packed[i] = make_float2(rr, h1);

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "prologue_fast.h"
 #include "sf21_device.cuh"
 #include "softdouble.h"
 
@@ -32,6 +33,8 @@ struct PrologueArgs {
   uint64_t src_mul[6];        // source multipliers before zeta (:273 or :258)
   int n_src_mul;
   sd_divc r2c, v_normc;       // r2 and v_norm as prepared divisors (sd_div_c)
+  RrecFast rf;                // fast-path constants (prologue_fast.h): Rrec,
+  ProdFast pf_resid, pf_src;  // the residual-fraction product, the source product
 };
 
 cudaError_t fft_setup(int N);

@@ -50,3 +50,29 @@ def test_uniform_products_bit_exact(tmp_path):
     r = subprocess.run([exe, "400000", "7"], capture_output=True, text=True)
     cases, bad = map(int, r.stdout.split())
     assert cases > 1_000_000 and bad == 0, r.stdout + r.stderr
+
+
+def test_prologue_fast_paths_match_exact_chains(tmp_path):
+    """prologue_fast.h, the prologue's fast paths, against the exact
+    soft-double chains they stand in for.  Rrec is checked on every float in
+    [0.5, 2) and on sampled densities at six redshifts and four boxes; the
+    residual-fraction and source products and XHI on the same sweeps.  Each
+    fast path must return the exact chain's float whenever it returns.  On
+    realistic inputs it must decline (guard band) for about one input in
+    2^21 only."""
+    cxx = shutil.which("g++")
+    if not cxx:
+        pytest.skip("g++ not available")
+    exe = str(tmp_path / "prologue_fast_check")
+    subprocess.run([cxx, "-O2", "-std=c++17", "-ffp-contract=off",
+                    "-I", os.path.join(ROOT, "simfast21_gb300", "csrc"),
+                    os.path.join(ROOT, "tests", "native", "prologue_fast_check.cpp"), "-o", exe], check=True)
+    r = subprocess.run([exe, "40000", "31"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    stats = {l.split()[0]: list(map(int, l.split()[1:])) for l in r.stdout.strip().splitlines()
+             if not l.startswith("#")}
+    assert stats["rrec_exhaustive"][0] == (1 << 24)
+    for name, (n, bad, fallback) in stats.items():
+        assert n > 0 and bad == 0, (name, stats[name], r.stdout)
+        if name != "rrec_wide":  # wide exponents include results below the float range
+            assert fallback <= max(8, n * 1e-5), (name, stats[name])
