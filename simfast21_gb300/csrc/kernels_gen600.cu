@@ -216,11 +216,18 @@ bool gen600_supported(int N) { return N == g600::N; }
 // MODE 0: forward, imaginary part times |alpha| (the packed prologue box);
 // MODE 1: inverse in place; MODE 2: inverse of the spectrum row times the
 // top-hat filter of each of the batch's K radii, into the K work boxes.
+// In MODE 2 the window takes one value per |k_c| (c and N - c share it): all
+// 32 lanes evaluate the row's N/2 + 1 values once per radius into a
+// shared-memory row, instead of 24 lanes evaluating 25 each.  Same
+// expression, same bits.
 namespace g600 {
 constexpr int RW = 8;                      // rows (warps) per CTA
 constexpr int RTHREADS = 32 * RW;
 constexpr int XS = N2 * N2;                // exchange float2 per warp (25 k2 x stride 25)
-constexpr size_t RSMEM = (size_t)(N + RW * (XS + N)) * sizeof(float2);  // twiddles, exchange + spectrum row per warp
+constexpr int WS = (N / 2 + 2) / 2;        // window row per warp, in float2 (N/2 + 1 floats, padded)
+constexpr int NW = (N / 2 + 32) / 32;      // window values per lane
+// twiddles; per warp: exchange, spectrum row, window row
+constexpr size_t RSMEM = (size_t)(N + RW * (XS + N + WS)) * sizeof(float2);
 }  // namespace g600
 
 template <int MODE, int LAYOUT>
@@ -232,8 +239,9 @@ __global__ void __launch_bounds__(g600::RTHREADS, 2) k_gen600_rows(const float2*
   extern __shared__ float2 gsm[];
   float2* tw = gsm;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  float2* ex = gsm + N + w * (XS + N);
+  float2* ex = gsm + N + w * (XS + N + WS);
   float2* zrow = ex + XS;
+  float* wrow = reinterpret_cast<float*>(zrow + N);
   for (int t = threadIdx.x; t < N; t += RTHREADS) tw[t] = gtw[t];
   __syncthreads();
   const long row = (long)blockIdx.x * RW + w;
@@ -241,24 +249,35 @@ __global__ void __launch_bounds__(g600::RTHREADS, 2) k_gen600_rows(const float2*
   const int nout = MODE == 2 ? bt.K : 1;
   float alpha = 1.0f;
   if (MODE == 0 && alpha_ptr) alpha = fabsf(*alpha_ptr);
-  int kab = 0;
+  float kmag[NW];  // MODE 2: |k| at |k_c| = lane + 32 i (<= N/2) of this row
   if (MODE == 2) {
     const int a = (int)(row / N), b = (int)(row % N);
     const int ka = kfreq(a, N), kb = kfreq(b, N);
-    kab = ka * ka + kb * kb;
+    const int kab = ka * ka + kb * kb;
+#pragma unroll
+    for (int i = 0; i < NW; ++i) {
+      const int kc = lane + 32 * i;
+      kmag[i] = kc <= N / 2 ? sqrtf((float)(kab + kc * kc)) : 0.0f;
+    }
     for (int c = lane; c < N; c += 32) zrow[c] = src[c];
-    __syncwarp();
   }
   for (int k = 0; k < nout; ++k) {
+    if (MODE == 2) {  // the window of radius k at every |k_c|
+      const float dkR = bt.r[k].dkR;
+#pragma unroll
+      for (int i = 0; i < NW; ++i) {
+        const int kc = lane + 32 * i;
+        if (kc <= N / 2) wrow[kc] = w_tophat(dkR * kmag[i]);
+      }
+      __syncwarp();
+    }
     if (lane < N1) {
       float2 y[25];
 #pragma unroll
       for (int n2 = 0; n2 < 25; ++n2) {
         const int c = lane + N1 * n2;
         if (MODE == 2) {
-          const int kc = kfreq(c, N);
-          const float kmag = sqrtf((float)(kab + kc * kc));
-          y[n2] = filter_mul(zrow[c], w_tophat(bt.r[k].dkR * kmag));
+          y[n2] = filter_mul(zrow[c], wrow[c <= N / 2 ? c : N - c]);
         } else {
           float2 v = src[c];
           if (MODE == 0) v.y *= alpha;
