@@ -87,6 +87,41 @@ def test_batched512_sets_match_oracle(hii, oracle_lib):
     fb.close()
 
 
+@pytest.mark.parametrize("z", [7.0, 11.5])
+def test_prologue_512_bit_exact_wide_inputs(hii, oracle_lib, z):
+    """The prologue's fixed-point fast paths and their exact fallbacks
+    (get_HIIbubbles.c:216-225, 272-274) on a 512^3 box of widely spread
+    inputs. 1 + d is log-uniform over [2^-20, 2^20], plus the edge values
+    d = -1, -1 + 2^-24 and 0. Sources are log-uniform over 60 binades, one
+    in eight zero. The fast paths decline about one input in 2^21 (values
+    within 2^-46 of a float rounding midpoint), so the box sends some tens
+    of voxels per path through the exact soft-double chains (counted on the
+    host for these inputs: Rrec 32 and 46, the residual-fraction product 27
+    and 48, XHI's division 38 and 35, the source product 0 and 26 voxels at
+    z = 7 and 11.5). rec0, fresid and the single-cell fill box must be
+    bit-identical with the CPU restatement on every voxel."""
+    w = workload("batched512")
+    N, L, h = w["N"], w["L"], w["hubble"]
+    n3 = N ** 3
+    rng = np.random.default_rng(int(z * 10))
+    one_d = np.exp2(rng.uniform(-20.0, 20.0, n3))
+    delta = (one_d - 1.0).astype(np.float32)
+    delta[:3] = [-1.0, np.float32(-1.0 + 2.0 ** -24), 0.0]
+    sfrd = np.exp2(rng.uniform(-40.0, 20.0, n3)).astype(np.float32)
+    sfrd[rng.random(n3) < 0.125] = 0.0
+    delta, sfrd = delta.reshape((N,) * 3), sfrd.reshape((N,) * 3)
+    st = w["sets"][0]
+    fb = hii.FilterBank(N, L, h, [st])
+    rec0, fres, fill0 = fb.prologue(z, delta, sfrd)
+    fb.close()
+    ex = _prologue(oracle_lib, N, L, h, st, z, delta, sfrd)
+    for name, got, want in (("rec0", rec0, ex["rec0"]), ("fresid", fres, ex["fresid"]),
+                            ("fill0", fill0, ex["fill0"])):
+        g, wv = got.reshape(-1).view(np.uint32), np.asarray(want).reshape(-1).view(np.uint32)
+        bad = np.flatnonzero(g != wv)
+        assert bad.size == 0, (name, bad[:8], delta.reshape(-1)[bad[:8]], sfrd.reshape(-1)[bad[:8]])
+
+
 def _two_inputs(N, L):
     w1 = synth.Workload(N=N, L=L, zs=[7.0], zeta=30.0, Rmax=L / 4, factor=1.05, seed=31)
     w2 = synth.Workload(N=N, L=L, zs=[8.5], zeta=30.0, Rmax=L / 4, factor=1.05, seed=32)
