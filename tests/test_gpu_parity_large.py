@@ -9,6 +9,9 @@
   outcome no decision within the tolerance band can change, the remaining
   voxels hold one of the two admissible values, and the first-hit radius lies
   within the FP64 bounds (get_HIIbubbles.c:298-471).
+* The prologue at 512^3 on wide-range densities and sources: rec0, fresid
+  and the single-cell fill bit-identical with the oracle, including the
+  voxels that the fixed-point fast paths hand to the exact chains.
 * The device entry point's CUDA graph: captured, replayed, updated across
   redshifts, input buffers and output buffers, and with the graph off or
   per-kernel timing on -- bit-identical with the host-buffer entry point.
