@@ -12,8 +12,8 @@
 // L2 holds: the a-axis pass reads the b-axis output from L2 (ld.global.cg),
 // and once a tile's lines have been read they are dropped from L2 without a
 // write-back (discard.global.L2: the values are dead).  Per voxel and radius
-// the DRAM sees the c-axis pass's write and the b-axis pass's read -- the
-// north-star "one HBM round trip per radius" -- instead of two (ncu, K = 8:
+// the DRAM sees the c-axis pass's write and the b-axis pass's read -- one
+// HBM round trip per radius -- instead of two (ncu, K = 8:
 // this launch reads the K boxes once and writes almost nothing, at 256^3 and
 // at 512^3).
 //

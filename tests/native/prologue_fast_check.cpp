@@ -92,7 +92,7 @@ static void check_prod(Stat& s, sd_t x, const ProdFast& k, const sd_t* ks, int n
 }
 
 static void check_xhi(Stat& s, float ratio) {
-  // the fast division's own verdict, for the fallback count
+  // the fast division's own decision, for the fallback count
   const sd_t r = sd_from_float(ratio);
   const sd_t two_r = sd_ldexp(r, 1);
   const sd_t b = sd_add(two_r, 0x3FF0000000000000ULL);

@@ -17,7 +17,7 @@ from simfast21_gb300 import params as P, synth
 
 pytestmark = pytest.mark.gpu
 
-TOL_BAND = 1e-5   # relative distance of h/d from 1 (spec tolerance band)
+TOL_BAND = 1e-5   # relative distance of h/d from 1 (the parity bar's tolerance band)
 TOL_FIELD = 1e-5  # filtered fields, relative to the field's max |value|
 
 
