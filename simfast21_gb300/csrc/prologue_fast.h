@@ -200,7 +200,7 @@ SD_HD bool rrec_fast(float od, const RrecFast& k, float* out) {
   const sd_i128 W = (sd_i128)k.r3 * e + (((sd_i128)k.r3 * dfrac) >> 62);
   const sd_i128 V = -W;
   const int nv = (int)(V >> 63);
-  const uint64_t f = (uint64_t)(V - ((sd_i128)nv << 63));  // Q.63
+  const uint64_t f = (uint64_t)(V - (sd_i128)nv * ((sd_i128)1 << 63));  // Q.63 (nv may be negative)
 
   // 2^f = 2^(j2/128) e^x, x = (f - j2/128) ln 2 < 2^-7.5, series to x^6
   // (remainder < 2^-65).  U in Q.62, [1, 2); relative error (the error of w
